@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark of the batched ray-casting path on GB300.
+
+Default workload: one particle-filter update -- 4,000 particles x 61 beams
+over 270 degrees on a seeded 2048x2048 corridor map at 0.05 m/px, ray
+marching to 200 px, a 201x201 float64 sensor table -- through the fused
+cast + sensor-model call (calc_range_repeat_angles_eval_sensor_model).
+
+  value  rays/s with inputs resident in HBM, CUDA-event time of the fused
+         kernel per step, L2 flushed (a 256 MiB write) before every step.
+  e2e    the same call through the public Python API with host (pinned)
+         numpy buffers: H2D of poses, angles and observations, the kernel
+         and the D2H of the weights inside the timed region.
+
+Other workloads (--workload): plain (cast to ranges, then the separate
+sensor model), batch (32 uneven filters in one persistent launch),
+cddt (1M queries, td 108, 2048^2 map), rect_disk (10k BL/RM queries, 512^2).
+
+--impl reference times the reference algorithm on the host cores instead
+(the C restatement in oracle/, all threads).  Multi-GPU: every rank runs
+its own replica of the workload (weak scaling); rank 0 reports.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rays/s & particle updates/s, batched & learned vs plain GPU march, fixed error"
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- distributed
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend=backend)
+    return rank, ws, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else torch.device("cpu")
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------- workloads
+def build_pf(rl, W, args):
+    wl = W.particle_filter_step()
+    omap = rl.PyOMap(np.ascontiguousarray(wl.occ.T))
+    omap.set_world(*wl.world[:4])
+    method = rl.PyRayMarchingGPU(omap, wl.max_range)
+    method.set_sensor_model(wl.table)
+    return wl, omap, method
+
+
+def cpu_reference_pf(wl, world, steps, warmup, budget_s, nthreads):
+    """The reference algorithm (C restatement, oracle/) on the host cores: full
+    particle-filter steps until `budget_s` seconds or `steps` steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build(reference=False)
+    ref = O.OracleMethod(wl.occ, "rm", wl.max_range, world=world)
+    ref.set_sensor_model(wl.table)
+    for _ in range(max(warmup, 0)):
+        ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=nthreads)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=nthreads)
+        done += 1
+        el = time.perf_counter() - t0
+        if done >= steps or el >= budget_s:
+            break
+    rays = done * len(wl.ins) * len(wl.angles)
+    return rays / el, done, el
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU implementation on the host cores."""
+    from range_libc_gb300 import workloads as W
+    rank, ws, dist = dist_init()
+    if rank != 0:
+        return 0
+    wl = W.particle_filter_step()
+    world = tuple(float(np.float32(v)) for v in (wl.world[0], wl.world[1], wl.world[2], wl.world[3], 0.0, 1.0))
+    nthreads = os.cpu_count() or 1
+    val, done, el = cpu_reference_pf(wl, world, args.steps, args.warmup, budget_s=60.0, nthreads=nthreads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": 0,
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
+        "config": {"workload": "particle-filter step, corridor 2048^2 @0.05 m/px, 4000 particles x 61 beams, "
+                               "RM max_range 200 px, 201x201 sensor table, fused cast+sensor model",
+                   "particles": len(wl.ins), "beams": len(wl.angles)},
+        "particle_updates_per_s": val / len(wl.angles),
+        "cpu_baseline": {"value": val, "unit": "rays/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{done} full steps ({len(wl.ins)}x{len(wl.angles)} rays each)"},
+        "e2e": {"value": val, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="fused", choices=["fused", "plain"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--out", default=None, help="also write the JSON line to this file")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import range_libc_gb300.range_libc as rl
+    from range_libc_gb300 import workloads as W
+
+    rank, ws, dist = dist_init()
+    dev_index = torch.cuda.current_device()
+    dev = torch.device("cuda", dev_index)
+    stream = torch.cuda.current_stream(dev)
+
+    wl, omap, method = build_pf(rl, W, args)
+    n, na = len(wl.ins), len(wl.angles)
+    rays_per_step = n * na
+    ins = torch.from_numpy(wl.ins).to(dev)
+    angles = torch.from_numpy(wl.angles).to(dev)
+    obs = torch.from_numpy(wl.obs).to(dev)
+    weights = torch.empty(n, dtype=torch.float64, device=dev)
+    ranges = torch.empty(rays_per_step, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        if args.workload == "fused":
+            method.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs, weights)
+            return 1
+        method.calc_range_repeat_angles(ins, angles, ranges)
+        method.eval_sensor_model(obs, ranges, weights, na, n)
+        return 2
+
+    # autotune the schedule on this workload, then warm up
+    if args.workload == "fused":
+        rl._lib.call("rlc_method_autotune", method.handle, ins.data_ptr(), angles.data_ptr(), obs.data_ptr(),
+                     weights.data_ptr(), n, na, rl._stream_of(ins))
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing: CUDA events around each step, L2 flushed before it
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(dev_index)
+    launches = 0
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        starts[k].record(stream)
+        launches += step()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clk = clocks.stop()
+    per_step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = max_over_ranks(dist, sum(per_step_ms))
+    value = ws * rays_per_step * args.steps / (total_ms / 1e3)
+
+    # ---- end to end through the public API with pinned host buffers
+    h_ins = torch.from_numpy(wl.ins).pin_memory().numpy()
+    h_ang = torch.from_numpy(wl.angles).pin_memory().numpy()
+    h_obs = torch.from_numpy(wl.obs).pin_memory().numpy()
+    h_w = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    h_r = torch.empty(rays_per_step, dtype=torch.float32).pin_memory().numpy()
+
+    def step_host():
+        if args.workload == "fused":
+            method.calc_range_repeat_angles_eval_sensor_model(h_ins, h_ang, h_obs, h_w)
+        else:
+            method.calc_range_repeat_angles(h_ins, h_ang, h_r)
+            method.eval_sensor_model(h_obs, h_r, h_w, na, n)
+
+    for _ in range(args.warmup):
+        step_host()
+    e2e_s = 0.0
+    barrier(dist)
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_host()                       # synchronous: results are in h_w on return
+        e2e_s += time.perf_counter() - t0
+    barrier(dist)
+    e2e_s = max_over_ranks(dist, e2e_s)
+    e2e = ws * rays_per_step * args.steps / e2e_s
+    h2d = wl.ins.nbytes + wl.angles.nbytes + wl.obs.nbytes
+    d2h = n * 8
+    if args.workload == "plain":
+        h2d += wl.obs.nbytes + rays_per_step * 4
+        d2h += rays_per_step * 4
+
+    # correctness check of the timed configuration against the host path
+    torch.cuda.synchronize()
+    dev_w = weights.cpu().numpy()
+    if not np.array_equal(dev_w, h_w):
+        raise SystemExit("bench: device and host paths disagree")
+
+    # ---- roofline of the dominant kernel (the fused cast + sensor model)
+    total_steps = method.count_steps(wl.ins, wl.angles)
+    # per particle 12 B pose + 8 B weight; per ray one 8 B table read + 4 B per distance-transform read
+    alg_bytes = n * (12 + 8) + rays_per_step * 8 + 4 * total_steps
+    kern_s = (sum(per_step_ms) / args.steps) / 1e3
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / kern_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_source": f"hbm_gbs burst ({peak_kind})",
+                "algorithmic_bytes_per_launch": alg_bytes, "mean_march_steps_per_ray": total_steps / rays_per_step,
+                "kernel": "k_fused (cast + sensor model)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        v1, d1, e1 = cpu_reference_pf(wl, omap.world, steps=1000, warmup=1, budget_s=10.0, nthreads=nthreads)
+        cpu = {"value": v1, "unit": "rays/s", "cores": nthreads, "kind": "port",
+               "sample": f"{d1} full steps ({n}x{na} rays each) in {e1:.1f} s, oracle/ C restatement, "
+                         f"{nthreads} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
+            "config": {"workload": f"particle-filter step ({args.workload}): corridor 2048^2 @0.05 m/px, "
+                                   f"{n} particles x {na} beams over 270 deg, RM max_range 200 px, "
+                                   f"201x201 f64 sensor table",
+                       "particles": n, "beams": na, "map": "2048x2048 corridor, seed 2000",
+                       "l2": "flushed before every step (256 MiB write)",
+                       "schedule": dict(zip(("dt_layout", "block"), method.schedule()))},
+            "particle_updates_per_s": value / na,
+            "e2e": {"value": e2e, "unit": "rays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "particle_updates_per_s": e2e / na},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        s = json.dumps(line)
+        print(s)
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(s + "\n")
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

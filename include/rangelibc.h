@@ -1,0 +1,200 @@
+/*
+ * rangelibc.h -- C ABI of the GB300 (sm_103a) ray-casting library.
+ *
+ * Drop-in boundary for range_libc's batched hot path (kctess5/range_libc).
+ * Every entry point below replaces one method of the reference's C++
+ * `ranges::RangeMethod` family (includes/RangeLib.h) or of its CUDA helper
+ * `RayMarchingCUDA` (includes/CudaRangeLib.h, includes/kernels.cu); the
+ * citation is given beside each declaration.  The C++ classes of
+ * include/RangeLib.h and the Python module range_libc_gb300.range_libc are
+ * thin layers over these functions.
+ *
+ * Conventions
+ *  - Status: every function returns RLC_OK (0) or an RLC_ERR_* code, and
+ *    rlc_last_error() gives a message for the calling thread.  Nothing
+ *    throws across the ABI.
+ *  - Grid layout: occ[x * height + y] != 0 marks cell (x, y) occupied, x <
+ *    width, y < height (the reference's OMap::grid[x][y]).
+ *  - Pointers: by default every array argument is HOST memory and the call is
+ *    synchronous (results are in place on return), like the reference.  With
+ *    RLC_DEVICE_PTRS every array argument is DEVICE memory and the call is
+ *    asynchronous on `stream` (NULL = the legacy default stream).
+ *  - World frame: calls without RLC_NO_WORLD apply the reference's ROS
+ *    world->grid transform (RangeLib.h:439-480): scale, rotate, then
+ *    calc_range(y, x, theta) with theta = -theta_world - world_angle - 3*pi/2,
+ *    and ranges multiplied by world_scale.
+ *  - Array layouts: poses ins[n][3] = (x, y, theta) float32; angles[na];
+ *    ranges of repeat-angle calls are particle-major outs[i * na + a];
+ *    sensor tables are K x K float64 row-major, table[r * K + d].
+ *  - A map's occupancy is immutable once created; methods share its device
+ *    data (reference-counted, so a map may be destroyed before its methods)
+ *    and copy its world parameters at creation, so like the reference's
+ *    methods (which take OMap by value) they do not see later
+ *    rlc_map_set_world calls.  A method handle must not be used by two host
+ *    threads at once.
+ *  - No CPU fallback: with no usable GPU every call returns RLC_ERR_CUDA.
+ */
+#ifndef RANGELIBC_H
+#define RANGELIBC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define RLC_API __attribute__((visibility("default")))
+#else
+#define RLC_API
+#endif
+
+#define RLC_ABI_VERSION 1
+
+typedef struct rlc_map rlc_map;
+typedef struct rlc_method rlc_method;
+typedef struct rlc_batch rlc_batch;
+
+enum rlc_status {
+    RLC_OK = 0,
+    RLC_ERR_ARG = 1,      /* invalid argument (null pointer, size, kind) */
+    RLC_ERR_CUDA = 2,     /* CUDA runtime error (message in rlc_last_error) */
+    RLC_ERR_STATE = 3,    /* call not valid in the handle's state (e.g. no sensor model) */
+    RLC_ERR_NOMEM = 4     /* device allocation failed */
+};
+
+enum rlc_kind {
+    RLC_BL = 0,           /* BresenhamsLine,   RangeLib.h:691-772 */
+    RLC_RM = 1,           /* RayMarching,      RangeLib.h:922-969 */
+    RLC_CDDT = 2,         /* CDDTCast,         RangeLib.h:971-1770 */
+    RLC_PCDDT = 3,        /* CDDTCast + prune(max_range) (PyCDDTCast + prune, RangeLibc.pyx:253-262) */
+    RLC_RMGPU = 4         /* RayMarchingGPU,   RangeLib.h:774-920 (same kernels as RLC_RM) */
+};
+
+enum rlc_flags {
+    RLC_DEVICE_PTRS = 1u, /* array arguments are device pointers; asynchronous on `stream` */
+    RLC_NO_WORLD = 2u     /* calc_range_many only: raw calc_range(x, y, theta) per row, no
+                             world transform (RayMarchingGPU::calc_range_many, RangeLib.h:835-846) */
+};
+
+/* kernel-reported conditions, read with rlc_method_device_flags */
+enum rlc_device_flag {
+    RLC_FLAG_BL_BOUND = 1u,       /* Bresenham loop bound hit (|coordinate| > 2^24) */
+    RLC_FLAG_WRAP_BOUND = 2u,     /* CDDT heading wrap bound hit (|heading| > ~6e5 rad) */
+    RLC_FLAG_CDDT_PAST_END = 4u,  /* query equal to a bin's last zero point (reference reads past the bin) */
+    RLC_FLAG_NAN_INDEX = 8u       /* NaN range or observation mapped to sensor bin 0 */
+};
+
+/* ---- library ---------------------------------------------------------- */
+RLC_API int rlc_abi_version(void);
+RLC_API const char* rlc_last_error(void);
+/* Number of CUDA devices visible (0 when none); never fails. */
+RLC_API int rlc_device_count(void);
+
+/* ---- maps: OMap (RangeLib.h:121-322) ---------------------------------- */
+/* OMap(int w, int h) + grid fill (RangeLib.h:143-156; PyOMap(ndarray), RangeLibc.pyx:140-145). */
+RLC_API int rlc_map_create(const uint8_t* occ, int width, int height, rlc_map** out);
+/* World parameters of the ROS conversion (RangeLib.h:134-141; RangeLibc.pyx:160-180). */
+RLC_API int rlc_map_set_world(rlc_map* map, float scale, float angle, float origin_x, float origin_y,
+                              float sin_angle, float cos_angle);
+RLC_API int rlc_map_destroy(rlc_map* map);
+/* OMap::width/height (RangeLibc.pyx:191-197). */
+RLC_API int rlc_map_size(const rlc_map* map, int* width, int* height);
+/* OMap::grid export (host, occ[x * height + y]). */
+RLC_API int rlc_map_occupancy(rlc_map* map, uint8_t* occ_out);
+/* DistanceTransform(OMap*) (RangeLib.h:345-373), computed on the device; host export. */
+RLC_API int rlc_map_distance_transform(rlc_map* map, float* dt_out);
+/* OMap::make_edge_map(true) (RangeLib.h:293-312); host export. */
+RLC_API int rlc_map_edge_map(rlc_map* map, uint8_t* edge_out);
+
+/* ---- range methods ----------------------------------------------------- */
+/* BresenhamsLine(OMap, mr) / RayMarching(OMap, mr) / CDDTCast(OMap, mr, td) /
+ * RayMarchingGPU(OMap, mr) constructors.  theta_disc is used by CDDT only.
+ * The CDDT table is built on the device. */
+RLC_API int rlc_method_create(rlc_map* map, int kind, float max_range, unsigned theta_disc, rlc_method** out);
+/* CDDT constructor with caller-supplied cosines and sines of the td discrete
+ * angles i * (2*pi/td) (as float).  Used to pin a table to another host's libm. */
+RLC_API int rlc_method_create_cddt_trig(rlc_map* map, int kind, float max_range, unsigned theta_disc,
+                                        const float* cos_tab, const float* sin_tab, rlc_method** out);
+RLC_API int rlc_method_destroy(rlc_method* m);
+RLC_API int rlc_method_info(const rlc_method* m, int* kind, float* max_range, unsigned* theta_disc);
+/* Kernel-reported conditions since the last call (see rlc_device_flag); clears them. */
+RLC_API int rlc_method_device_flags(rlc_method* m, unsigned* flags);
+
+/* CDDTCast::prune(float max_range) (RangeLib.h:1176-1283), on the device. */
+RLC_API int rlc_cddt_prune(rlc_method* m, float max_range);
+/* CDDT table access (compressed_lut, lut_translations; RangeLib.h:1742-1748). */
+RLC_API int rlc_cddt_table_size(rlc_method* m, int64_t* num_bins, int64_t* num_zeros);
+RLC_API int rlc_cddt_table_export(rlc_method* m, int* widths, float* trans, int64_t* bin_len, float* zeros);
+/* Replace the table (same theta_disc and bin counts), e.g. one exported from the reference. */
+RLC_API int rlc_cddt_table_load(rlc_method* m, const float* trans, const int64_t* bin_len, const float* zeros,
+                                int64_t num_zeros);
+
+/* ---- queries ----------------------------------------------------------- */
+/* RangeMethod::calc_range(x, y, heading) (virtual, RangeLib.h:419): one ray in grid space. */
+RLC_API int rlc_calc_range(rlc_method* m, float x, float y, float heading, float* out);
+/* RangeMethod::numpy_calc_range (RangeLib.h:439-480; RayMarchingCUDA::numpy_calc_range,
+ * kernels.cu:245-260).  With RLC_NO_WORLD: RayMarchingGPU::calc_range_many (kernels.cu:232-243). */
+RLC_API int rlc_calc_range_many(rlc_method* m, const float* ins, float* outs, int n, unsigned flags,
+                                void* stream);
+/* RangeMethod::numpy_calc_range_angles (RangeLib.h:482-520; kernels.cu:263-279). */
+RLC_API int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* angles, float* outs,
+                                         int n, int num_angles, unsigned flags, void* stream);
+/* RangeMethod::set_sensor_model (RangeLib.h:523-532; RayMarchingCUDA::set_sensor_table, kernels.cu:224-229). */
+RLC_API int rlc_set_sensor_model(rlc_method* m, const double* table, int table_width);
+/* RangeMethod::eval_sensor_model (RangeLib.h:533-555). */
+RLC_API int rlc_eval_sensor_model(rlc_method* m, const float* obs, const float* ranges, double* outs,
+                                  int rays_per_particle, int particles, unsigned flags, void* stream);
+/* RangeMethod::calc_range_repeat_angles_eval_sensor_model (RangeLib.h:558-612); fused on the
+ * device, replacing the unimplemented RayMarchingCUDA version (kernels.cu:281-315). */
+RLC_API int rlc_calc_range_repeat_angles_eval_sensor_model(rlc_method* m, const float* ins,
+                                                           const float* angles, const float* obs,
+                                                           double* weights, int n, int num_angles,
+                                                           unsigned flags, void* stream);
+
+/* Parity mode (testing): per-ray (cos, sin) pairs, ray-indexed like the outputs of the
+ * next query calls (BL and RM).  trig = NULL restores device sincosf.  `count` rays,
+ * host pointer; the array is copied. */
+RLC_API int rlc_method_set_trig_override(rlc_method* m, const float* trig, int64_t count);
+
+/* Measurement: total march steps of the rays of a repeat-angle call (RM: distance-transform
+ * reads; BL: cells tested), for stating algorithmic bytes.  Synchronous; RM and BL only. */
+RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n, int num_angles,
+                            unsigned flags, int64_t* total_steps);
+
+/* ---- tuning ------------------------------------------------------------ */
+/* Distance-transform layout for RM: 0 = linear x-major, 1 = 8x8 tiles; -1 = autotune on
+ * the next fused call.  block = threads per block of the fused kernel (0 = default). */
+RLC_API int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block);
+RLC_API int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_block);
+/* Time the schedule candidates on a workload (device pointers) and keep the fastest. */
+RLC_API int rlc_method_autotune(rlc_method* m, const float* d_ins, const float* d_angles, const float* d_obs,
+                                double* d_weights, int n, int num_angles, void* stream);
+
+/* ---- batched multi-filter particle update (no reference counterpart) --------
+ * Many independent filters, each a method (RM or BL or CDDT) with its own map, poses,
+ * beams, observation and sensor table, run as one persistent launch that draws
+ * particle tiles from a device queue; rlc_batch_run replays it as a CUDA graph. */
+typedef struct rlc_filter_desc {
+    rlc_method* method;   /* sensor model must be set */
+    const float* ins;     /* device [n_particles][3] world poses */
+    const float* angles;  /* device [n_angles] */
+    const float* obs;     /* device [n_angles] world ranges */
+    float* ranges;        /* device [n_particles * n_angles] pixel ranges, or NULL */
+    double* weights;      /* device [n_particles] */
+    int n_particles;
+    int n_angles;
+} rlc_filter_desc;
+
+/* The methods must outlive the batch.  block = threads per block (0 = 256). */
+RLC_API int rlc_batch_create(const rlc_filter_desc* filters, int n_filters, int block, rlc_batch** out);
+RLC_API int rlc_batch_run(rlc_batch* b, void* stream);
+RLC_API int rlc_batch_destroy(rlc_batch* b);
+/* rays = sum of n_particles * n_angles; tiles = work items of the device queue */
+RLC_API int rlc_batch_info(const rlc_batch* b, int64_t* rays, int64_t* tiles);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RANGELIBC_H */

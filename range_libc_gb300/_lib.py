@@ -1,0 +1,121 @@
+"""Loader of the CUDA library (``_build/librangelibc_gb300.so``) and its C ABI.
+
+The library is the only compute path: there is no CPU fallback.  If the
+shared object is missing it is built with nvcc (``build.py``); if that is not
+possible, or the ABI does not match, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from .build import LIB_PATH as _LIB_PATH, build as _build_library
+
+RLC_OK, RLC_ERR_ARG, RLC_ERR_CUDA, RLC_ERR_STATE, RLC_ERR_NOMEM = range(5)
+RLC_BL, RLC_RM, RLC_CDDT, RLC_PCDDT, RLC_RMGPU = range(5)
+RLC_DEVICE_PTRS = 1
+RLC_NO_WORLD = 2
+ABI_VERSION = 1
+
+_f32p = C.POINTER(C.c_float)
+_f64p = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+_i32p = C.POINTER(C.c_int)
+_i64p = C.POINTER(C.c_int64)
+_u32p = C.POINTER(C.c_uint)
+_vp = C.c_void_p
+
+
+class RangeLibError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[rlc status {code}] {message}")
+        self.code = code
+
+
+class FilterDesc(C.Structure):
+    _fields_ = [
+        ("method", _vp), ("ins", _vp), ("angles", _vp), ("obs", _vp),
+        ("ranges", _vp), ("weights", _vp), ("n_particles", C.c_int), ("n_angles", C.c_int),
+    ]
+
+
+# name -> (restype, argtypes); every function returns an int status unless noted
+SIGNATURES = {
+    "rlc_abi_version": (C.c_int, []),
+    "rlc_last_error": (C.c_char_p, []),
+    "rlc_device_count": (C.c_int, []),
+    "rlc_map_create": (C.c_int, [_u8p, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "rlc_map_set_world": (C.c_int, [_vp] + [C.c_float] * 6),
+    "rlc_map_destroy": (C.c_int, [_vp]),
+    "rlc_map_size": (C.c_int, [_vp, _i32p, _i32p]),
+    "rlc_map_occupancy": (C.c_int, [_vp, _u8p]),
+    "rlc_map_distance_transform": (C.c_int, [_vp, _f32p]),
+    "rlc_map_edge_map": (C.c_int, [_vp, _u8p]),
+    "rlc_method_create": (C.c_int, [_vp, C.c_int, C.c_float, C.c_uint, C.POINTER(_vp)]),
+    "rlc_method_create_cddt_trig": (C.c_int, [_vp, C.c_int, C.c_float, C.c_uint, _f32p, _f32p, C.POINTER(_vp)]),
+    "rlc_method_destroy": (C.c_int, [_vp]),
+    "rlc_method_info": (C.c_int, [_vp, _i32p, _f32p, _u32p]),
+    "rlc_method_device_flags": (C.c_int, [_vp, _u32p]),
+    "rlc_cddt_prune": (C.c_int, [_vp, C.c_float]),
+    "rlc_cddt_table_size": (C.c_int, [_vp, _i64p, _i64p]),
+    "rlc_cddt_table_export": (C.c_int, [_vp, _i32p, _f32p, _i64p, _f32p]),
+    "rlc_cddt_table_load": (C.c_int, [_vp, _f32p, _i64p, _f32p, C.c_int64]),
+    "rlc_calc_range": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, _f32p]),
+    "rlc_calc_range_many": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_uint, _vp]),
+    "rlc_calc_range_repeat_angles": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_uint, _vp]),
+    "rlc_set_sensor_model": (C.c_int, [_vp, _f64p, C.c_int]),
+    "rlc_eval_sensor_model": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_uint, _vp]),
+    "rlc_calc_range_repeat_angles_eval_sensor_model": (
+        C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_uint, _vp]),
+    "rlc_method_set_trig_override": (C.c_int, [_vp, _f32p, C.c_int64]),
+    "rlc_count_steps": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_uint, _i64p]),
+    "rlc_method_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "rlc_method_get_schedule": (C.c_int, [_vp, _i32p, _i32p]),
+    "rlc_method_autotune": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "rlc_batch_create": (C.c_int, [C.POINTER(FilterDesc), C.c_int, C.c_int, C.POINTER(_vp)]),
+    "rlc_batch_run": (C.c_int, [_vp, _vp]),
+    "rlc_batch_destroy": (C.c_int, [_vp]),
+    "rlc_batch_info": (C.c_int, [_vp, _i64p, _i64p]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """The loaded C ABI (built on first use if the toolkit is present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            path = _LIB_PATH
+            if not os.path.exists(path):
+                _build_library()
+            L = C.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            v = L.rlc_abi_version()
+            if v != ABI_VERSION:
+                raise RuntimeError(f"{path}: ABI version {v}, expected {ABI_VERSION}")
+            _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != RLC_OK:
+        msg = lib().rlc_last_error()
+        raise RangeLibError(rc, msg.decode() if msg else "")
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args))

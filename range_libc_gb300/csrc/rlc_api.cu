@@ -1,0 +1,889 @@
+// C ABI (include/rangelibc.h): handle management, host<->device staging,
+// argument checking and error reporting around the device kernels.
+#include "rangelibc.h"
+#include "rlc_internal.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace rlc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(RLC_ERR_NOMEM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(RLC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CUDA_OR_FAIL(expr, what)                       \
+    do {                                               \
+        cudaError_t _e = (expr);                       \
+        if (_e != cudaSuccess) return cuda_fail(_e, what); \
+    } while (0)
+
+constexpr double kM2Pi = 6.28318530718;   // RangeLib.h:61
+constexpr double kEps = 0.00001;          // RangeLib.h:60
+
+}  // namespace
+
+struct rlc_map {
+    int device = 0;
+    int W = 0, H = 0, TY = 0;
+    float world[6] = {1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f};   // scale, angle, ox, oy, sin, cos
+    uint64_t* d_bits = nullptr;
+    float* d_dt = nullptr;
+    float* d_dt_tiled = nullptr;
+    std::atomic<int> refs{1};
+    std::mutex mu;
+
+    ~rlc_map() {
+        cudaFree(d_bits);
+        cudaFree(d_dt);
+        cudaFree(d_dt_tiled);
+    }
+    // distance transform on first use (RayMarching constructor, RangeLib.h:924)
+    int ensure_dt() {
+        std::lock_guard<std::mutex> lk(mu);
+        if (d_dt) return RLC_OK;
+        size_t n = (size_t)W * H;
+        size_t tiled = (size_t)((W + 7) >> 3) * TY * 64;
+        float* dt = nullptr;
+        float* dtt = nullptr;
+        void* scratch = nullptr;
+        size_t sb = edt_scratch_bytes(W, H);
+        cudaError_t e = cudaMalloc(&dt, (n ? n : 1) * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&dtt, (tiled ? tiled : 1) * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&scratch, sb);
+        if (e == cudaSuccess) e = launch_edt(d_bits, W, H, TY, dt, scratch, sb, 0);
+        if (e == cudaSuccess) e = launch_dt_to_tiled(dt, W, H, dtt, 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+        cudaFree(scratch);
+        if (e != cudaSuccess) {
+            cudaFree(dt);
+            cudaFree(dtt);
+            return cuda_fail(e, "distance transform");
+        }
+        d_dt = dt;
+        d_dt_tiled = dtt;
+        return RLC_OK;
+    }
+    void retain() { refs.fetch_add(1); }
+    void release() {
+        if (refs.fetch_sub(1) == 1) delete this;
+    }
+};
+
+struct rlc_method {
+    rlc_map* map = nullptr;
+    int kind = RLC_RM;        // public kind
+    int dkind = K_RM;         // device kind
+    float mr = 0.0f;
+    unsigned td = 0;
+    WorldDev world{};
+    // CDDT
+    std::vector<int> h_widths;
+    std::vector<float> h_trans, h_cos, h_sin;
+    std::vector<uint32_t> h_slice_base;
+    float td_div_2pi = 0.0f, twopi_div_td = 0.0f;
+    int* d_widths = nullptr;
+    float* d_trans = nullptr;
+    float* d_cos = nullptr;
+    float* d_sin = nullptr;
+    CddtBuild tab;
+    // sensor model
+    double* d_table = nullptr;
+    int K = 0;
+    // staging for host-pointer calls
+    void* d_stage = nullptr;
+    size_t stage_cap = 0;
+    unsigned* d_err = nullptr;
+    float* d_trig = nullptr;
+    int64_t trig_count = 0;
+    // schedule
+    int layout = DT_LINEAR;
+    int fused_block = 256;
+    bool autotune_pending = false;
+
+    ~rlc_method() {
+        cudaFree(d_widths);
+        cudaFree(d_trans);
+        cudaFree(d_cos);
+        cudaFree(d_sin);
+        cudaFree(tab.slice_base);
+        cudaFree(tab.bin_start);
+        cudaFree(tab.zeros);
+        cudaFree(d_table);
+        cudaFree(d_stage);
+        cudaFree(d_err);
+        cudaFree(d_trig);
+        if (map) map->release();
+    }
+
+    CastParams params() const {
+        CastParams p{};
+        p.kind = dkind;
+        p.mr = mr;
+        p.map.W = map->W;
+        p.map.H = map->H;
+        p.map.tiles_y = map->TY;
+        p.map.dt = layout == DT_TILED ? map->d_dt_tiled : map->d_dt;
+        p.map.bits = map->d_bits;
+        p.cddt.td = td;
+        p.cddt.td_div_2pi = td_div_2pi;
+        p.cddt.twopi_div_td = twopi_div_td;
+        p.cddt.widths = d_widths;
+        p.cddt.trans = d_trans;
+        p.cddt.cosv = d_cos;
+        p.cddt.sinv = d_sin;
+        p.cddt.slice_base = tab.slice_base;
+        p.cddt.bin_start = tab.bin_start;
+        p.cddt.zeros = tab.zeros;
+        p.world = world;
+        p.trig = d_trig;
+        p.err = d_err;
+        return p;
+    }
+
+    int stage(size_t bytes, void** out) {
+        if (bytes > stage_cap) {
+            cudaFree(d_stage);
+            d_stage = nullptr;
+            stage_cap = 0;
+            size_t cap = bytes + bytes / 4 + 256;
+            CUDA_OR_FAIL(cudaMalloc(&d_stage, cap), "staging buffer");
+            stage_cap = cap;
+        }
+        *out = d_stage;
+        return RLC_OK;
+    }
+};
+
+namespace {
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+WorldDev world_consts(const float* w) {
+    WorldDev d;
+    d.s = w[0];
+    d.inv_s = (float)(1.0 / (double)w[0]);                          // RangeLib.h:442
+    d.rc = (float)(-1.0 * (double)w[1] - 3.0 * M_PI / 2.0);         // RangeLib.h:450
+    d.ox = w[2];
+    d.oy = w[3];
+    d.sa = w[4];
+    d.ca = w[5];
+    return d;
+}
+
+// Per-slice constants of CDDTCast (RangeLib.h:1007-1061), host libm.
+void cddt_constants(rlc_method* m, const float* cos_tab, const float* sin_tab) {
+    const unsigned td = m->td;
+    const int W = m->map->W, H = m->map->H;
+    m->td_div_2pi = (float)((double)td / kM2Pi);
+    m->twopi_div_td = (float)(kM2Pi / (double)(float)td);
+    m->h_widths.resize(td);
+    m->h_trans.resize(td);
+    m->h_cos.resize(td);
+    m->h_sin.resize(td);
+    m->h_slice_base.resize(td + 1);
+    m->h_slice_base[0] = 0;
+    // (host code is compiled with -ffp-contract=off: plain IEEE float ops)
+    for (unsigned i = 0; i < td; ++i) {
+        const float angle = (float)(int)i * m->twopi_div_td;
+        const float c = cos_tab ? cos_tab[i] : cosf(angle);
+        const float s = sin_tab ? sin_tab[i] : sinf(angle);
+        m->h_cos[i] = c;
+        m->h_sin[i] = s;
+        const float rotated_height = std::fabs((float)W * s) + std::fabs((float)H * c);
+        m->h_widths[i] = (int)(unsigned)std::ceil((double)rotated_height - kEps);
+        const float left_top = (float)H * c;
+        const float right_top = (float)W * s + (float)H * c;
+        const float right_bottom = (float)W * s;
+        const float inner = (right_bottom < right_top) ? right_bottom : right_top;   // std::min
+        const float min_y = (inner < left_top) ? inner : left_top;
+        const double tr = -1.0 * (double)min_y - kEps;
+        m->h_trans[i] = (float)((0.0 < tr) ? tr : 0.0);                            // std::max(0.0, .)
+        m->h_slice_base[i + 1] = m->h_slice_base[i] + (uint32_t)m->h_widths[i];
+    }
+}
+
+int upload(void** d, const void* h, size_t bytes, const char* what) {
+    CUDA_OR_FAIL(cudaMalloc(d, bytes ? bytes : 4), what);
+    if (bytes) CUDA_OR_FAIL(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice), what);
+    return RLC_OK;
+}
+
+int check_method(const rlc_method* m) {
+    if (!m) return fail(RLC_ERR_ARG, "null method handle");
+    return RLC_OK;
+}
+
+int finish_launch(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    return RLC_OK;
+}
+
+int check_trig(const rlc_method* m, long long rays) {
+    if (m->d_trig && m->trig_count < rays)
+        return fail(RLC_ERR_ARG, "trig override holds %lld rays, call needs %lld", (long long)m->trig_count, rays);
+    return RLC_OK;
+}
+
+}  // namespace
+
+// ======================================================================= ABI
+extern "C" {
+
+int rlc_abi_version(void) { return RLC_ABI_VERSION; }
+
+const char* rlc_last_error(void) { return g_err.c_str(); }
+
+int rlc_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int rlc_map_create(const uint8_t* occ, int width, int height, rlc_map** out) {
+    if (!out) return fail(RLC_ERR_ARG, "null output handle");
+    *out = nullptr;
+    if (width <= 0 || height <= 0) return fail(RLC_ERR_ARG, "map size %dx%d must be positive", width, height);
+    if (!occ) return fail(RLC_ERR_ARG, "null occupancy grid");
+    if ((long long)width * height > (1ll << 31)) return fail(RLC_ERR_ARG, "map of %dx%d cells is too large", width, height);
+    rlc_map* m = new rlc_map();
+    cudaGetDevice(&m->device);
+    m->W = width;
+    m->H = height;
+    m->TY = (height + 7) >> 3;
+    size_t n = (size_t)width * height;
+    size_t words = (size_t)((width + 7) >> 3) * m->TY;
+    uint8_t* d_occ = nullptr;
+    cudaError_t e = cudaMalloc(&d_occ, n);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_bits, words * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMemcpy(d_occ, occ, n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_pack_bits(d_occ, width, height, m->d_bits, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    cudaFree(d_occ);
+    if (e != cudaSuccess) {
+        delete m;
+        return cuda_fail(e, "map upload");
+    }
+    *out = m;
+    return RLC_OK;
+}
+
+int rlc_map_set_world(rlc_map* map, float scale, float angle, float ox, float oy, float sin_angle,
+                      float cos_angle) {
+    if (!map) return fail(RLC_ERR_ARG, "null map handle");
+    map->world[0] = scale;
+    map->world[1] = angle;
+    map->world[2] = ox;
+    map->world[3] = oy;
+    map->world[4] = sin_angle;
+    map->world[5] = cos_angle;
+    return RLC_OK;
+}
+
+int rlc_map_destroy(rlc_map* map) {
+    if (map) map->release();
+    return RLC_OK;
+}
+
+int rlc_map_size(const rlc_map* map, int* width, int* height) {
+    if (!map) return fail(RLC_ERR_ARG, "null map handle");
+    if (width) *width = map->W;
+    if (height) *height = map->H;
+    return RLC_OK;
+}
+
+int rlc_map_occupancy(rlc_map* map, uint8_t* occ_out) {
+    if (!map || !occ_out) return fail(RLC_ERR_ARG, "null argument");
+    size_t n = (size_t)map->W * map->H;
+    uint8_t* d = nullptr;
+    CUDA_OR_FAIL(cudaMalloc(&d, n), "occupancy export");
+    cudaError_t e = launch_unpack_bits(map->d_bits, map->W, map->H, map->TY, d, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(occ_out, d, n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return finish_launch(e, "occupancy export");
+}
+
+int rlc_map_distance_transform(rlc_map* map, float* dt_out) {
+    if (!map || !dt_out) return fail(RLC_ERR_ARG, "null argument");
+    int rc = map->ensure_dt();
+    if (rc) return rc;
+    CUDA_OR_FAIL(cudaMemcpy(dt_out, map->d_dt, (size_t)map->W * map->H * sizeof(float), cudaMemcpyDeviceToHost),
+                 "distance transform export");
+    return RLC_OK;
+}
+
+int rlc_map_edge_map(rlc_map* map, uint8_t* edge_out) {
+    if (!map || !edge_out) return fail(RLC_ERR_ARG, "null argument");
+    size_t n = (size_t)map->W * map->H;
+    uint8_t* d = nullptr;
+    CUDA_OR_FAIL(cudaMalloc(&d, n), "edge map");
+    cudaError_t e = launch_edge_map(map->d_bits, map->W, map->H, map->TY, d, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(edge_out, d, n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return finish_launch(e, "edge map");
+}
+
+static int method_create(rlc_map* map, int kind, float max_range, unsigned td, const float* cos_tab,
+                         const float* sin_tab, rlc_method** out) {
+    if (!out) return fail(RLC_ERR_ARG, "null output handle");
+    *out = nullptr;
+    if (!map) return fail(RLC_ERR_ARG, "null map handle");
+    if (kind < RLC_BL || kind > RLC_RMGPU) return fail(RLC_ERR_ARG, "unknown method kind %d", kind);
+    if (!std::isfinite(max_range)) return fail(RLC_ERR_ARG, "max_range must be finite");
+    bool cddt = kind == RLC_CDDT || kind == RLC_PCDDT;
+    if (cddt && td < 2) return fail(RLC_ERR_ARG, "theta_discretization %u must be >= 2", td);
+    rlc_method* m = new rlc_method();
+    map->retain();
+    m->map = map;
+    m->kind = kind;
+    m->dkind = kind == RLC_BL ? K_BL : (cddt ? K_CDDT : K_RM);
+    m->mr = max_range;
+    m->td = cddt ? td : 0;
+    m->world = world_consts(map->world);
+    int rc = RLC_OK;
+    cudaError_t e = cudaMalloc(&m->d_err, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(m->d_err, 0, sizeof(unsigned));
+    if (e != cudaSuccess) rc = cuda_fail(e, "method state");
+    if (!rc && m->dkind == K_RM) rc = map->ensure_dt();
+    if (!rc && cddt) {
+        cddt_constants(m, cos_tab, sin_tab);
+        rc = upload((void**)&m->d_widths, m->h_widths.data(), td * sizeof(int), "cddt widths");
+        if (!rc) rc = upload((void**)&m->d_trans, m->h_trans.data(), td * sizeof(float), "cddt translations");
+        if (!rc) rc = upload((void**)&m->d_cos, m->h_cos.data(), td * sizeof(float), "cddt cos");
+        if (!rc) rc = upload((void**)&m->d_sin, m->h_sin.data(), td * sizeof(float), "cddt sin");
+        if (!rc) {
+            char why[256] = {0};
+            e = cddt_build(map->d_bits, map->W, map->H, map->TY, td, m->d_widths, m->d_trans, m->d_cos, m->d_sin,
+                           m->h_slice_base.data(), &m->tab, 0, why, sizeof(why));
+            if (e != cudaSuccess) rc = why[0] ? fail(RLC_ERR_ARG, "%s", why) : cuda_fail(e, "CDDT construction");
+        }
+        if (!rc && kind == RLC_PCDDT) {
+            e = cddt_prune(map->d_bits, map->W, map->H, map->TY, td, max_range, m->d_widths, m->d_trans, m->d_cos,
+                           m->d_sin, &m->tab, 0);
+            if (e != cudaSuccess) rc = cuda_fail(e, "CDDT prune");
+        }
+    }
+    if (rc) {
+        delete m;
+        return rc;
+    }
+    *out = m;
+    return RLC_OK;
+}
+
+int rlc_method_create(rlc_map* map, int kind, float max_range, unsigned theta_disc, rlc_method** out) {
+    return method_create(map, kind, max_range, theta_disc, nullptr, nullptr, out);
+}
+
+int rlc_method_create_cddt_trig(rlc_map* map, int kind, float max_range, unsigned theta_disc,
+                                const float* cos_tab, const float* sin_tab, rlc_method** out) {
+    if (kind != RLC_CDDT && kind != RLC_PCDDT) return fail(RLC_ERR_ARG, "trig tables apply to CDDT kinds");
+    if (!cos_tab || !sin_tab) return fail(RLC_ERR_ARG, "null trig table");
+    return method_create(map, kind, max_range, theta_disc, cos_tab, sin_tab, out);
+}
+
+int rlc_method_destroy(rlc_method* m) {
+    delete m;
+    return RLC_OK;
+}
+
+int rlc_method_info(const rlc_method* m, int* kind, float* max_range, unsigned* theta_disc) {
+    if (int rc = check_method(m)) return rc;
+    if (kind) *kind = m->kind;
+    if (max_range) *max_range = m->mr;
+    if (theta_disc) *theta_disc = m->td;
+    return RLC_OK;
+}
+
+int rlc_method_device_flags(rlc_method* m, unsigned* flags) {
+    if (int rc = check_method(m)) return rc;
+    unsigned f = 0;
+    CUDA_OR_FAIL(cudaDeviceSynchronize(), "device flags");
+    CUDA_OR_FAIL(cudaMemcpy(&f, m->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost), "device flags");
+    CUDA_OR_FAIL(cudaMemset(m->d_err, 0, sizeof(unsigned)), "device flags");
+    if (flags) *flags = f;
+    return RLC_OK;
+}
+
+int rlc_cddt_prune(rlc_method* m, float max_range) {
+    if (int rc = check_method(m)) return rc;
+    if (m->dkind != K_CDDT) return fail(RLC_ERR_STATE, "prune applies to CDDT methods");
+    cudaError_t e = cddt_prune(m->map->d_bits, m->map->W, m->map->H, m->map->TY, m->td, max_range, m->d_widths,
+                               m->d_trans, m->d_cos, m->d_sin, &m->tab, 0);
+    return finish_launch(e, "CDDT prune");
+}
+
+int rlc_cddt_table_size(rlc_method* m, int64_t* num_bins, int64_t* num_zeros) {
+    if (int rc = check_method(m)) return rc;
+    if (m->dkind != K_CDDT) return fail(RLC_ERR_STATE, "not a CDDT method");
+    if (num_bins) *num_bins = m->tab.total_bins;
+    if (num_zeros) *num_zeros = m->tab.nzeros;
+    return RLC_OK;
+}
+
+int rlc_cddt_table_export(rlc_method* m, int* widths, float* trans, int64_t* bin_len, float* zeros) {
+    if (int rc = check_method(m)) return rc;
+    if (m->dkind != K_CDDT) return fail(RLC_ERR_STATE, "not a CDDT method");
+    if (widths) std::memcpy(widths, m->h_widths.data(), m->td * sizeof(int));
+    if (trans) std::memcpy(trans, m->h_trans.data(), m->td * sizeof(float));
+    if (bin_len) {
+        std::vector<uint32_t> st(m->tab.total_bins + 1);
+        CUDA_OR_FAIL(cudaMemcpy(st.data(), m->tab.bin_start, st.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost),
+                     "CDDT export");
+        for (uint32_t b = 0; b < m->tab.total_bins; ++b) bin_len[b] = (int64_t)st[b + 1] - st[b];
+    }
+    if (zeros && m->tab.nzeros)
+        CUDA_OR_FAIL(cudaMemcpy(zeros, m->tab.zeros, (size_t)m->tab.nzeros * sizeof(float), cudaMemcpyDeviceToHost),
+                     "CDDT export");
+    return RLC_OK;
+}
+
+int rlc_cddt_table_load(rlc_method* m, const float* trans, const int64_t* bin_len, const float* zeros,
+                        int64_t num_zeros) {
+    if (int rc = check_method(m)) return rc;
+    if (m->dkind != K_CDDT) return fail(RLC_ERR_STATE, "not a CDDT method");
+    if (!trans || !bin_len || (num_zeros > 0 && !zeros)) return fail(RLC_ERR_ARG, "null table argument");
+    if (num_zeros < 0 || num_zeros >= (int64_t)0xffffffffll) return fail(RLC_ERR_ARG, "bad zero count");
+    const uint32_t nb = m->tab.total_bins;
+    std::vector<uint32_t> st(nb + 1);
+    st[0] = 0;
+    for (uint32_t b = 0; b < nb; ++b) {
+        if (bin_len[b] < 0) return fail(RLC_ERR_ARG, "negative bin length");
+        uint64_t next = (uint64_t)st[b] + (uint64_t)bin_len[b];
+        if (next > (uint64_t)num_zeros) return fail(RLC_ERR_ARG, "bin lengths exceed num_zeros");
+        st[b + 1] = (uint32_t)next;
+    }
+    if (st[nb] != (uint32_t)num_zeros) return fail(RLC_ERR_ARG, "bin lengths sum to %u, not %lld", st[nb], (long long)num_zeros);
+    uint32_t* d_st = nullptr;
+    float* d_z = nullptr;
+    if (int rc = upload((void**)&d_st, st.data(), st.size() * sizeof(uint32_t), "CDDT load")) return rc;
+    if (int rc = upload((void**)&d_z, zeros, (size_t)num_zeros * sizeof(float), "CDDT load")) {
+        cudaFree(d_st);
+        return rc;
+    }
+    cudaFree(m->tab.bin_start);
+    cudaFree(m->tab.zeros);
+    m->tab.bin_start = d_st;
+    m->tab.zeros = d_z;
+    m->tab.nzeros = (uint32_t)num_zeros;
+    std::memcpy(m->h_trans.data(), trans, m->td * sizeof(float));
+    CUDA_OR_FAIL(cudaMemcpy(m->d_trans, trans, m->td * sizeof(float), cudaMemcpyHostToDevice), "CDDT load");
+    return RLC_OK;
+}
+
+int rlc_method_set_trig_override(rlc_method* m, const float* trig, int64_t count) {
+    if (int rc = check_method(m)) return rc;
+    cudaFree(m->d_trig);
+    m->d_trig = nullptr;
+    m->trig_count = 0;
+    if (!trig || count <= 0) return RLC_OK;
+    if (int rc = upload((void**)&m->d_trig, trig, (size_t)count * 2 * sizeof(float), "trig override")) return rc;
+    m->trig_count = count;
+    return RLC_OK;
+}
+
+int rlc_calc_range(rlc_method* m, float x, float y, float heading, float* out) {
+    if (int rc = check_method(m)) return rc;
+    if (!out) return fail(RLC_ERR_ARG, "null output");
+    float in[3] = {x, y, heading};
+    return rlc_calc_range_many(m, in, out, 1, RLC_NO_WORLD, nullptr);
+}
+
+int rlc_calc_range_many(rlc_method* m, const float* ins, float* outs, int n, unsigned flags, void* stream) {
+    if (int rc = check_method(m)) return rc;
+    if (n < 0) return fail(RLC_ERR_ARG, "negative query count");
+    if (n == 0) return RLC_OK;
+    if (!ins || !outs) return fail(RLC_ERR_ARG, "null array");
+    if (int rc = check_trig(m, n)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    CastParams p = m->params();
+    bool world = !(flags & RLC_NO_WORLD);
+    if (flags & RLC_DEVICE_PTRS)
+        return finish_launch(launch_calc_range_many(p, m->layout, world, ins, outs, n, s), "calc_range_many");
+    size_t bin = align256((size_t)n * 3 * sizeof(float));
+    void* st;
+    if (int rc = m->stage(bin + (size_t)n * sizeof(float), &st)) return rc;
+    float* d_in = (float*)st;
+    float* d_out = (float*)((char*)st + bin);
+    CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    CUDA_OR_FAIL(launch_calc_range_many(p, m->layout, world, d_in, d_out, n, s), "calc_range_many");
+    CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+    CUDA_OR_FAIL(cudaStreamSynchronize(s), "calc_range_many");
+    return RLC_OK;
+}
+
+int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* angles, float* outs, int n, int na,
+                                 unsigned flags, void* stream) {
+    if (int rc = check_method(m)) return rc;
+    if (n < 0 || na < 0) return fail(RLC_ERR_ARG, "negative size");
+    if ((long long)n * na == 0) return RLC_OK;
+    if ((long long)n * na > (1ll << 31) - 1) return fail(RLC_ERR_ARG, "too many rays in one call");
+    if (!ins || !angles || !outs) return fail(RLC_ERR_ARG, "null array");
+    if (int rc = check_trig(m, (long long)n * na)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    CastParams p = m->params();
+    if (flags & RLC_DEVICE_PTRS)
+        return finish_launch(launch_repeat_angles(p, m->layout, ins, angles, outs, n, na, s), "repeat_angles");
+    size_t b0 = align256((size_t)n * 3 * sizeof(float));
+    size_t b1 = align256((size_t)na * sizeof(float));
+    void* st;
+    if (int rc = m->stage(b0 + b1 + (size_t)n * na * sizeof(float), &st)) return rc;
+    float* d_in = (float*)st;
+    float* d_ang = (float*)((char*)st + b0);
+    float* d_out = (float*)((char*)st + b0 + b1);
+    CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    CUDA_OR_FAIL(cudaMemcpyAsync(d_ang, angles, (size_t)na * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    CUDA_OR_FAIL(launch_repeat_angles(p, m->layout, d_in, d_ang, d_out, n, na, s), "repeat_angles");
+    CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, (size_t)n * na * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+    CUDA_OR_FAIL(cudaStreamSynchronize(s), "repeat_angles");
+    return RLC_OK;
+}
+
+int rlc_set_sensor_model(rlc_method* m, const double* table, int K) {
+    if (int rc = check_method(m)) return rc;
+    if (!table || K <= 0) return fail(RLC_ERR_ARG, "sensor model needs a K x K table with K > 0");
+    if ((long long)K * K > (1ll << 28)) return fail(RLC_ERR_ARG, "sensor table too large");
+    cudaFree(m->d_table);
+    m->d_table = nullptr;
+    m->K = 0;
+    if (int rc = upload((void**)&m->d_table, table, (size_t)K * K * sizeof(double), "sensor model")) return rc;
+    m->K = K;
+    return RLC_OK;
+}
+
+int rlc_eval_sensor_model(rlc_method* m, const float* obs, const float* ranges, double* outs, int na, int n,
+                          unsigned flags, void* stream) {
+    if (int rc = check_method(m)) return rc;
+    if (!m->d_table) return fail(RLC_ERR_STATE, "set_sensor_model has not been called");
+    if (n < 0 || na < 0) return fail(RLC_ERR_ARG, "negative size");
+    if (n == 0) return RLC_OK;
+    if (!outs || (na > 0 && (!obs || !ranges))) return fail(RLC_ERR_ARG, "null array");
+    if (na > 16384) return fail(RLC_ERR_ARG, "at most 16384 rays per particle");
+    cudaStream_t s = (cudaStream_t)stream;
+    CastParams p = m->params();
+    SensorDev sm{m->d_table, m->K};
+    if (flags & RLC_DEVICE_PTRS)
+        return finish_launch(launch_eval_sensor(p, sm, obs, ranges, outs, na, n, s), "eval_sensor_model");
+    size_t b0 = align256((size_t)na * sizeof(float));
+    size_t b1 = align256((size_t)n * na * sizeof(float));
+    void* st;
+    if (int rc = m->stage(b0 + b1 + (size_t)n * sizeof(double), &st)) return rc;
+    float* d_obs = (float*)st;
+    float* d_rng = (float*)((char*)st + b0);
+    double* d_out = (double*)((char*)st + b0 + b1);
+    if (na) {
+        CUDA_OR_FAIL(cudaMemcpyAsync(d_obs, obs, (size_t)na * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+        CUDA_OR_FAIL(cudaMemcpyAsync(d_rng, ranges, (size_t)n * na * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    }
+    CUDA_OR_FAIL(launch_eval_sensor(p, sm, d_obs, d_rng, d_out, na, n, s), "eval_sensor_model");
+    CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+    CUDA_OR_FAIL(cudaStreamSynchronize(s), "eval_sensor_model");
+    return RLC_OK;
+}
+
+static int fused_device(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
+                        int na, cudaStream_t s);
+
+int rlc_calc_range_repeat_angles_eval_sensor_model(rlc_method* m, const float* ins, const float* angles,
+                                                   const float* obs, double* weights, int n, int na,
+                                                   unsigned flags, void* stream) {
+    if (int rc = check_method(m)) return rc;
+    if (!m->d_table) return fail(RLC_ERR_STATE, "set_sensor_model has not been called");
+    if (n < 0 || na < 0) return fail(RLC_ERR_ARG, "negative size");
+    if (n == 0) return RLC_OK;
+    if (!ins || !weights || (na > 0 && (!angles || !obs))) return fail(RLC_ERR_ARG, "null array");
+    if (na > 16384) return fail(RLC_ERR_ARG, "at most 16384 beams per particle");
+    if ((long long)n * na > (1ll << 31) - 1) return fail(RLC_ERR_ARG, "too many rays in one call");
+    if (int rc = check_trig(m, (long long)n * na)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (flags & RLC_DEVICE_PTRS) return fused_device(m, ins, angles, obs, weights, n, na, s);
+    size_t b0 = align256((size_t)n * 3 * sizeof(float));
+    size_t b1 = align256((size_t)na * sizeof(float));
+    size_t b2 = align256((size_t)na * sizeof(float));
+    void* st;
+    if (int rc = m->stage(b0 + b1 + b2 + (size_t)n * sizeof(double), &st)) return rc;
+    float* d_in = (float*)st;
+    float* d_ang = (float*)((char*)st + b0);
+    float* d_obs = (float*)((char*)st + b0 + b1);
+    double* d_w = (double*)((char*)st + b0 + b1 + b2);
+    CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    if (na) {
+        CUDA_OR_FAIL(cudaMemcpyAsync(d_ang, angles, (size_t)na * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+        CUDA_OR_FAIL(cudaMemcpyAsync(d_obs, obs, (size_t)na * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    }
+    if (int rc = fused_device(m, d_in, d_ang, d_obs, d_w, n, na, s)) return rc;
+    CUDA_OR_FAIL(cudaMemcpyAsync(weights, d_w, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+    CUDA_OR_FAIL(cudaStreamSynchronize(s), "fused sensor model");
+    return RLC_OK;
+}
+
+static int fused_device(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
+                        int na, cudaStream_t s) {
+    if (m->autotune_pending) {
+        m->autotune_pending = false;
+        int rc = rlc_method_autotune(m, ins, angles, obs, w, n, na, s);
+        if (rc) return rc;
+    }
+    CastParams p = m->params();
+    SensorDev sm{m->d_table, m->K};
+    return finish_launch(launch_fused(p, m->layout, sm, ins, angles, obs, w, n, na, m->fused_block, s),
+                         "fused sensor model");
+}
+
+int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n, int na, unsigned flags,
+                    int64_t* total_steps) {
+    if (int rc = check_method(m)) return rc;
+    if (!total_steps) return fail(RLC_ERR_ARG, "null output");
+    if (m->dkind == K_CDDT) return fail(RLC_ERR_STATE, "step counts apply to RM and BL");
+    if (n < 0 || na < 0) return fail(RLC_ERR_ARG, "negative size");
+    *total_steps = 0;
+    if ((long long)n * na == 0) return RLC_OK;
+    if (!ins || !angles) return fail(RLC_ERR_ARG, "null array");
+    if (int rc = check_trig(m, (long long)n * na)) return rc;
+    CastParams p = m->params();
+    const float* d_in = ins;
+    const float* d_ang = angles;
+    void* st = nullptr;
+    size_t b0 = align256((size_t)n * 3 * sizeof(float)), b1 = align256((size_t)na * sizeof(float));
+    if (int rc = m->stage(b0 + b1 + sizeof(unsigned long long), &st)) return rc;
+    unsigned long long* d_total = (unsigned long long*)((char*)st + b0 + b1);
+    if (!(flags & RLC_DEVICE_PTRS)) {
+        CUDA_OR_FAIL(cudaMemcpy(st, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice), "H2D");
+        CUDA_OR_FAIL(cudaMemcpy((char*)st + b0, angles, (size_t)na * sizeof(float), cudaMemcpyHostToDevice), "H2D");
+        d_in = (const float*)st;
+        d_ang = (const float*)((char*)st + b0);
+    }
+    CUDA_OR_FAIL(cudaMemset(d_total, 0, sizeof(unsigned long long)), "count steps");
+    CUDA_OR_FAIL(launch_count_steps(p, d_in, d_ang, n, na, d_total, 0), "count steps");
+    unsigned long long tot = 0;
+    CUDA_OR_FAIL(cudaMemcpy(&tot, d_total, sizeof(tot), cudaMemcpyDeviceToHost), "count steps");
+    *total_steps = (int64_t)tot;
+    return RLC_OK;
+}
+
+int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block) {
+    if (int rc = check_method(m)) return rc;
+    if (dt_layout < -1 || dt_layout > 1) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0 or 1");
+    if (fused_block != 0 && (fused_block < 32 || fused_block > 1024 || fused_block % 32))
+        return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 1024]");
+    if (dt_layout == -1) m->autotune_pending = true;
+    else m->layout = dt_layout;
+    if (fused_block) m->fused_block = fused_block;
+    return RLC_OK;
+}
+
+int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_block) {
+    if (int rc = check_method(m)) return rc;
+    if (dt_layout) *dt_layout = m->layout;
+    if (fused_block) *fused_block = m->fused_block;
+    return RLC_OK;
+}
+
+int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
+                        int na, void* stream) {
+    if (int rc = check_method(m)) return rc;
+    if (!m->d_table) return fail(RLC_ERR_STATE, "set_sensor_model has not been called");
+    if (n <= 0) return RLC_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    CUDA_OR_FAIL(cudaEventCreate(&e0), "autotune");
+    CUDA_OR_FAIL(cudaEventCreate(&e1), "autotune");
+    const int layouts[2] = {DT_LINEAR, DT_TILED};
+    const int blocks[3] = {128, 256, 512};
+    float best = 1e30f;
+    int best_layout = m->layout, best_block = m->fused_block;
+    SensorDev sm{m->d_table, m->K};
+    cudaError_t err = cudaSuccess;
+    for (int li = 0; li < (m->dkind == K_RM ? 2 : 1) && err == cudaSuccess; ++li) {
+        for (int bi = 0; bi < 3 && err == cudaSuccess; ++bi) {
+            m->layout = layouts[li];
+            CastParams p = m->params();
+            float total = 0.0f;
+            for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+                err = launch_fused(p, m->layout, sm, ins, angles, obs, w, n, na, blocks[bi], s);   // warm
+                if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+                if (err == cudaSuccess) err = launch_fused(p, m->layout, sm, ins, angles, obs, w, n, na, blocks[bi], s);
+                if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) total += ms;
+            }
+            if (err == cudaSuccess && total < best) {
+                best = total;
+                best_layout = layouts[li];
+                best_block = blocks[bi];
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    m->layout = best_layout;
+    m->fused_block = best_block;
+    if (err != cudaSuccess) return cuda_fail(err, "autotune");
+    return RLC_OK;
+}
+
+}  // extern "C"
+
+// ============================================================ batched filters
+struct rlc_batch {
+    int nf = 0;
+    FilterDev* d_filters = nullptr;
+    unsigned* d_queue = nullptr;
+    unsigned total_tiles = 0;
+    long long rays = 0;
+    int block = 256, grid = 0;
+    size_t smem = 0;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~rlc_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+        cudaFree(d_filters);
+        cudaFree(d_queue);
+    }
+};
+
+extern "C" {
+
+int rlc_batch_create(const rlc_filter_desc* fd, int nf, int block, rlc_batch** out) {
+    if (!out) return fail(RLC_ERR_ARG, "null output handle");
+    *out = nullptr;
+    if (nf <= 0 || !fd) return fail(RLC_ERR_ARG, "a batch needs at least one filter");
+    if (block == 0) block = 256;
+    if (block < 32 || block > 512 || block % 32) return fail(RLC_ERR_ARG, "block must be a multiple of 32 in [32, 512]");
+    struct Item { FilterDev f; double cost; };
+    std::vector<Item> items;
+    long long rays = 0;
+    size_t smem = 0;
+    for (int i = 0; i < nf; ++i) {
+        const rlc_filter_desc& d = fd[i];
+        rlc_method* m = d.method;
+        if (!m) return fail(RLC_ERR_ARG, "filter %d: null method", i);
+        if (!m->d_table) return fail(RLC_ERR_STATE, "filter %d: sensor model not set", i);
+        if (d.n_particles < 0 || d.n_angles < 0) return fail(RLC_ERR_ARG, "filter %d: negative size", i);
+        if (d.n_angles > 16384) return fail(RLC_ERR_ARG, "filter %d: at most 16384 beams", i);
+        if (d.n_particles > 0 && (!d.ins || !d.weights || (d.n_angles > 0 && (!d.angles || !d.obs))))
+            return fail(RLC_ERR_ARG, "filter %d: null array", i);
+        if ((long long)d.n_particles * d.n_angles > (1ll << 31) - 1) return fail(RLC_ERR_ARG, "filter %d: too many rays", i);
+        if (m->d_trig && m->trig_count < (long long)d.n_particles * d.n_angles)
+            return fail(RLC_ERR_ARG, "filter %d: trig override too short", i);
+        Item it{};
+        it.f.p = m->params();
+        it.f.layout = m->layout;
+        it.f.sm = SensorDev{m->d_table, m->K};
+        it.f.ins = d.ins;
+        it.f.angles = d.angles;
+        it.f.obs = d.obs;
+        it.f.ranges = d.ranges;
+        it.f.weights = d.weights;
+        it.f.n = d.n_particles;
+        it.f.na = d.n_angles;
+        it.f.ppb = d.n_angles >= block ? 1 : (d.n_angles > 0 ? block / d.n_angles : block);
+        // heavier tiles first: rays per tile x march length
+        it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
+        smem = std::max(smem, (size_t)it.f.ppb * d.n_angles * sizeof(double));
+        rays += (long long)d.n_particles * d.n_angles;
+        items.push_back(it);
+    }
+    std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
+    unsigned long long tiles = 0;
+    std::vector<FilterDev> hf;
+    for (auto& it : items) {
+        it.f.tile_begin = (unsigned)tiles;
+        tiles += (unsigned long long)((it.f.n + it.f.ppb - 1) / it.f.ppb);
+        if (tiles >= 0xffffffffull) return fail(RLC_ERR_ARG, "too many tiles in one batch");
+        hf.push_back(it.f);
+    }
+    rlc_batch* b = new rlc_batch();
+    b->nf = nf;
+    b->total_tiles = (unsigned)tiles;
+    b->rays = rays;
+    b->block = block;
+    b->smem = smem;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = batch_occupancy(block, smem, &per_sm);
+    if (e == cudaSuccess && per_sm <= 0) e = cudaErrorInvalidConfiguration;
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_filters, hf.size() * sizeof(FilterDev));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_filters, hf.data(), hf.size() * sizeof(FilterDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "batch setup");
+    }
+    long long g = (long long)sms * per_sm;
+    if (g > (long long)tiles) g = (long long)tiles;
+    b->grid = (int)(g > 0 ? g : 1);
+    *out = b;
+    return RLC_OK;
+}
+
+int rlc_batch_run(rlc_batch* b, void* stream) {
+    if (!b) return fail(RLC_ERR_ARG, "null batch handle");
+    if (b->total_tiles == 0) return RLC_OK;
+    if (!b->exec) {
+        // capture [queue reset, persistent kernel] once; later runs replay the graph
+        CUDA_OR_FAIL(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal), "batch capture");
+        cudaError_t e = cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->cap);
+        if (e == cudaSuccess)
+            e = launch_batch(b->d_filters, b->nf, b->total_tiles, b->d_queue, b->grid, b->block, b->smem, b->cap);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(b->cap, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            b->exec = nullptr;
+            return cuda_fail(e, "batch graph");
+        }
+        b->graph = g;
+    }
+    CUDA_OR_FAIL(cudaGraphLaunch(b->exec, (cudaStream_t)stream), "batch launch");
+    return RLC_OK;
+}
+
+int rlc_batch_destroy(rlc_batch* b) {
+    delete b;
+    return RLC_OK;
+}
+
+int rlc_batch_info(const rlc_batch* b, int64_t* rays, int64_t* tiles) {
+    if (!b) return fail(RLC_ERR_ARG, "null batch handle");
+    if (rays) *rays = b->rays;
+    if (tiles) *tiles = b->total_tiles;
+    return RLC_OK;
+}
+
+}  // extern "C"

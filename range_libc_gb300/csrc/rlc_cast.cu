@@ -1,0 +1,548 @@
+// Ray casting kernels: Bresenham's line, ray marching on the distance
+// transform and CDDT queries, the world-frame batched wrappers, the sensor
+// model and the fused cast + sensor-model particle update.
+//
+// Every parity-relevant float operation is an explicit round-to-nearest
+// intrinsic (__fmul_rn, __fadd_rn, ...) so that no multiply-add is ever
+// contracted into an FMA: the reference is plain IEEE float/double C++
+// (RangeLib.h), and its results are reproduced bit for bit.  Mixed
+// float/double expressions of the reference are evaluated in double here
+// too, except where the float evaluation is provably identical (noted).
+// The only source of difference is the per-ray cosf/sinf of RM and BL (the
+// host libm and CUDA's sincosf are not both correctly rounded); the optional
+// per-ray trig override removes it for parity tests.
+#include "rlc_internal.cuh"
+
+namespace rlc {
+namespace {
+
+constexpr double kM2Pi = 6.28318530718;           // RangeLib.h:61 M_2PI
+constexpr double kMPi = 3.14159265358979323846;   // <cmath> M_PI
+constexpr int kBinarySearchThreshold = 64;         // RangeLib.h:62
+constexpr int kMaxWrap = 100000;                   // bound on discretize_theta's loops
+
+__device__ __forceinline__ float ref_maxf(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float ref_minf(float a, float b) { return (b < a) ? b : a; }
+
+// ---------------------------------------------------------------- map access
+template <int LAYOUT>
+__device__ __forceinline__ float dt_at(const MapDev& m, int x, int y) {
+    if (LAYOUT == DT_TILED)
+        return __ldg(m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7));
+    return __ldg(m.dt + (size_t)x * m.H + y);
+}
+
+__device__ __forceinline__ bool occ_at(const MapDev& m, int x, int y) {
+    if ((unsigned)x >= (unsigned)m.W || (unsigned)y >= (unsigned)m.H) return false;
+    uint64_t w = __ldg(m.bits + (size_t)(x >> 3) * m.tiles_y + (y >> 3));
+    return (w >> (((x & 7) << 3) | (y & 7))) & 1ull;
+}
+
+// ------------------------------------------------------- ray marching (RM)
+// RangeLib.h:927-962 (RayMarching::calc_range).  t grows by >= 1 per step,
+// so the loop runs at most ceil(max_range) + 1 times.
+template <int LAYOUT>
+__device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps = nullptr) {
+    if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
+    float t = 0.0f;
+    while (t < mr) {
+        int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
+        int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
+        if ((unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H) return mr;
+        float d = dt_at<LAYOUT>(m, px, py);
+        if (steps) ++*steps;
+        if (d <= 0.0f) {
+            float xd = __fsub_rn(__int2float_rn(px), x0);
+            float yd = __fsub_rn(__int2float_rn(py), y0);
+            return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+        }
+        t = __fadd_rn(t, ref_maxf(__fmul_rn(d, 0.999f), 1.0f));
+    }
+    return mr;
+}
+
+// ---------------------------------------------------- Bresenham's line (BL)
+// RangeLib.h:696-769.  The occupancy word of the current 8x8 tile stays in a
+// register; a new word is read only when the line leaves the tile.
+struct BitCache {
+    long long tile = -1;
+    uint64_t word = 0;
+    __device__ __forceinline__ bool test(const MapDev& m, int x, int y) {
+        long long t = (long long)(x >> 3) * m.tiles_y + (y >> 3);
+        if (t != tile) { tile = t; word = __ldg(m.bits + t); }
+        return (word >> (((x & 7) << 3) | (y & 7))) & 1ull;
+    }
+};
+
+__device__ float bl_cast(const MapDev& m, float mr, float x, float y, float c, float s, unsigned* err,
+                         int* steps = nullptr) {
+    if (isnan(x) || isnan(y)) return mr;
+    if (occ_at(m, __float2int_rz(x), __float2int_rz(y))) return 0.0f;
+    if (isnan(c) || isnan(s)) return mr;   // the reference never terminates on a NaN heading
+    float x0 = y, y0 = x;
+    float x1 = __fadd_rn(y, __fmul_rn(mr, s));
+    float y1 = __fadd_rn(x, __fmul_rn(mr, c));
+    bool steep = fabsf(__fsub_rn(y1, y0)) > fabsf(__fsub_rn(x1, x0));
+    if (steep) {
+        float t = x0; x0 = y0; y0 = t;
+        t = x1; x1 = y1; y1 = t;
+    }
+    const float deltax = fabsf(__fsub_rn(x1, x0));
+    const float deltaerr = fabsf(__fsub_rn(y1, y0));
+    float error = 0.0f;
+    float _x = x0, _y = y0;
+    const float xstep = (x0 < x1) ? 1.0f : -1.0f;
+    const float ystep = (y0 < y1) ? 1.0f : -1.0f;
+    const float fw = __int2float_rn(m.W), fh = __int2float_rn(m.H);
+    const int end = __float2int_rz(__fadd_rn(x1, xstep));
+    // the reference loop ends after at most |x1 - x0| + 3 steps; the bound
+    // only fires where float +-1 no longer moves _x (|coordinates| > 2^24)
+    const int bound = (int)(deltax < 1e9f ? deltax : 1e9f) + 4;
+    int n = 0;
+    BitCache cache;
+    while (__float2int_rz(_x) != end) {
+        if (n > bound) { atomicOr(err, F_BL_BOUND); return mr; }
+        ++n;
+        if (steps) ++*steps;
+        _x = __fadd_rn(_x, xstep);
+        error = __fadd_rn(error, deltaerr);
+        // `error * 2.00 >= deltax` is a double comparison in the reference;
+        // doubling a finite float is exact, so the float comparison is identical
+        if (__fmul_rn(error, 2.0f) >= deltax) {
+            _y = __fadd_rn(_y, ystep);
+            error = __fsub_rn(error, deltax);
+        }
+        const float gx = steep ? _x : _y;   // isOccupied(_y, _x) when not steep
+        const float gy = steep ? _y : _x;
+        if (0.0f <= gx && gx < fw && 0.0f <= gy && gy < fh &&
+            cache.test(m, __float2int_rz(gx), __float2int_rz(gy))) {
+            float xd = __fsub_rn(_x, x0), yd = __fsub_rn(_y, y0);
+            return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+        }
+    }
+    return mr;
+}
+
+// ------------------------------------------------------------------ CDDT
+// RangeLib.h:1287-1340 discretize_theta (alternate mod, cached constants)
+__device__ __forceinline__ void cddt_discretize(const CddtDev& c, float theta, int& binned, bool& flipped,
+                                                unsigned* err) {
+    int it = 0;
+    if (theta < 0.0f) {
+        while (theta < 0.0f) {
+            if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
+            theta = __double2float_rn(__dadd_rn((double)theta, kM2Pi));
+        }
+    } else if ((double)theta > kM2Pi) {
+        while ((double)theta > kM2Pi) {
+            if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
+            theta = __double2float_rn(__dsub_rn((double)theta, kM2Pi));
+        }
+    }
+    bool fl = false;
+    if ((double)theta >= kMPi) {
+        fl = true;
+        theta = __double2float_rn(__dsub_rn((double)theta, kMPi));
+    }
+    int rounded = __float2int_rz(roundf(__fmul_rn(theta, c.td_div_2pi)));
+    if ((unsigned)rounded == (c.td >> 1)) {
+        rounded = 0;
+        fl = !fl;
+    }
+    binned = (int)((unsigned)rounded % c.td);
+    flipped = fl;
+}
+
+// upper_bound: first index with bin[i] > v
+__device__ __forceinline__ int upper_bound_g(const float* __restrict__ bin, int n, float v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (v < __ldg(bin + mid)) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+// RangeLib.h:1342-1516 (CDDTCast::calc_range)
+__device__ float cddt_cast(const CastParams& p, float x, float y, float heading) {
+    const CddtDev& c = p.cddt;
+    const float mr = p.mr;
+    if (isnan(x) || isnan(y) || isnan(heading)) return mr;
+    int a;
+    bool fl;
+    cddt_discretize(c, -heading, a, fl, p.err);   // discretize_theta(-1.0 * heading)
+    const float ca = __ldg(c.cosv + a), sa = __ldg(c.sinv + a);
+    const float lx = __fsub_rn(__fmul_rn(x, ca), __fmul_rn(y, sa));
+    const float ly = __fadd_rn(__fadd_rn(__fmul_rn(x, sa), __fmul_rn(y, ca)), __ldg(c.trans + a));
+    const unsigned li = (unsigned)__float2int_rz(ly);
+    if (li >= (unsigned)__ldg(c.widths + a)) return mr;
+    const unsigned b = __ldg(c.slice_base + a) + li;
+    const unsigned lo = __ldg(c.bin_start + b);
+    const int n = (int)(__ldg(c.bin_start + b + 1) - lo);
+    const float* bin = c.zeros + lo;
+    const int high = n - 1;
+    if (high == -1) return mr;
+    const float first = __ldg(bin), last = __ldg(bin + high);
+    // grid[x][y] with float indices: the cell under the query point
+    auto occupied = [&]() -> bool {
+        if (!(x > -1.0f) || !(y > -1.0f)) return false;
+        return occ_at(p.map, __float2int_rz(x), __float2int_rz(y));
+    };
+    if (fl) {
+        if (first > lx) return mr;
+        if (last < lx) return __fsub_rn(lx, last);
+        if (occupied()) return 0.0f;
+        if (high > kBinarySearchThreshold) {
+            int idx = upper_bound_g(bin, n, lx);
+            return __fsub_rn(lx, __ldg(bin + idx - 1));
+        }
+        for (int i = high; i >= 0; --i) {
+            float z = __ldg(bin + i);
+            if (z <= lx) return __fsub_rn(lx, z);
+        }
+    } else {
+        if (last < lx) return mr;
+        if (first > lx) return __fsub_rn(first, lx);
+        if (occupied()) return 0.0f;
+        if (high > kBinarySearchThreshold) {
+            int idx = upper_bound_g(bin, n, lx);
+            if (idx == n) { atomicOr(p.err, F_CDDT_PAST_END); return 0.0f; }
+            return __fsub_rn(__ldg(bin + idx), lx);
+        }
+        for (int i = 0; i < n; ++i) {
+            float z = __ldg(bin + i);
+            if (z >= lx) return __fsub_rn(z, lx);
+        }
+    }
+    return -1.0f;
+}
+
+// ------------------------------------------------------------- dispatch
+template <int KIND, int LAYOUT>
+__device__ __forceinline__ float cast_one(const CastParams& p, float x, float y, float h, long long ray) {
+    if (KIND == K_CDDT) return cddt_cast(p, x, y, h);
+    float c, s;
+    if (p.trig) {
+        c = p.trig[2 * ray];
+        s = p.trig[2 * ray + 1];
+    } else {
+        sincosf(h, &s, &c);
+    }
+    if (KIND == K_RM) return rm_cast<LAYOUT>(p.map, p.mr, x, y, c, s);
+    return bl_cast(p.map, p.mr, x, y, c, s, p.err);
+}
+
+// RangeLib.h:468-475: world -> grid, then calc_range(y, x, theta)
+__device__ __forceinline__ void world_to_grid(const WorldDev& w, float xw, float yw, float thw,
+                                              float& ax, float& ay, float& th) {
+    float x = __fmul_rn(__fsub_rn(xw, w.ox), w.inv_s);
+    float y = __fmul_rn(__fsub_rn(yw, w.oy), w.inv_s);
+    float tmp = x;
+    x = __fsub_rn(__fmul_rn(w.ca, x), __fmul_rn(w.sa, y));
+    y = __fadd_rn(__fmul_rn(w.sa, tmp), __fmul_rn(w.ca, y));
+    th = __fadd_rn(-thw, w.rc);
+    ax = y;
+    ay = x;
+}
+
+// std::min<float>(std::max<float>(v, 0.0), (float)K - 1.0), then (int)
+__device__ __forceinline__ int sensor_bin(float v, int K, unsigned* err) {
+    const float hi = __int2float_rn(K - 1);
+    v = ref_minf(ref_maxf(v, 0.0f), hi);
+    if (isnan(v)) { atomicOr(err, F_NAN_INDEX); return 0; }
+    return __float2int_rz(v);
+}
+
+// ---------------------------------------------------------------- kernels
+template <int KIND, int LAYOUT, bool WORLD>
+__global__ void __launch_bounds__(256) k_calc_range_many(CastParams p, const float* __restrict__ ins,
+                                                         float* __restrict__ outs, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float q0 = __ldg(ins + 3 * (size_t)i), q1 = __ldg(ins + 3 * (size_t)i + 1), q2 = __ldg(ins + 3 * (size_t)i + 2);
+    if (WORLD) {
+        float ax, ay, th;
+        world_to_grid(p.world, q0, q1, q2, ax, ay, th);
+        outs[i] = __fmul_rn(cast_one<KIND, LAYOUT>(p, ax, ay, th, i), p.world.s);
+    } else {
+        outs[i] = cast_one<KIND, LAYOUT>(p, q0, q1, q2, i);
+    }
+}
+
+// RangeLib.h:482-520: rays are particle-major, ray = i * na + a
+template <int KIND, int LAYOUT>
+__global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float* __restrict__ ins,
+                                                       const float* __restrict__ angles,
+                                                       float* __restrict__ outs, int n, int na) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)n * na) return;
+    int i = (int)(g / na);
+    int a = (int)(g - (long long)i * na);
+    float ax, ay, th;
+    world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
+                  __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
+    float r = cast_one<KIND, LAYOUT>(p, ax, ay, __fsub_rn(th, __ldg(angles + a)), g);
+    outs[g] = __fmul_rn(r, p.world.s);
+}
+
+// RangeLib.h:533-555: the weight is the product over beams in beam order
+__global__ void __launch_bounds__(256) k_eval_sensor(CastParams p, SensorDev sm, const float* __restrict__ obs,
+                                                     const float* __restrict__ ranges, double* __restrict__ outs,
+                                                     int na, int n, int ppb) {
+    extern __shared__ double fac[];
+    const int first = blockIdx.x * ppb;
+    const int nr = ppb * na;
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+        int li = r / na, a = r - li * na, i = first + li;
+        if (i < n) {
+            int ri = sensor_bin(__fmul_rn(__ldg(obs + a), p.world.inv_s), sm.K, p.err);
+            int di = sensor_bin(__fmul_rn(__ldg(ranges + (size_t)i * na + a), p.world.inv_s), sm.K, p.err);
+            fac[r] = __ldg(sm.table + (size_t)ri * sm.K + di);
+        }
+    }
+    __syncthreads();
+    for (int li = threadIdx.x; li < ppb; li += blockDim.x) {
+        int i = first + li;
+        if (i >= n) continue;
+        double w = 1.0;
+        for (int a = 0; a < na; ++a) w = __dmul_rn(w, fac[li * na + a]);
+        outs[i] = w;
+    }
+}
+
+// RangeLib.h:558-612: ranges stay in pixels; factors are staged in shared
+// memory and multiplied in beam order so the weight is bit-identical.
+template <int KIND, int LAYOUT>
+__global__ void __launch_bounds__(256) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
+                                               const float* __restrict__ angles, const float* __restrict__ obs,
+                                               double* __restrict__ weights, int n, int na, int ppb) {
+    extern __shared__ double fac[];
+    const int first = blockIdx.x * ppb;
+    const int nr = ppb * na;
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+        int li = r / na, a = r - li * na, i = first + li;
+        if (i < n) {
+            float ax, ay, th;
+            world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
+                          __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
+            float d = cast_one<KIND, LAYOUT>(p, ax, ay, __fsub_rn(th, __ldg(angles + a)), (long long)i * na + a);
+            int di = sensor_bin(d, sm.K, p.err);
+            int ri = sensor_bin(__fmul_rn(__ldg(obs + a), p.world.inv_s), sm.K, p.err);
+            fac[r] = __ldg(sm.table + (size_t)ri * sm.K + di);
+        }
+    }
+    __syncthreads();
+    for (int li = threadIdx.x; li < ppb; li += blockDim.x) {
+        int i = first + li;
+        if (i >= n) continue;
+        double w = 1.0;
+        for (int a = 0; a < na; ++a) w = __dmul_rn(w, fac[li * na + a]);
+        weights[i] = w;
+    }
+}
+
+
+// ------------------------------------------------- persistent multi-filter
+__device__ __forceinline__ float cast_dyn(const CastParams& p, int layout, float x, float y, float h, long long ray) {
+    if (p.kind == K_RM)
+        return layout == DT_TILED ? cast_one<K_RM, DT_TILED>(p, x, y, h, ray) : cast_one<K_RM, DT_LINEAR>(p, x, y, h, ray);
+    if (p.kind == K_BL) return cast_one<K_BL, DT_LINEAR>(p, x, y, h, ray);
+    return cast_one<K_CDDT, DT_LINEAR>(p, x, y, h, ray);
+}
+
+// Every block loops: take the next tile index from the device queue, cast
+// the tile's rays (whole particles of one filter) into shared memory, then
+// multiply each particle's factors in beam order.  Filters are stored in
+// descending per-tile cost, so heavy tiles are handed out first.  There is
+// no waiting on other blocks: a block that finds the queue exhausted exits.
+__global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
+                                               unsigned* __restrict__ queue) {
+    extern __shared__ double fac[];
+    __shared__ unsigned s_tile;
+    __shared__ int s_f;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            unsigned t = atomicAdd(queue, 1u);
+            s_tile = t;
+            int lo = 0, hi = nf - 1;   // last filter with tile_begin <= t
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (filters[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
+            }
+            s_f = lo;
+        }
+        __syncthreads();
+        const unsigned t = s_tile;
+        if (t >= total_tiles) break;
+        const FilterDev& F = filters[s_f];
+        const int na = F.na, ppb = F.ppb;
+        const int first = (int)(t - F.tile_begin) * ppb;
+        const int nr = ppb * na;
+        for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+            int li = r / na, a = r - li * na, i = first + li;
+            if (i < F.n) {
+                float ax, ay, th;
+                world_to_grid(F.p.world, __ldg(F.ins + 3 * (size_t)i), __ldg(F.ins + 3 * (size_t)i + 1),
+                              __ldg(F.ins + 3 * (size_t)i + 2), ax, ay, th);
+                long long ray = (long long)i * na + a;
+                float d = cast_dyn(F.p, F.layout, ax, ay, __fsub_rn(th, __ldg(F.angles + a)), ray);
+                if (F.ranges) F.ranges[ray] = d;
+                int di = sensor_bin(d, F.sm.K, F.p.err);
+                int ri = sensor_bin(__fmul_rn(__ldg(F.obs + a), F.p.world.inv_s), F.sm.K, F.p.err);
+                fac[r] = __ldg(F.sm.table + (size_t)ri * F.sm.K + di);
+            }
+        }
+        __syncthreads();
+        for (int li = threadIdx.x; li < ppb; li += blockDim.x) {
+            int i = first + li;
+            if (i >= F.n) continue;
+            double w = 1.0;
+            for (int a = 0; a < na; ++a) w = __dmul_rn(w, fac[li * na + a]);
+            F.weights[i] = w;
+        }
+        __syncthreads();
+    }
+}
+
+// Diagnostic: march steps (RM: distance-transform reads; BL: cells tested)
+// of the world-frame repeat-angle rays, summed into *total.  Same arithmetic
+// as the casting kernels; used to state the algorithmic bytes of a workload.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_count_steps(CastParams p, const float* __restrict__ ins,
+                                                     const float* __restrict__ angles, int n, int na,
+                                                     unsigned long long* total) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int steps = 0;
+    if (g < (long long)n * na) {
+        int i = (int)(g / na), a = (int)(g - (long long)i * na);
+        float ax, ay, th;
+        world_to_grid(p.world, ins[3 * (size_t)i], ins[3 * (size_t)i + 1], ins[3 * (size_t)i + 2], ax, ay, th);
+        float h = __fsub_rn(th, angles[a]);
+        float c, s;
+        if (p.trig) { c = p.trig[2 * g]; s = p.trig[2 * g + 1]; } else sincosf(h, &s, &c);
+        if (KIND == K_RM) rm_cast<DT_LINEAR>(p.map, p.mr, ax, ay, c, s, &steps);
+        else bl_cast(p.map, p.mr, ax, ay, c, s, p.err, &steps);
+    }
+    for (int o = 16; o; o >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, o);
+    if ((threadIdx.x & 31) == 0 && steps) atomicAdd(total, (unsigned long long)steps);
+}
+
+inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+template <template <int, int> class F, class... Args>
+cudaError_t dispatch(int kind, int layout, Args... args) {
+    if (kind == K_RM) {
+        if (layout == DT_TILED) return F<K_RM, DT_TILED>::run(args...);
+        return F<K_RM, DT_LINEAR>::run(args...);
+    }
+    if (kind == K_BL) return F<K_BL, DT_LINEAR>::run(args...);
+    return F<K_CDDT, DT_LINEAR>::run(args...);
+}
+
+template <int KIND, int LAYOUT>
+struct RunMany {
+    static cudaError_t run(const CastParams& p, bool world, const float* ins, float* outs, int n, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        if (world) k_calc_range_many<KIND, LAYOUT, true><<<blocks_for(n, 256), 256, 0, s>>>(p, ins, outs, n);
+        else k_calc_range_many<KIND, LAYOUT, false><<<blocks_for(n, 256), 256, 0, s>>>(p, ins, outs, n);
+        return cudaGetLastError();
+    }
+};
+
+template <int KIND, int LAYOUT>
+struct RunAngles {
+    static cudaError_t run(const CastParams& p, const float* ins, const float* angles, float* outs, int n, int na,
+                           cudaStream_t s) {
+        long long total = (long long)n * na;
+        if (total <= 0) return cudaSuccess;
+        k_repeat_angles<KIND, LAYOUT><<<blocks_for(total, 256), 256, 0, s>>>(p, ins, angles, outs, n, na);
+        return cudaGetLastError();
+    }
+};
+
+// particles per block and block size for the product kernels
+inline void product_shape(int na, int block, int& ppb, int& threads) {
+    if (block <= 0) block = 256;
+    if (na <= 0) { ppb = block; threads = block; return; }   // empty product: weight 1.0
+    ppb = na >= block ? 1 : block / na;
+    int nr = ppb * na;
+    threads = nr >= block ? block : ((nr + 31) / 32) * 32;
+}
+
+template <class K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <int KIND, int LAYOUT>
+struct RunFused {
+    static cudaError_t run(const CastParams& p, const SensorDev& sm, const float* ins, const float* angles,
+                           const float* obs, double* w, int n, int na, int block, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        int ppb, threads;
+        product_shape(na, block, ppb, threads);
+        size_t smem = (size_t)ppb * na * sizeof(double);
+        cudaError_t e = set_smem(k_fused<KIND, LAYOUT>, smem);
+        if (e != cudaSuccess) return e;
+        k_fused<KIND, LAYOUT><<<blocks_for(n, ppb), threads, smem, s>>>(p, sm, ins, angles, obs, w, n, na, ppb);
+        return cudaGetLastError();
+    }
+};
+
+}  // namespace
+
+cudaError_t launch_calc_range_many(const CastParams& p, int layout, bool world, const float* ins, float* outs,
+                                   int n, cudaStream_t s) {
+    return dispatch<RunMany>(p.kind, layout, p, world, ins, outs, n, s);
+}
+
+cudaError_t launch_repeat_angles(const CastParams& p, int layout, const float* ins, const float* angles,
+                                 float* outs, int n, int na, cudaStream_t s) {
+    return dispatch<RunAngles>(p.kind, layout, p, ins, angles, outs, n, na, s);
+}
+
+cudaError_t launch_eval_sensor(const CastParams& p, const SensorDev& sm, const float* obs, const float* ranges,
+                               double* outs, int na, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    int ppb, threads;
+    product_shape(na, 256, ppb, threads);
+    size_t smem = (size_t)ppb * na * sizeof(double);
+    cudaError_t e = set_smem(k_eval_sensor, smem);
+    if (e != cudaSuccess) return e;
+    k_eval_sensor<<<blocks_for(n, ppb), threads, smem, s>>>(p, sm, obs, ranges, outs, na, n, ppb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused(const CastParams& p, int layout, const SensorDev& sm, const float* ins,
+                         const float* angles, const float* obs, double* weights, int n, int na, int block,
+                         cudaStream_t s) {
+    return dispatch<RunFused>(p.kind, layout, p, sm, ins, angles, obs, weights, n, na, block, s);
+}
+
+cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,
+                               unsigned long long* total, cudaStream_t s) {
+    long long rays = (long long)n * na;
+    if (rays <= 0) return cudaSuccess;
+    if (p.kind == K_RM) k_count_steps<K_RM><<<blocks_for(rays, 256), 256, 0, s>>>(p, ins, angles, n, na, total);
+    else if (p.kind == K_BL) k_count_steps<K_BL><<<blocks_for(rays, 256), 256, 0, s>>>(p, ins, angles, n, na, total);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t batch_occupancy(int block, size_t smem, int* blocks_per_sm) {
+    cudaError_t e = set_smem(k_batch, smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch, block, smem);
+}
+
+cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tiles, unsigned* queue, int grid,
+                         int block, size_t smem, cudaStream_t s) {
+    if (total_tiles == 0 || nf == 0) return cudaSuccess;
+    cudaError_t e = set_smem(k_batch, smem);
+    if (e != cudaSuccess) return e;
+    k_batch<<<grid, block, smem, s>>>(d_filters, nf, total_tiles, queue);
+    return cudaGetLastError();
+}
+
+}  // namespace rlc

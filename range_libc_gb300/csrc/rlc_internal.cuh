@@ -1,0 +1,134 @@
+// Internal device structures and kernel launchers of the GB300 ray-casting
+// library.  Everything here is private to librangelibc_gb300.so; the public
+// surface is include/rangelibc.h.
+//
+// Grid layout: the occupancy grid and the distance transform index cells as
+// (x, y) with x < width, y < height -- the reference's OMap::grid[x][y].
+//   * occupancy: 8x8 bit tiles, one uint64 per tile, tiles x-major;
+//     bit ((x & 7) << 3 | (y & 7)) of word (x >> 3) * tiles_y + (y >> 3).
+//   * distance transform: float, either linear x-major (x * height + y,
+//     the reference's kernels.cu:15-17 layout) or 8x8 tiles of 64 floats
+//     (256 B, two 128-B lines) in the same tile order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rlc {
+
+enum Kind : int { K_BL = 0, K_RM = 1, K_CDDT = 2 };
+
+// error flags a kernel can raise (ORed into a per-method device word)
+enum DevFlag : unsigned {
+    F_BL_BOUND = 1u,       // Bresenham loop bound reached (coordinates beyond float's integer range)
+    F_WRAP_BOUND = 2u,     // CDDT heading wrap loop bound reached (|heading| > ~6e5 rad)
+    F_CDDT_PAST_END = 4u,  // forward binary search with x equal to the last zero point
+    F_NAN_INDEX = 8u,      // NaN range/observation mapped to sensor bin 0
+};
+
+enum DtLayout : int { DT_LINEAR = 0, DT_TILED = 1 };
+
+struct MapDev {
+    int W, H;
+    int tiles_y;              // ceil(H / 8)
+    const float* dt;          // distance transform (layout per DtLayout)
+    const uint64_t* bits;     // occupancy bit tiles
+};
+
+struct CddtDev {
+    unsigned td;
+    float td_div_2pi;         // theta_discretization / M_2PI, as float
+    float twopi_div_td;       // M_2PI / theta_discretization, as float
+    const int* widths;        // [td]
+    const float* trans;       // [td]
+    const float* cosv;        // [td] cosf of each discrete angle (host libm)
+    const float* sinv;        // [td]
+    const uint32_t* slice_base;  // [td + 1]
+    const uint32_t* bin_start;   // [total_bins + 1]
+    const float* zeros;
+};
+
+struct WorldDev {
+    float inv_s, s, rc, ox, oy, sa, ca;
+};
+
+struct CastParams {
+    int kind;
+    float mr;
+    MapDev map;
+    CddtDev cddt;
+    WorldDev world;
+    const float* trig;        // optional per-ray (cos, sin) override (parity mode)
+    unsigned* err;            // device error word
+};
+
+struct SensorDev {
+    const double* table;      // K x K row-major, table[r * K + d]
+    int K;
+};
+
+// ---- map preprocessing (rlc_map.cu) ----
+cudaError_t launch_pack_bits(const uint8_t* d_occ, int W, int H, uint64_t* d_bits, cudaStream_t s);
+cudaError_t launch_edt(const uint64_t* d_bits, int W, int H, int tiles_y, float* d_dt_linear,
+                       void* scratch, size_t scratch_bytes, cudaStream_t s);
+size_t edt_scratch_bytes(int W, int H);
+cudaError_t launch_dt_to_tiled(const float* d_lin, int W, int H, float* d_tiled, cudaStream_t s);
+cudaError_t launch_edge_map(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_edge, cudaStream_t s);
+cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_occ, cudaStream_t s);
+
+// ---- casting (rlc_cast.cu) ----
+cudaError_t launch_calc_range_many(const CastParams& p, int layout, bool world, const float* ins,
+                                   float* outs, int n, cudaStream_t s);
+cudaError_t launch_repeat_angles(const CastParams& p, int layout, const float* ins, const float* angles,
+                                 float* outs, int n, int na, cudaStream_t s);
+cudaError_t launch_eval_sensor(const CastParams& p, const SensorDev& sm, const float* obs,
+                               const float* ranges, double* outs, int na, int n, cudaStream_t s);
+cudaError_t launch_fused(const CastParams& p, int layout, const SensorDev& sm, const float* ins,
+                         const float* angles, const float* obs, double* weights, int n, int na,
+                         int block, cudaStream_t s);
+
+// march steps of world-frame repeat-angle rays (RM and BL), summed into *total
+cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,
+                               unsigned long long* total, cudaStream_t s);
+
+// ---- batched multi-filter update (rlc_cast.cu) ----
+struct FilterDev {
+    CastParams p;
+    int layout;
+    SensorDev sm;
+    const float* ins;
+    const float* angles;
+    const float* obs;
+    float* ranges;            // optional pixel ranges
+    double* weights;
+    int n, na, ppb;           // particles, beams, particles per tile
+    unsigned tile_begin;      // first global tile of this filter
+};
+// Persistent launch: `grid` blocks of `block` threads draw tiles from *queue
+// (which must be zero) until all `total_tiles` are done.
+cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tiles, unsigned* queue, int grid,
+                         int block, size_t smem, cudaStream_t s);
+cudaError_t batch_occupancy(int block, size_t smem, int* blocks_per_sm);
+
+// ---- CDDT table (rlc_cddt.cu) ----
+struct CddtBuild {
+    uint32_t* slice_base = nullptr;   // device [td + 1]
+    uint32_t* bin_start = nullptr;    // device [total_bins + 1]
+    float* zeros = nullptr;           // device
+    uint32_t total_bins = 0;
+    uint32_t nzeros = 0;
+};
+// Builds the table on the device; widths/trans/cos/sin are device arrays of td entries,
+// h_slice_base the host copy of the per-slice bin offsets.
+cudaError_t cddt_build(const uint64_t* d_bits, int W, int H, int tiles_y, unsigned td,
+                       const int* d_widths, const float* d_trans, const float* d_cos, const float* d_sin,
+                       const uint32_t* h_slice_base, CddtBuild* out, cudaStream_t s, char* why, size_t why_len);
+cudaError_t cddt_prune(const uint64_t* d_bits, int W, int H, int tiles_y, unsigned td, float max_range,
+                       const int* d_widths, const float* d_trans, const float* d_cos, const float* d_sin,
+                       CddtBuild* tab, cudaStream_t s);
+
+// ---- utilities (rlc_cddt.cu) ----
+// exclusive scan of n uint32 values; d_out[n] receives the total.
+cudaError_t scan_exclusive_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, cudaStream_t s);
+
+}  // namespace rlc

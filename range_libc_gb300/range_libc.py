@@ -1,0 +1,555 @@
+"""Python face of the GB300 library, mirroring range_libc's Cython module.
+
+Class and method names, argument order and meaning follow the reference's
+``pywrapper/RangeLibc.pyx`` (kctess5/range_libc) so that existing callers
+(particle filters written against ``range_libc``) switch by changing the
+import::
+
+    import range_libc_gb300.range_libc as range_libc
+    m = range_libc.PyOMap(occupancy_bool_array)
+    rm = range_libc.PyRayMarchingGPU(m, 200)
+    rm.set_sensor_model(table)
+    rm.calc_range_repeat_angles_eval_sensor_model(particles, angles, obs, weights)
+
+Every call runs on the GPU through the C ABI (include/rangelibc.h).
+Arrays may be numpy arrays (host memory; the call is synchronous, like the
+reference) or CUDA torch tensors (device memory; the call is queued on the
+current torch stream and returns immediately).  Dtypes and layouts are
+those of the reference's typed buffers: float32 C-contiguous poses
+``[N, 3]``, float32 angles/observations/ranges, float64 weights and tables.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import struct
+import sys
+import zlib
+
+import numpy as np
+
+from . import _lib
+from ._lib import call, lib
+
+# module flags of the reference (RangeLibc.pyx:94-102), for the shipped build
+USE_CACHED_TRIG = False
+USE_ALTERNATE_MOD = True
+USE_CACHED_CONSTANTS = True
+USE_FAST_ROUND = False
+NO_INLINE = False
+USE_LRU_CACHE = False
+LRU_CACHE_SIZE = 1000000
+SHOULD_USE_CUDA = True
+
+
+# ---------------------------------------------------------------- arrays
+def _is_device(a) -> bool:
+    return getattr(a, "is_cuda", False) is True
+
+
+def _stream_of(a):
+    import torch  # device arrays are torch tensors
+    return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+
+
+_TORCH_DTYPES = {np.float32: "torch.float32", np.float64: "torch.float64"}
+
+
+def _arg(a, dtype, ndim: int, name: str):
+    """(pointer, is_device) for a reference-typed buffer; raises like a Cython typed buffer."""
+    if _is_device(a):
+        if str(a.dtype) != _TORCH_DTYPES[dtype]:
+            raise ValueError(f"Buffer dtype mismatch for {name}: expected {np.dtype(dtype).name}, got {a.dtype}")
+        if a.dim() != ndim:
+            raise ValueError(f"Buffer has wrong number of dimensions for {name} (expected {ndim}, got {a.dim()})")
+        if not a.is_contiguous():
+            raise ValueError(f"{name} must be C-contiguous")
+        return C.c_void_p(a.data_ptr()), True
+    if not isinstance(a, np.ndarray):
+        raise TypeError(f"{name} must be a numpy.ndarray or a CUDA tensor")
+    if a.dtype != dtype:
+        raise ValueError(f"Buffer dtype mismatch for {name}: expected {np.dtype(dtype).name}, got {a.dtype.name}")
+    if a.ndim != ndim:
+        raise ValueError(f"Buffer has wrong number of dimensions for {name} (expected {ndim}, got {a.ndim})")
+    if not a.flags.c_contiguous:
+        raise ValueError(f"{name} must be C-contiguous")
+    return C.c_void_p(a.ctypes.data), False
+
+
+def _flags_stream(dev_flags, first):
+    devs = set(dev_flags)
+    if len(devs) != 1:
+        raise ValueError("all arrays of one call must be host (numpy) or all device (CUDA) arrays")
+    if devs.pop():
+        return _lib.RLC_DEVICE_PTRS, _stream_of(first)
+    return 0, None
+
+
+# ---------------------------------------------------------------- PNG
+def _read_png_rgba(path: str) -> np.ndarray:
+    """Decode a non-interlaced PNG (grey, RGB, palette, grey+alpha, RGBA; 1-8 bit) to RGBA8 [H, W, 4]."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise IOError(f"{path}: not a PNG file")
+    pos, idat, plte, trns = 8, [], None, None
+    w = h = bd = ct = il = None
+    while pos < len(data):
+        ln, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + ln]
+        pos += 12 + ln
+        if typ == b"IHDR":
+            w, h, bd, ct, _cm, _fm, il = struct.unpack(">IIBBBBB", body)
+        elif typ == b"PLTE":
+            plte = np.frombuffer(body, np.uint8).reshape(-1, 3)
+        elif typ == b"tRNS":
+            trns = body
+        elif typ == b"IDAT":
+            idat.append(body)
+        elif typ == b"IEND":
+            break
+    if il:
+        raise IOError(f"{path}: interlaced PNGs are not supported")
+    channels = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ct]
+    if bd == 16 or (bd < 8 and ct not in (0, 3)):
+        raise IOError(f"{path}: unsupported bit depth {bd} for colour type {ct}")
+    raw = zlib.decompress(b"".join(idat))
+    bpp = max(1, channels * bd // 8)
+    stride = (w * channels * bd + 7) // 8
+    img = np.zeros((h, stride), np.uint8)
+    prev = np.zeros(stride, np.int32)
+    p = 0
+    for y in range(h):
+        ftype = raw[p]
+        line = np.frombuffer(raw, np.uint8, stride, p + 1).astype(np.int32)
+        p += 1 + stride
+        if ftype == 0:
+            cur = line
+        elif ftype == 2:
+            cur = (line + prev) & 255
+        else:
+            cur = np.zeros(stride, np.int32)
+            for i in range(stride):
+                a = cur[i - bpp] if i >= bpp else 0
+                b = prev[i]
+                c = prev[i - bpp] if i >= bpp else 0
+                if ftype == 1:
+                    pred = a
+                elif ftype == 3:
+                    pred = (a + b) >> 1
+                else:
+                    pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                    pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                cur[i] = (line[i] + pred) & 255
+        img[y] = cur
+        prev = cur
+    if bd < 8:
+        bits = np.unpackbits(img, axis=1)[:, : w * bd].reshape(h, w, bd)
+        vals = np.zeros((h, w), np.int32)
+        for k in range(bd):
+            vals = (vals << 1) | bits[:, :, k]
+        samples = vals.astype(np.uint8)
+        if ct == 0:
+            samples = (vals * 255 // ((1 << bd) - 1)).astype(np.uint8)
+        px = samples[:, :, None]
+    else:
+        px = img[:, : w * channels].reshape(h, w, channels)
+    out = np.empty((h, w, 4), np.uint8)
+    if ct == 0:
+        out[..., :3] = px[..., :1]
+        out[..., 3] = 255
+    elif ct == 2:
+        out[..., :3] = px
+        out[..., 3] = 255
+    elif ct == 3:
+        idx = px[..., 0]
+        out[..., :3] = plte[idx]
+        alpha = np.full(256, 255, np.uint8)
+        if trns:
+            alpha[: len(trns)] = np.frombuffer(trns, np.uint8)
+        out[..., 3] = alpha[idx]
+    elif ct == 4:
+        out[..., :3] = px[..., :1]
+        out[..., 3] = px[..., 1]
+    else:
+        out[...] = px
+    return out
+
+
+def _write_png_gray(path: str, gray: np.ndarray) -> None:
+    h, w = gray.shape
+    raw = b"".join(b"\x00" + gray[y].tobytes() for y in range(h))
+
+    def chunk(t, b):
+        return struct.pack(">I", len(b)) + t + b + struct.pack(">I", zlib.crc32(t + b) & 0xFFFFFFFF)
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 0, 0, 0, 0))
+                + chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+
+
+def _quaternion_yaw(q) -> float:
+    x, y, z, w = q.x, q.y, q.z, q.w
+    return float(np.arctan2(2.0 * (w * z + x * y), 1.0 - 2.0 * (y * y + z * z)))
+
+
+# ---------------------------------------------------------------- PyOMap
+class PyOMap:
+    """Occupancy grid (OMap, RangeLib.h:121-322; PyOMap, RangeLibc.pyx:130-197).
+
+    PyOMap(width, height)          empty map
+    PyOMap(path[, threshold])      PNG: grey (0.229 B + 0.587 G + 0.114 R, as the
+                                   reference reads its channels) < threshold is occupied
+    PyOMap(ndarray)                bool array indexed [row, col]; grid[x][y] = arr[y, x]
+    PyOMap(occupancy_grid_msg)     any object shaped like nav_msgs/OccupancyGrid:
+                                   cells > 10 are occupied, world parameters from info
+    """
+
+    def __init__(self, arg1, arg2=None):
+        self._error = False
+        world = (1.0, 0.0, 0.0, 0.0, 0.0, 1.0)
+        if arg1 is not None and arg2 is not None and isinstance(arg1, (int, np.integer)):
+            occ = np.zeros((int(arg1), int(arg2)), np.uint8)
+        elif arg1 is not None and arg2 is not None:
+            occ = self._from_png(str(arg1), float(arg2))
+        elif isinstance(arg1, np.ndarray):
+            occ = np.ascontiguousarray((arg1 != 0).T, dtype=np.uint8)
+        elif hasattr(arg1, "info") and hasattr(arg1, "data"):
+            info = arg1.info
+            width, height = int(info.width), int(info.height)
+            arr = np.asarray(arg1.data, dtype=np.int64).reshape((height, width))
+            occ = np.ascontiguousarray(arr > 10, dtype=np.uint8)
+            angle = -1.0 * _quaternion_yaw(info.origin.orientation)
+            world = (float(info.resolution), angle, float(info.origin.position.x), float(info.origin.position.y),
+                     float(np.sin(angle)), float(np.cos(angle)))
+        elif isinstance(arg1, str):
+            occ = self._from_png(arg1, 128.0)
+        else:
+            print("Failed to construct PyOMap, check argument types.")
+            occ = np.zeros((1, 1), np.uint8)
+        if occ.size == 0:
+            occ = np.zeros((1, 1), np.uint8)
+            self._error = True
+        self._occ = np.ascontiguousarray(occ, dtype=np.uint8)
+        self.world = tuple(float(np.float32(v)) for v in world)
+        h = C.c_void_p()
+        W, H = self._occ.shape
+        call("rlc_map_create", self._occ.ctypes.data_as(_lib._u8p), W, H, C.byref(h))
+        self._h = h
+        call("rlc_map_set_world", self._h, *self.world)
+
+    def _from_png(self, path: str, threshold: float) -> np.ndarray:
+        try:
+            rgba = _read_png_rgba(path)
+        except (IOError, OSError, KeyError, zlib.error, struct.error) as e:
+            print(f"ERROR: {e}")
+            self._error = True
+            return np.zeros((0, 0), np.uint8)
+        # RangeLib.h:188-197: r = image[idx+2], g = image[idx+1], b = image[idx+0]
+        r = rgba[..., 2].astype(np.float32)
+        g = rgba[..., 1].astype(np.float32)
+        b = rgba[..., 0].astype(np.float32)
+        gray = (0.229 * r.astype(np.float64) + 0.587 * g.astype(np.float64) + 0.114 * b.astype(np.float64))
+        gray = gray.astype(np.float32).astype(np.int32)
+        return np.ascontiguousarray((gray < threshold).T, dtype=np.uint8)   # grid[x][y], x = column
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.rlc_map_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_world(self, scale: float, angle: float, origin_x: float, origin_y: float,
+                  sin_angle: float | None = None, cos_angle: float | None = None) -> None:
+        """World parameters of the ROS conversion (the OMap fields the OccupancyGrid path sets).
+
+        Methods copy them when they are created, like the reference's by-value OMap."""
+        if sin_angle is None:
+            sin_angle = float(np.sin(angle))
+        if cos_angle is None:
+            cos_angle = float(np.cos(angle))
+        self.world = tuple(float(np.float32(v)) for v in (scale, angle, origin_x, origin_y, sin_angle, cos_angle))
+        call("rlc_map_set_world", self._h, *self.world)
+
+    @property
+    def occupancy(self) -> np.ndarray:
+        """grid[x][y] as a uint8 array of shape (width, height)."""
+        return self._occ
+
+    def save(self, fn) -> bool:
+        """PNG with white = free, black = occupied (OMap::save, RangeLib.h:263-291)."""
+        gray = np.where(self._occ.T != 0, 0, 255).astype(np.uint8)
+        _write_png_gray(fn if isinstance(fn, str) else fn.decode(), gray)
+        return False   # the reference returns the encoder's error code: 0 = success
+
+    def isOccupied(self, x: int, y: int) -> bool:
+        return bool(self._occ[x, y])
+
+    def error(self) -> bool:
+        return self._error
+
+    def width(self) -> int:
+        return int(self._occ.shape[0])
+
+    def height(self) -> int:
+        return int(self._occ.shape[1])
+
+
+# ---------------------------------------------------------------- methods
+class _RangeMethod:
+    _kind = None
+
+    def __init__(self, Map: PyOMap, max_range: float, theta_disc: int = 0, *, _trig=None):
+        self.map = Map
+        self.max_range = float(np.float32(max_range))
+        self.theta_disc = int(theta_disc)
+        h = C.c_void_p()
+        if _trig is not None:
+            cos_t = np.ascontiguousarray(_trig[0], np.float32)
+            sin_t = np.ascontiguousarray(_trig[1], np.float32)
+            call("rlc_method_create_cddt_trig", Map.handle, self._kind, self.max_range, self.theta_disc,
+                 cos_t.ctypes.data_as(_lib._f32p), sin_t.ctypes.data_as(_lib._f32p), C.byref(h))
+        else:
+            call("rlc_method_create", Map.handle, self._kind, self.max_range, self.theta_disc, C.byref(h))
+        self._h = h
+        self._table_width = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.rlc_method_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    # RangeMethod::calc_range -- one ray in grid space (no world transform)
+    def calc_range(self, x: float, y: float, heading: float) -> float:
+        out = C.c_float()
+        call("rlc_calc_range", self._h, float(x), float(y), float(heading), C.byref(out))
+        return out.value
+
+    def calc_range_many(self, ins, outs) -> None:
+        pi, di = _arg(ins, np.float32, 2, "ins")
+        po, do = _arg(outs, np.float32, 1, "outs")
+        flags, stream = _flags_stream([di, do], ins)
+        n = outs.shape[0]
+        if n and ins.shape[0] < n:
+            raise ValueError("ins has fewer rows than outs")
+        call("rlc_calc_range_many", self._h, pi, po, n, flags, stream)
+
+    def calc_range_repeat_angles(self, ins, angles, outs) -> None:
+        pi, di = _arg(ins, np.float32, 2, "ins")
+        pa, da = _arg(angles, np.float32, 1, "angles")
+        po, do = _arg(outs, np.float32, 1, "outs")
+        flags, stream = _flags_stream([di, da, do], ins)
+        n, na = ins.shape[0], angles.shape[0]
+        if outs.shape[0] < n * na:
+            raise ValueError(f"outs needs {n * na} entries")
+        call("rlc_calc_range_repeat_angles", self._h, pi, pa, po, n, na, flags, stream)
+
+    def set_sensor_model(self, table) -> None:
+        if not isinstance(table, np.ndarray) or table.dtype != np.float64 or table.ndim != 2:
+            raise ValueError("Buffer dtype mismatch: the sensor model is a 2-D float64 array")
+        if not table.shape[0] == table.shape[1]:
+            print("Sensor model must have equal matrix dimensions, failing!")
+            return
+        t = np.ascontiguousarray(table)
+        call("rlc_set_sensor_model", self._h, t.ctypes.data_as(_lib._f64p), t.shape[0])
+        self._table_width = t.shape[0]
+
+    def eval_sensor_model(self, observation, ranges, outs, num_rays: int, num_particles: int) -> None:
+        po, do = _arg(observation, np.float32, 1, "observation")
+        pr, dr = _arg(ranges, np.float32, 1, "ranges")
+        pw, dw = _arg(outs, np.float64, 1, "outs")
+        flags, stream = _flags_stream([do, dr, dw], observation)
+        if observation.shape[0] < num_rays or ranges.shape[0] < num_rays * num_particles or outs.shape[0] < num_particles:
+            raise ValueError("array shorter than num_rays / num_particles")
+        call("rlc_eval_sensor_model", self._h, po, pr, pw, int(num_rays), int(num_particles), flags, stream)
+
+    def calc_range_repeat_angles_eval_sensor_model(self, ins, angles, obs, weights) -> None:
+        pi, di = _arg(ins, np.float32, 2, "ins")
+        pa, da = _arg(angles, np.float32, 1, "angles")
+        po, do = _arg(obs, np.float32, 1, "obs")
+        pw, dw = _arg(weights, np.float64, 1, "weights")
+        flags, stream = _flags_stream([di, da, do, dw], ins)
+        n, na = ins.shape[0], angles.shape[0]
+        if obs.shape[0] < na or weights.shape[0] < n:
+            raise ValueError("obs needs one entry per angle and weights one per particle")
+        call("rlc_calc_range_repeat_angles_eval_sensor_model", self._h, pi, pa, po, pw, n, na, flags, stream)
+
+    def saveTrace(self, path) -> float:
+        print("WARNING: trace map not generated, must compile with trace support enabled.")
+        return 0.0
+
+    # ---- extras (no reference counterpart) ----
+    def device_flags(self) -> int:
+        f = C.c_uint()
+        call("rlc_method_device_flags", self._h, C.byref(f))
+        return f.value
+
+    def set_trig_override(self, trig) -> None:
+        """Parity mode: per-ray (cos, sin) used by the next BL/RM queries (None restores sincosf)."""
+        if trig is None:
+            call("rlc_method_set_trig_override", self._h, None, 0)
+            return
+        t = np.ascontiguousarray(trig, np.float32).reshape(-1, 2)
+        self._trig = t
+        call("rlc_method_set_trig_override", self._h, t.ctypes.data_as(_lib._f32p), t.shape[0])
+
+    def count_steps(self, ins, angles) -> int:
+        """Total march steps of the repeat-angle rays (RM: DT reads; BL: cells tested)."""
+        pi, di = _arg(ins, np.float32, 2, "ins")
+        pa, da = _arg(angles, np.float32, 1, "angles")
+        flags, _ = _flags_stream([di, da], ins)
+        tot = C.c_int64()
+        call("rlc_count_steps", self._h, pi, pa, ins.shape[0], angles.shape[0], flags, C.byref(tot))
+        return tot.value
+
+    def set_schedule(self, dt_layout: int = 0, fused_block: int = 0) -> None:
+        call("rlc_method_set_schedule", self._h, int(dt_layout), int(fused_block))
+
+    def schedule(self):
+        a, b = C.c_int(), C.c_int()
+        call("rlc_method_get_schedule", self._h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+
+class PyBresenhamsLine(_RangeMethod):
+    """BresenhamsLine (RangeLib.h:691-772; RangeLibc.pyx:200-225)."""
+    _kind = _lib.RLC_BL
+
+    def __init__(self, Map: PyOMap, max_range: float):
+        super().__init__(Map, max_range)
+
+
+class PyRayMarching(_RangeMethod):
+    """RayMarching (RangeLib.h:922-969; RangeLibc.pyx:227-251)."""
+    _kind = _lib.RLC_RM
+
+    def __init__(self, Map: PyOMap, max_range: float):
+        super().__init__(Map, max_range)
+
+
+class PyCDDTCast(_RangeMethod):
+    """CDDTCast (RangeLib.h:971-1770; RangeLibc.pyx:253-287); the table is built on the GPU."""
+    _kind = _lib.RLC_CDDT
+
+    def __init__(self, Map: PyOMap, max_range: float, theta_disc: int, *, trig=None):
+        super().__init__(Map, max_range, theta_disc, _trig=trig)
+
+    def prune(self, max_range: float = -1.0) -> None:
+        call("rlc_cddt_prune", self._h, self.max_range if max_range < 0.0 else float(max_range))
+
+    def table(self):
+        """(widths[td], translations[td], bin_len[num_bins], zeros) -- compressed_lut in CSR form."""
+        nb, nz = C.c_int64(), C.c_int64()
+        call("rlc_cddt_table_size", self._h, C.byref(nb), C.byref(nz))
+        widths = np.empty(self.theta_disc, np.int32)
+        trans = np.empty(self.theta_disc, np.float32)
+        bin_len = np.empty(nb.value, np.int64)
+        zeros = np.empty(max(nz.value, 1), np.float32)
+        call("rlc_cddt_table_export", self._h, widths.ctypes.data_as(_lib._i32p), trans.ctypes.data_as(_lib._f32p),
+             bin_len.ctypes.data_as(_lib._i64p), zeros.ctypes.data_as(_lib._f32p))
+        return widths, trans, bin_len, zeros[: nz.value]
+
+    def load_table(self, trans, bin_len, zeros) -> None:
+        trans = np.ascontiguousarray(trans, np.float32)
+        bin_len = np.ascontiguousarray(bin_len, np.int64)
+        zeros = np.ascontiguousarray(zeros, np.float32)
+        call("rlc_cddt_table_load", self._h, trans.ctypes.data_as(_lib._f32p), bin_len.ctypes.data_as(_lib._i64p),
+             zeros.ctypes.data_as(_lib._f32p), len(zeros))
+
+    def calc_range_many_radial_optimized(self, num_rays, min_angle, max_angle, ins, outs):
+        raise NotImplementedError("calc_range_many_radial_optimized is not part of the GPU path")
+
+
+class PyRayMarchingGPU(_RangeMethod):
+    """RayMarchingGPU (RangeLib.h:774-920; RangeLibc.pyx:314-340)."""
+    _kind = _lib.RLC_RMGPU
+
+    def __init__(self, Map: PyOMap, max_range: float):
+        super().__init__(Map, max_range)
+
+
+class PyNull:
+    """Call-overhead probe of the reference (RangeLibc.pyx:342-351)."""
+
+    def __init__(self, Map, max_range, theta_disc):
+        pass
+
+    def calc_range(self, x, y, heading):
+        return x + y + heading
+
+    def calc_range_many(self, ins, outs):
+        a = ins[0, 0]
+        b = outs[0]
+        c = outs.shape[0]
+        return a, b, c
+
+
+# ---------------------------------------------------------------- batch
+class PyFilterBatch:
+    """Many particle filters updated by one persistent launch, replayed as a CUDA graph.
+
+    filters: list of (method, ins, angles, obs, weights[, ranges]) with CUDA tensors;
+    every method needs its sensor model set.  run() queues the whole update on
+    the current stream.  No reference counterpart.
+    """
+
+    def __init__(self, filters, block: int = 0):
+        self._keep = []
+        descs = (_lib.FilterDesc * len(filters))()
+        for i, f in enumerate(filters):
+            method, ins, angles, obs, weights = f[:5]
+            ranges = f[5] if len(f) > 5 else None
+            for a, dt, nd, nm in ((ins, np.float32, 2, "ins"), (angles, np.float32, 1, "angles"),
+                                  (obs, np.float32, 1, "obs"), (weights, np.float64, 1, "weights")):
+                if not _arg(a, dt, nd, nm)[1]:
+                    raise ValueError("batched filters take CUDA tensors")
+            d = descs[i]
+            d.method = method.handle
+            d.ins, d.angles, d.obs, d.weights = ins.data_ptr(), angles.data_ptr(), obs.data_ptr(), weights.data_ptr()
+            d.ranges = ranges.data_ptr() if ranges is not None else None
+            d.n_particles, d.n_angles = ins.shape[0], angles.shape[0]
+            self._keep.append((method, ins, angles, obs, weights, ranges))
+        h = C.c_void_p()
+        call("rlc_batch_create", descs, len(filters), int(block), C.byref(h))
+        self._h = h
+        self._device = filters[0][1].device
+
+    def run(self) -> None:
+        call("rlc_batch_run", self._h, _stream_of(self._keep[0][1]))
+
+    def info(self):
+        r, t = C.c_int64(), C.c_int64()
+        call("rlc_batch_info", self._h, C.byref(r), C.byref(t))
+        return r.value, t.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.rlc_batch_destroy(h)
+            self._h = None
+
+
+def device_count() -> int:
+    return lib().rlc_device_count()
+
+
+def library_path() -> str:
+    return _lib.library_path()
+
+
+__all__ = [
+    "PyOMap", "PyBresenhamsLine", "PyRayMarching", "PyCDDTCast", "PyRayMarchingGPU", "PyNull",
+    "PyFilterBatch", "USE_CACHED_TRIG", "USE_ALTERNATE_MOD", "USE_CACHED_CONSTANTS", "USE_FAST_ROUND",
+    "NO_INLINE", "USE_LRU_CACHE", "LRU_CACHE_SIZE", "SHOULD_USE_CUDA",
+]
+
+if __name__ == "__main__":  # pragma: no cover
+    print(library_path(), device_count(), file=sys.stderr)

@@ -1,0 +1,377 @@
+"""Parity of the CUDA library against the CPU oracle on the same inputs.
+
+Bit-exact for the distance transform, the edge map, the CDDT tables and
+every range and weight when the per-ray cos/sin of BL and RM are the
+oracle's (parity mode).  With the device's own sincosf, ranges may differ
+where a last-bit difference of cos/sin moves a ray across a cell corner;
+that is bounded below.
+"""
+import numpy as np
+import pytest
+
+from range_libc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+MAPS = {}
+
+
+def _map(name):
+    if name in MAPS:
+        return MAPS[name]
+    if name == "single_occ":
+        occ = np.ones((1, 1), np.uint8)
+    elif name == "single_free":
+        occ = np.zeros((1, 1), np.uint8)
+    elif name == "quad":
+        occ = np.array([[1, 0], [0, 0]], np.uint8)
+    elif name == "small_5x6":
+        occ = (np.random.default_rng(3).random((5, 6)) < 0.3).astype(np.uint8)
+    elif name == "empty_40x25":
+        occ = np.zeros((40, 25), np.uint8)
+    elif name == "rect_128":
+        occ = W.rect_disk_map(128, 21)
+    elif name == "rect_200x120":
+        occ = np.ascontiguousarray(W.rect_disk_map(256, 22)[:200, :120])
+    elif name == "corridor_512":
+        occ = W.corridor_map(512, 23)
+    else:
+        raise KeyError(name)
+    MAPS[name] = occ
+    return occ
+
+
+def _pymap(rl, occ, world=None):
+    m = rl.PyOMap(np.ascontiguousarray(occ.T))
+    assert np.array_equal(m.occupancy, occ)
+    if world is not None:
+        m.set_world(*world[:4])
+    return m
+
+
+def _queries(occ, n, seed, spread=0.0):
+    rng = np.random.default_rng(seed)
+    W_, H_ = occ.shape
+    q = np.empty((n, 3), np.float32)
+    q[:, 0] = rng.uniform(-spread, W_ + spread, n)
+    q[:, 1] = rng.uniform(-spread, H_ + spread, n)
+    q[:, 2] = rng.uniform(-7.0, 7.0, n)
+    return q
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32 if a.dtype == np.float32 else np.uint64)
+
+
+ALL_MAPS = ["single_occ", "single_free", "quad", "small_5x6", "empty_40x25", "rect_128", "rect_200x120",
+            "corridor_512"]
+
+
+@pytest.mark.parametrize("name", ALL_MAPS)
+def test_distance_transform_and_edge_map(rl, oracle_mod, name):
+    occ = _map(name)
+    m = _pymap(rl, occ)
+    dt = np.empty(occ.shape, np.float32)
+    rl._lib.call("rlc_map_distance_transform", m.handle, dt.ctypes.data_as(rl._lib._f32p))
+    assert np.array_equal(_bits(dt), _bits(oracle_mod.edt(occ)))
+    edge = np.empty(occ.shape, np.uint8)
+    rl._lib.call("rlc_map_edge_map", m.handle, edge.ctypes.data_as(rl._lib._u8p))
+    assert np.array_equal(edge, oracle_mod.edge_map(occ))
+
+
+def test_distance_transform_large_map(rl, oracle_mod):
+    # 2048^2: the pass-2 sums f + q^2 exceed 2^24 and round in float
+    occ = W.rect_disk_map(2048, 31)
+    m = _pymap(rl, occ)
+    dt = np.empty(occ.shape, np.float32)
+    rl._lib.call("rlc_map_distance_transform", m.handle, dt.ctypes.data_as(rl._lib._f32p))
+    assert np.array_equal(_bits(dt), _bits(oracle_mod.edt(occ)))
+
+
+WORLDS = {
+    "identity": (1.0, 0.0, 0.0, 0.0),
+    "ros": (0.05, 0.0, -3.25, -1.5),
+    "rotated": (0.1, 0.7, 2.0, -1.0),
+}
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm"])
+@pytest.mark.parametrize("name", ["small_5x6", "rect_128", "rect_200x120", "corridor_512"])
+@pytest.mark.parametrize("wname", list(WORLDS))
+def test_calc_range_many_parity_mode(rl, oracle_mod, kind, name, wname):
+    occ = _map(name)
+    m = _pymap(rl, occ, WORLDS[wname])
+    mr = 120.0
+    cls = rl.PyBresenhamsLine if kind == "bl" else rl.PyRayMarching
+    g = cls(m, mr)
+    ref = oracle_mod.OracleMethod(occ, kind, mr, world=m.world)
+    s = m.world[0]
+    q = _queries(occ, 4000, 5, spread=3.0)
+    q[:, :2] *= s
+    _, trig = oracle_mod.world_rays(m.world, q)
+    g.set_trig_override(trig)
+    out = np.empty(len(q), np.float32)
+    g.calc_range_many(q, out)
+    assert np.array_equal(_bits(out), _bits(ref.calc_range_many(q)))
+    # raw calc_range semantics (no world transform)
+    qr = _queries(occ, 4000, 6, spread=3.0)
+    trig_raw = np.stack([np.cos(qr[:, 2].astype(np.float64)), np.sin(qr[:, 2].astype(np.float64))], 1)
+    trig_raw = trig_raw.astype(np.float32)
+    g.set_trig_override(trig_raw)
+    out2 = np.empty(len(qr), np.float32)
+    rl._lib.call("rlc_calc_range_many", g.handle, qr.ctypes.data, out2.ctypes.data, len(qr), rl._lib.RLC_NO_WORLD,
+                 None)
+    exp2 = np.array([ref.calc_range_trig(float(a), float(b), float(c), float(d))
+                     for (a, b, _), (c, d) in zip(qr, trig_raw)], np.float32)
+    assert np.array_equal(_bits(out2), _bits(exp2))
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm"])
+def test_calc_range_many_device_trig(rl, oracle_mod, kind):
+    """Device sincosf: ranges equal the oracle's except where cos/sin differ in the last bit."""
+    occ = _map("corridor_512")
+    m = _pymap(rl, occ)
+    g = (rl.PyBresenhamsLine if kind == "bl" else rl.PyRayMarching)(m, 300.0)
+    ref = oracle_mod.OracleMethod(occ, kind, 300.0)
+    q = W.free_cell_queries(occ, 100_000, 9)
+    out = np.empty(len(q), np.float32)
+    g.calc_range_many(q, out)
+    exp = ref.calc_range_many(q)
+    frac = np.mean(_bits(out) != _bits(exp))
+    assert frac < 1e-3, f"{frac:.2e} of rays differ"
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm", "cddt"])
+def test_repeat_angles_parity(rl, oracle_mod, kind):
+    occ = _map("corridor_512")
+    world = WORLDS["ros"]
+    m = _pymap(rl, occ, world)
+    mr = 150.0
+    if kind == "cddt":
+        g = rl.PyCDDTCast(m, mr, 108)
+    else:
+        g = (rl.PyBresenhamsLine if kind == "bl" else rl.PyRayMarching)(m, mr)
+    ref = oracle_mod.OracleMethod(occ, kind, mr, td=108, world=m.world)
+    fs = W.free_cell_queries(occ, 300, 12)
+    xw, yw = W.grid_to_world(fs[:, 0], fs[:, 1], m.world)
+    ins = np.stack([xw, yw, fs[:, 2]], 1).astype(np.float32)
+    angles = W.laser_angles(61)
+    if kind != "cddt":
+        _, trig = oracle_mod.world_rays(m.world, ins, angles)
+        g.set_trig_override(trig)
+    out = np.empty(len(ins) * len(angles), np.float32)
+    g.calc_range_repeat_angles(ins, angles, out)
+    assert np.array_equal(_bits(out), _bits(ref.calc_range_repeat_angles(ins, angles)))
+
+
+@pytest.mark.parametrize("name", ["quad", "small_5x6", "rect_128", "rect_200x120", "corridor_512"])
+@pytest.mark.parametrize("td", [16, 108, 107, 216])
+def test_cddt_table_and_queries(rl, oracle_mod, name, td):
+    occ = _map(name)
+    m = _pymap(rl, occ)
+    mr = 100.0
+    for pruned in (False, True):
+        g = rl.PyCDDTCast(m, mr, td)
+        ref = oracle_mod.OracleMethod(occ, "cddt", mr, td=td)
+        if pruned:
+            g.prune()
+            ref.prune()
+        gw, gt, gl, gz = g.table()
+        rw, rt, rlen, rz = ref.cddt_table()
+        assert np.array_equal(gw, rw) and np.array_equal(_bits(gt), _bits(rt))
+        assert np.array_equal(gl, rlen)
+        assert np.array_equal(_bits(gz), _bits(rz))
+        q = W.free_cell_queries(occ, 3000, 4) if occ.min() == 0 else _queries(occ, 3000, 4)
+        q[:, 2] = np.random.default_rng(td).uniform(-10, 10, len(q))
+        out = np.empty(len(q), np.float32)
+        g.calc_range_many(q, out)
+        assert np.array_equal(_bits(out), _bits(ref.calc_range_many(q)))
+
+
+def test_cddt_given_table(rl, oracle_mod):
+    """Queries over a table loaded from outside equal the oracle's over the same table."""
+    occ = _map("rect_128")
+    m = _pymap(rl, occ)
+    ref = oracle_mod.OracleMethod(occ, "cddt", 100.0, td=108)
+    w, t, bl, z = ref.cddt_table()
+    # drop every third zero point: a table unlike the one built here
+    keep = np.ones(len(z), bool)
+    keep[::3] = False
+    starts = np.concatenate([[0], np.cumsum(bl)])
+    seg = np.repeat(np.arange(len(bl)), bl)
+    bl2 = np.bincount(seg[keep], minlength=len(bl)).astype(np.int64)
+    z2 = z[keep]
+    assert starts[-1] == len(z)
+    ref.load_cddt_table(w, t, bl2, z2)
+    g = rl.PyCDDTCast(m, 100.0, 108)
+    g.load_table(t, bl2, z2)
+    q = W.free_cell_queries(occ, 5000, 8)
+    out = np.empty(len(q), np.float32)
+    g.calc_range_many(q, out)
+    assert np.array_equal(_bits(out), _bits(ref.calc_range_many(q)))
+
+
+def _pf(seed=2000, side=512, n=256, m=61, mr=200.0):
+    return W.particle_filter_step(side=side, n_particles=n, n_beams=m, max_range_px=mr, seed=seed,
+                                  origin=(-1.25, -2.5))
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm", "cddt", "pcddt"])
+def test_sensor_model_and_fused_parity(rl, oracle_mod, kind):
+    wl = _pf()
+    m = _pymap(rl, wl.occ, wl.world)
+    if kind in ("cddt", "pcddt"):
+        g = rl.PyCDDTCast(m, wl.max_range, 108)
+        if kind == "pcddt":
+            g.prune()
+    else:
+        g = {"bl": rl.PyBresenhamsLine, "rm": rl.PyRayMarchingGPU}[kind](m, wl.max_range)
+    ref = oracle_mod.OracleMethod(wl.occ, kind, wl.max_range, td=108, world=m.world)
+    g.set_sensor_model(wl.table)
+    ref.set_sensor_model(wl.table)
+    if kind in ("bl", "rm"):
+        _, trig = oracle_mod.world_rays(m.world, wl.ins, wl.angles)
+        g.set_trig_override(trig)
+    n, na = len(wl.ins), len(wl.angles)
+    ranges = np.empty(n * na, np.float32)
+    g.calc_range_repeat_angles(wl.ins, wl.angles, ranges)
+    exp_ranges = ref.calc_range_repeat_angles(wl.ins, wl.angles)
+    assert np.array_equal(_bits(ranges), _bits(exp_ranges))
+    w = np.empty(n, np.float64)
+    g.eval_sensor_model(wl.obs, ranges, w, na, n)
+    assert np.array_equal(_bits(w), _bits(ref.eval_sensor_model(wl.obs, exp_ranges, na, n)))
+    wf = np.empty(n, np.float64)
+    g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, wf)
+    assert np.array_equal(_bits(wf), _bits(ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs)))
+
+
+def test_fused_many_beams_underflow(rl, oracle_mod):
+    """1,081 beams: products reach subnormals and zero; the in-order product stays bit-exact."""
+    wl = _pf(n=64, m=1081)
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyRayMarching(m, wl.max_range)
+    ref = oracle_mod.OracleMethod(wl.occ, "rm", wl.max_range, world=m.world)
+    g.set_sensor_model(wl.table)
+    ref.set_sensor_model(wl.table)
+    _, trig = oracle_mod.world_rays(m.world, wl.ins, wl.angles)
+    g.set_trig_override(trig)
+    obs = np.resize(wl.obs, len(wl.angles)).astype(np.float32)
+    wf = np.empty(len(wl.ins), np.float64)
+    g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, obs, wf)
+    exp = ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, obs)
+    assert np.array_equal(_bits(wf), _bits(exp))
+
+
+def test_fused_device_trig_weights(rl, oracle_mod):
+    """Production mode (device sincosf) on the particle-filter step: weights within 1e-6 relative
+    wherever every range of the particle equals the oracle's."""
+    wl = _pf(n=1000)
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyRayMarchingGPU(m, wl.max_range)
+    ref = oracle_mod.OracleMethod(wl.occ, "rm", wl.max_range, world=m.world)
+    g.set_sensor_model(wl.table)
+    ref.set_sensor_model(wl.table)
+    wf = np.empty(len(wl.ins), np.float64)
+    g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, wf)
+    exp = ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs)
+    rel = np.abs(wf - exp) / np.maximum(np.abs(exp), 1e-300)
+    assert np.mean(rel <= 1e-6) >= 0.99
+
+
+def test_device_pointer_path(rl, oracle_mod):
+    torch = pytest.importorskip("torch")
+    wl = _pf(n=500)
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyRayMarchingGPU(m, wl.max_range)
+    g.set_sensor_model(wl.table)
+    host_w = np.empty(len(wl.ins), np.float64)
+    g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, host_w)
+    dev = torch.device("cuda:0")
+    ins, ang, obs = (torch.from_numpy(a).to(dev) for a in (wl.ins, wl.angles, wl.obs))
+    w = torch.empty(len(wl.ins), dtype=torch.float64, device=dev)
+    g.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs, w)
+    torch.cuda.synchronize()
+    assert np.array_equal(w.cpu().numpy(), host_w)
+    r = torch.empty(len(wl.ins) * len(wl.angles), dtype=torch.float32, device=dev)
+    g.calc_range_repeat_angles(ins, ang, r)
+    hr = np.empty(r.numel(), np.float32)
+    g.calc_range_repeat_angles(wl.ins, wl.angles, hr)
+    torch.cuda.synchronize()
+    assert np.array_equal(r.cpu().numpy(), hr)
+
+
+def test_edge_cases(rl, oracle_mod):
+    occ = _map("rect_128")
+    m = _pymap(rl, occ)
+    g = rl.PyRayMarching(m, 50.0)
+    b = rl.PyBresenhamsLine(m, 50.0)
+    # empty batches
+    g.calc_range_many(np.zeros((0, 3), np.float32), np.zeros(0, np.float32))
+    g.set_sensor_model(W.sensor_table(51))
+    w = np.full(4, -1.0)
+    g.calc_range_repeat_angles_eval_sensor_model(np.zeros((4, 3), np.float32), np.zeros(0, np.float32),
+                                                 np.zeros(0, np.float32), w)
+    assert np.all(w == 1.0)   # empty product
+    # non-finite poses return max_range, never fault
+    q = np.array([[np.nan, 5, 0], [5, np.nan, 0], [5, 5, np.nan], [np.inf, 5, 0], [1e30, -1e30, 1.0],
+                  [-3.0, 200.0, 2.0]], np.float32)
+    for meth in (g, b):
+        out = np.empty(len(q), np.float32)
+        meth.calc_range_many(q, out)
+        assert np.all(np.isfinite(out))
+    ref = oracle_mod.OracleMethod(occ, "rm", 50.0)
+    out = np.empty(len(q), np.float32)
+    g.calc_range_many(q, out)
+    assert np.array_equal(_bits(out), _bits(ref.calc_range_many(q)))
+
+
+def test_argument_errors(rl):
+    occ = _map("rect_128")
+    m = _pymap(rl, occ)
+    g = rl.PyRayMarching(m, 50.0)
+    with pytest.raises(rl._lib.RangeLibError):
+        g.calc_range_repeat_angles_eval_sensor_model(np.zeros((2, 3), np.float32), np.zeros(3, np.float32),
+                                                     np.zeros(3, np.float32), np.zeros(2))
+    with pytest.raises(ValueError):
+        g.calc_range_many(np.zeros((2, 3), np.float64), np.zeros(2, np.float32))
+    g.set_sensor_model(np.ones((3, 4)))   # non-square: reference prints and returns
+    with pytest.raises(rl._lib.RangeLibError):
+        rl.PyCDDTCast(m, 50.0, 1)
+
+
+def test_batch_matches_per_filter_calls(rl, oracle_mod):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    specs = [W.FilterSpec(256, 300, 45, 120.0, 51), W.FilterSpec(512, 40, 700, 250.0, 52),
+             W.FilterSpec(128, 1000, 30, 60.0, 53), W.FilterSpec(256, 7, 300, 90.0, 54)]
+    kinds = ["rm", "bl", "cddt", "rm"]
+    filters, expect, keep = [], [], []
+    for spec, kind in zip(specs, kinds):
+        wl = W.batch_filter(spec)
+        m = _pymap(rl, wl.occ)
+        if kind == "cddt":
+            g = rl.PyCDDTCast(m, wl.max_range, 108)
+        else:
+            g = (rl.PyBresenhamsLine if kind == "bl" else rl.PyRayMarching)(m, wl.max_range)
+        g.set_sensor_model(wl.table)
+        w = np.empty(len(wl.ins), np.float64)
+        g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, w)
+        r = np.empty(len(wl.ins) * len(wl.angles), np.float32)
+        g.calc_range_repeat_angles(wl.ins, wl.angles, r)
+        expect.append((w, r / np.float32(1.0)))
+        t = [torch.from_numpy(a).to(dev) for a in (wl.ins, wl.angles, wl.obs)]
+        tw = torch.zeros(len(wl.ins), dtype=torch.float64, device=dev)
+        tr = torch.zeros(len(wl.ins) * len(wl.angles), dtype=torch.float32, device=dev)
+        filters.append((g, t[0], t[1], t[2], tw, tr))
+        keep.append(m)
+    batch = rl.PyFilterBatch(filters)
+    rays, tiles = batch.info()
+    assert rays == sum(len(f[1]) * len(f[2]) for f in filters) and tiles > 0
+    for _ in range(3):   # graph replays
+        for f in filters:
+            f[4].zero_()
+        batch.run()
+        torch.cuda.synchronize()
+        for f, (w, r) in zip(filters, expect):
+            assert np.array_equal(f[4].cpu().numpy(), w)
+            assert np.array_equal(f[5].cpu().numpy(), r)
