@@ -690,8 +690,8 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
 int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block) {
     if (int rc = check_method(m)) return rc;
     if (dt_layout < -1 || dt_layout > 1) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0 or 1");
-    if (fused_block != 0 && (fused_block < 32 || fused_block > 1024 || fused_block % 32))
-        return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 1024]");
+    if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
+        return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
     if (dt_layout == -1) m->autotune_pending = true;
     else m->layout = dt_layout;
     if (fused_block) m->fused_block = fused_block;

@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
 }
 
 // RangeLib.h:533-555: the weight is the product over beams in beam order
-__global__ void __launch_bounds__(256) k_eval_sensor(CastParams p, SensorDev sm, const float* __restrict__ obs,
+__global__ void __launch_bounds__(512) k_eval_sensor(CastParams p, SensorDev sm, const float* __restrict__ obs,
                                                      const float* __restrict__ ranges, double* __restrict__ outs,
                                                      int na, int n, int ppb) {
     extern __shared__ double fac[];
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256) k_eval_sensor(CastParams p, SensorDev sm,
 // RangeLib.h:558-612: ranges stay in pixels; factors are staged in shared
 // memory and multiplied in beam order so the weight is bit-identical.
 template <int KIND, int LAYOUT>
-__global__ void __launch_bounds__(256) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
+__global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
                                                const float* __restrict__ angles, const float* __restrict__ obs,
                                                double* __restrict__ weights, int n, int na, int ppb) {
     extern __shared__ double fac[];
