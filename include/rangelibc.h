@@ -172,6 +172,23 @@ RLC_API int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fu
 RLC_API int rlc_method_autotune(rlc_method* m, const float* d_ins, const float* d_angles, const float* d_obs,
                                 double* d_weights, int n, int num_angles, void* stream);
 
+/* ---- distance transform without device allocation ----------------------------
+ * No counterpart in the reference.  For callers that may not call cudaMalloc (real-time
+ * loops that forbid allocation after start-up; hosts whose device memory belongs to another
+ * allocator): computes the same distance transform as rlc_map_distance_transform from a
+ * device occupancy grid d_occ[x * height + y] (uint8, != 0 occupied) into device memory
+ * d_dt[x * height + y] (float), asynchronously on `stream`, allocating nothing.  Its
+ * scratch is a fixed device array of RLC_NOALLOC_SCRATCH_BYTES that every GPU loading this
+ * library holds until exit; maps beyond RLC_NOALLOC_MAX_CELLS cells or RLC_NOALLOC_MAX_SIDE
+ * per side are rejected with RLC_ERR_ARG.  The first call on a device looks up the array's
+ * address there (make it before any stream capture).  Calls share the array: calls that
+ * overlap on the GPU race and corrupt each other's results. */
+#define RLC_NOALLOC_MAX_CELLS 1048576
+#define RLC_NOALLOC_MAX_SIDE 4096
+#define RLC_NOALLOC_SCRATCH_BYTES 16949760
+RLC_API int rlc_distance_transform_noalloc(const uint8_t* d_occ, int width, int height, float* d_dt,
+                                           void* stream);
+
 /* ---- batched multi-filter particle update (no reference counterpart) --------
  * Many independent filters, each a method (RM or BL or CDDT) with its own map, poses,
  * beams, observation and sensor table, run as one persistent launch that draws

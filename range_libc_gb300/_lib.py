@@ -75,6 +75,7 @@ SIGNATURES = {
     "rlc_method_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int]),
     "rlc_method_get_schedule": (C.c_int, [_vp, _i32p, _i32p]),
     "rlc_method_autotune": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "rlc_distance_transform_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "rlc_batch_create": (C.c_int, [C.POINTER(FilterDesc), C.c_int, C.c_int, C.POINTER(_vp)]),
     "rlc_batch_run": (C.c_int, [_vp, _vp]),
     "rlc_batch_destroy": (C.c_int, [_vp]),

@@ -46,6 +46,11 @@ constexpr double kEps = 0.00001;          // RangeLib.h:60
 
 }  // namespace
 
+int rlc::set_last_error(int code, const char* msg) {
+    g_err = msg ? msg : "";
+    return code;
+}
+
 struct rlc_map {
     int device = 0;
     int W = 0, H = 0, TY = 0;

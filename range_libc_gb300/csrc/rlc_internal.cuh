@@ -72,6 +72,10 @@ cudaError_t launch_pack_bits(const uint8_t* d_occ, int W, int H, uint64_t* d_bit
 cudaError_t launch_edt(const uint64_t* d_bits, int W, int H, int tiles_y, float* d_dt_linear,
                        void* scratch, size_t scratch_bytes, cudaStream_t s);
 size_t edt_scratch_bytes(int W, int H);
+// upper bound of edt_scratch_bytes(W, H) over all W * H <= cells with W, H <= side
+constexpr size_t edt_scratch_bound(size_t cells, size_t side) {
+    return ((cells * 4 + 255) & ~(size_t)255) + cells * 4 + (cells + side) * 8 + 256;
+}
 cudaError_t launch_dt_to_tiled(const float* d_lin, int W, int H, float* d_tiled, cudaStream_t s);
 cudaError_t launch_edge_map(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_edge, cudaStream_t s);
 cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_occ, cudaStream_t s);
@@ -126,6 +130,10 @@ cudaError_t cddt_build(const uint64_t* d_bits, int W, int H, int tiles_y, unsign
 cudaError_t cddt_prune(const uint64_t* d_bits, int W, int H, int tiles_y, unsigned td, float max_range,
                        const int* d_widths, const float* d_trans, const float* d_cos, const float* d_sin,
                        CddtBuild* tab, cudaStream_t s);
+
+// ---- error reporting (rlc_api.cu) ----
+// records `msg` as the calling thread's rlc_last_error() text and returns `code`
+int set_last_error(int code, const char* msg);
 
 // ---- utilities (rlc_cddt.cu) ----
 // exclusive scan of n uint32 values; d_out[n] receives the total.

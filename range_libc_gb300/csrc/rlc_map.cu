@@ -9,9 +9,12 @@
 // f[q] + q*q are float (they round above 2^24, which matters on 4096^2
 // maps), breakpoints are double, and the per-line output is a float.
 // Pass 1 runs along y for every x, pass 2 along x for every y.
+#include "rangelibc.h"
 #include "rlc_internal.cuh"
 
 #include <cfloat>
+#include <cstdio>
+#include <mutex>
 
 namespace rlc {
 namespace {
@@ -207,3 +210,115 @@ cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int TY, uin
 }
 
 }  // namespace rlc
+
+// ===========================================================================
+// rlc_distance_transform_noalloc: the distance transform for callers that
+// cannot allocate device memory.
+//
+// Some callers may not call cudaMalloc at all: real-time loops (a robot's
+// localisation node) that forbid allocation after start-up, and hosts whose
+// device memory belongs to another allocator (a framework's caching
+// allocator, a fixed pool handed out by an embedding application).  This
+// entry point computes the same distance transform as
+// rlc_map_distance_transform from a caller-owned device occupancy grid into
+// a caller-owned device output, and keeps every intermediate (the packed
+// occupancy bits, the first-pass output and the per-line envelope arrays) in
+// one file-scope device array of fixed size, so it allocates nothing.
+//
+// * The array holds RLC_NOALLOC_SCRATCH_BYTES (~16.2 MiB) on every GPU that
+//   loads this library, until the process exits.
+// * Maps are limited to RLC_NOALLOC_MAX_CELLS cells with sides of at most
+//   RLC_NOALLOC_MAX_SIDE; larger maps are rejected with RLC_ERR_ARG.
+// * The first call on a device looks up the array's device address there
+//   (cudaGetSymbolAddress, with that device current) and caches it; make
+//   that first call before any stream capture.
+// * All calls share the array and it keeps the last call's contents.  No
+//   word of it needs to start at zero (each is written before it is read),
+//   but calls that overlap on the GPU -- on different streams, or from
+//   different host threads -- race on it and corrupt each other's results.
+// ===========================================================================
+namespace rlc {
+namespace {
+
+constexpr size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr size_t kNoAllocMaxCells = RLC_NOALLOC_MAX_CELLS;
+constexpr size_t kNoAllocMaxSide = RLC_NOALLOC_MAX_SIDE;
+// packed bits: ceil(W/8) * ceil(H/8) words <= cells/64 + (W + H)/8 + 1
+constexpr size_t kNoAllocBitsBytes = align_up((kNoAllocMaxCells / 64 + 2 * kNoAllocMaxSide / 8 + 1) * 8);
+constexpr size_t kNoAllocScratchBytes = kNoAllocBitsBytes + edt_scratch_bound(kNoAllocMaxCells, kNoAllocMaxSide);
+static_assert(kNoAllocScratchBytes == RLC_NOALLOC_SCRATCH_BYTES, "rangelibc.h states the scratch size");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kMaxDevices] = {};
+
+// device address of g_noalloc_scratch on the current device (looked up once per device)
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    char msg[256];
+    if (e != cudaSuccess) {
+        snprintf(msg, sizeof(msg), "rlc_distance_transform_noalloc: %s", cudaGetErrorString(e));
+        return set_last_error(RLC_ERR_CUDA, msg);
+    }
+    if (dev < 0 || dev >= kMaxDevices) return set_last_error(RLC_ERR_CUDA, "rlc_distance_transform_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            snprintf(msg, sizeof(msg), "rlc_distance_transform_noalloc: scratch address: %s",
+                     cudaGetErrorString(e));
+            return set_last_error(RLC_ERR_CUDA, msg);
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return RLC_OK;
+}
+
+bool is_device_pointer(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+}  // namespace rlc
+
+extern "C" int rlc_distance_transform_noalloc(const uint8_t* d_occ, int width, int height, float* d_dt,
+                                              void* stream) {
+    using namespace rlc;
+    char msg[256];
+    if (!d_occ || !d_dt) return set_last_error(RLC_ERR_ARG, "rlc_distance_transform_noalloc: null pointer");
+    if (width <= 0 || height <= 0) return set_last_error(RLC_ERR_ARG, "rlc_distance_transform_noalloc: sizes must be positive");
+    if ((size_t)width > kNoAllocMaxSide || (size_t)height > kNoAllocMaxSide ||
+        (size_t)width * (size_t)height > kNoAllocMaxCells) {
+        snprintf(msg, sizeof(msg),
+                 "rlc_distance_transform_noalloc: a %dx%d map exceeds the fixed scratch (at most %zu cells and "
+                 "%zu per side); use rlc_map_create + rlc_map_distance_transform",
+                 width, height, kNoAllocMaxCells, kNoAllocMaxSide);
+        return set_last_error(RLC_ERR_ARG, msg);
+    }
+    if (!is_device_pointer(d_occ) || !is_device_pointer(d_dt))
+        return set_last_error(RLC_ERR_ARG, "rlc_distance_transform_noalloc: d_occ and d_dt must be device memory");
+    void* base = nullptr;
+    if (int rc = noalloc_scratch(&base)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t* bits = static_cast<uint64_t*>(base);
+    void* edt_scratch = static_cast<char*>(base) + kNoAllocBitsBytes;
+    const int TY = (height + 7) >> 3;
+    cudaError_t e = launch_pack_bits(d_occ, width, height, bits, s);
+    if (e == cudaSuccess)
+        e = launch_edt(bits, width, height, TY, d_dt, edt_scratch, kNoAllocScratchBytes - kNoAllocBitsBytes, s);
+    if (e != cudaSuccess) {
+        snprintf(msg, sizeof(msg), "rlc_distance_transform_noalloc: %s", cudaGetErrorString(e));
+        return set_last_error(RLC_ERR_CUDA, msg);
+    }
+    return RLC_OK;
+}
