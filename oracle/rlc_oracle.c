@@ -14,8 +14,8 @@
  *  - CDDT: a query cell outside the grid counts as free; the forward
  *    binary-search read one past the end of a bin (RangeLib.h:1480-1481 when
  *    x equals the last zero point) returns 0; prune's linear search that
- *    finds nothing (RangeLib.h:1242-1247, uninitialised index) behaves like
- *    the binary branch (index = bin size).
+ *    finds nothing (RangeLib.h:1242-1247, uninitialised index) reuses the
+ *    index last assigned in the slice (see orc_cddt_prune).
  *  - sensor model: a NaN observation or range indexes bin 0.
  */
 #include "rlc_oracle.h"
@@ -447,7 +447,16 @@ float orc_cddt_calc_range(const orc_cddt* c, float x, float y, float heading, in
     return -1.0f;
 }
 
-/* prune, RangeLib.h:1176-1283 */
+/* prune, RangeLib.h:1176-1283.
+ *
+ * In the linear-search branch (bins of <= 65 entries) the reference leaves
+ * `index` unassigned when no zero point is >= x (RangeLib.h:1242-1247: the
+ * free cell lies more than max_range beyond the bin's last zero point).  The
+ * compiled reference then reuses the value `index` last received, so it
+ * marks that stale index (and the one before it) in the current bin; the
+ * golden tables reproduce exactly under that reading.  This restatement
+ * carries the last assigned index through the cells of a slice in the
+ * reference's visiting order (x outer, y inner), starting each slice at 0. */
 typedef struct { orc_cddt* c; float mr; uint8_t* used; } prune_ctx;
 
 static void prune_slices(void* p, int lo, int hi) {
@@ -457,6 +466,7 @@ static void prune_slices(void* p, int lo, int hi) {
         float angle = (float)a * c->twopi_div_td;
         float ca = cosf(angle), sa = sinf(angle);
         float tr = c->trans[a];
+        int index = 0;   /* the reference's `index`, carried across cells */
         for (int x = 0; x < c->width; ++x) {
             float fx = (float)(0.5 + x);
             for (int y = 0; y < c->height; ++y) {
@@ -473,7 +483,6 @@ static void prune_slices(void* p, int lo, int hi) {
                 if (high == -1) continue;
                 if (c->occ[(size_t)x * c->height + y]) continue;
                 if (bin[high] < lx && lx - bin[high] < ctx->mr) { ctx->used[base + high] = 1; continue; }
-                int index = n;
                 if (high > ORC_BSEARCH_THRESHOLD) {
                     int l = 0, h = n;                            /* lower_bound */
                     while (l < h) { int mid = (l + h) >> 1; if (bin[mid] < lx) l = mid + 1; else h = mid; }
@@ -481,8 +490,8 @@ static void prune_slices(void* p, int lo, int hi) {
                 } else {
                     for (int i = 0; i < n; ++i) if (bin[i] >= lx) { index = i; break; }
                 }
-                if (index < n) ctx->used[base + index] = 1;
-                if (index - 1 >= 0) ctx->used[base + index - 1] = 1;
+                if (index >= 0 && index < n) ctx->used[base + index] = 1;
+                if (index - 1 >= 0 && index - 1 < n) ctx->used[base + index - 1] = 1;
             }
         }
     }

@@ -33,81 +33,105 @@ constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t& total) {
+struct OpSum {
+    typedef uint32_t T;
+    static __device__ __forceinline__ T id() { return 0u; }
+    static __device__ __forceinline__ T op(T a, T b) { return a + b; }
+};
+struct OpMax {
+    typedef int T;
+    static __device__ __forceinline__ T id() { return -2147483647 - 1; }
+    static __device__ __forceinline__ T op(T a, T b) { return a > b ? a : b; }
+};
+
+// block-wide scan of one value per thread: returns the exclusive prefix,
+// `total` gets the reduction over the block
+template <class Op>
+__device__ __forceinline__ typename Op::T block_scan(typename Op::T v, typename Op::T* warp_vals,
+                                                     typename Op::T& total) {
+    typedef typename Op::T T;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t x = v;
+    T x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+        T y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = Op::op(y, x);
     }
-    if (lane == 31) warp_sums[wid] = x;
+    T excl_in_warp = __shfl_up_sync(0xffffffffu, x, 1);
+    if (lane == 0) excl_in_warp = Op::id();
+    if (lane == 31) warp_vals[wid] = x;
     __syncthreads();
     if (wid == 0) {
         const int nw = blockDim.x >> 5;
-        uint32_t w = lane < nw ? warp_sums[lane] : 0;
+        T w = lane < nw ? warp_vals[lane] : Op::id();
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
+            T y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w = Op::op(y, w);
         }
-        if (lane < nw) warp_sums[lane] = w;
+        if (lane < nw) warp_vals[lane] = w;
     }
     __syncthreads();
-    total = warp_sums[(blockDim.x >> 5) - 1];
-    uint32_t excl = x - v + (wid > 0 ? warp_sums[wid - 1] : 0);
+    total = warp_vals[(blockDim.x >> 5) - 1];
+    T excl = wid > 0 ? Op::op(warp_vals[wid - 1], excl_in_warp) : excl_in_warp;
     __syncthreads();
     return excl;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_tile_sums(const uint32_t* __restrict__ in, size_t n,
-                                                            uint32_t* __restrict__ sums) {
-    __shared__ uint32_t ws[32];
+template <class Op>
+__global__ void __launch_bounds__(kScanThreads) k_tile_reduce(const typename Op::T* __restrict__ in, size_t n,
+                                                              typename Op::T* __restrict__ sums) {
+    __shared__ typename Op::T ws[32];
     size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
-    uint32_t s = 0;
+    typename Op::T s = Op::id();
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i)
-        if (base + i < n) s += in[base + i];
-    uint32_t total;
-    block_exclusive_scan(s, ws, total);
+        if (base + i < n) s = Op::op(s, in[base + i]);
+    typename Op::T total;
+    block_scan<Op>(s, ws, total);
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-// single block: exclusive scan of the tile sums in place; sums[ntiles] = total
-__global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t* sums, size_t ntiles) {
-    __shared__ uint32_t ws[32];
-    uint32_t carry = 0;
+// single block: exclusive scan of the tile reductions in place; sums[ntiles] = total
+template <class Op>
+__global__ void __launch_bounds__(kScanThreads) k_scan_partials(typename Op::T* sums, size_t ntiles) {
+    __shared__ typename Op::T ws[32];
+    typename Op::T carry = Op::id();
     for (size_t base = 0; base < ntiles; base += kScanThreads) {
         size_t i = base + threadIdx.x;
-        uint32_t v = i < ntiles ? sums[i] : 0;
-        uint32_t total;
-        uint32_t e = block_exclusive_scan(v, ws, total);
-        if (i < ntiles) sums[i] = carry + e;
-        carry += total;
+        typename Op::T v = i < ntiles ? sums[i] : Op::id();
+        typename Op::T total;
+        typename Op::T e = block_scan<Op>(v, ws, total);
+        if (i < ntiles) sums[i] = Op::op(carry, e);
+        carry = Op::op(carry, total);
     }
     if (threadIdx.x == 0) sums[ntiles] = carry;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ in, size_t n,
-                                                             const uint32_t* __restrict__ sums,
-                                                             uint32_t* __restrict__ out, size_t ntiles) {
-    __shared__ uint32_t ws[32];
+// INCLUSIVE = false: out[i] = op(in[0..i-1]) and out[n] = total; true: out[i] = op(in[0..i])
+template <class Op, bool INCLUSIVE>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const typename Op::T* __restrict__ in, size_t n,
+                                                             const typename Op::T* __restrict__ sums,
+                                                             typename Op::T* __restrict__ out, size_t ntiles) {
+    typedef typename Op::T T;
+    __shared__ T ws[32];
     size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t s = 0;
+    T v[kScanItems];
+    T s = Op::id();
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        v[i] = base + i < n ? in[base + i] : 0;
-        s += v[i];
+        v[i] = base + i < n ? in[base + i] : Op::id();
+        s = Op::op(s, v[i]);
     }
-    uint32_t total;
-    uint32_t run = block_exclusive_scan(s, ws, total) + sums[blockIdx.x];
+    T total;
+    T run = Op::op(sums[blockIdx.x], block_scan<Op>(s, ws, total));
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
+        if (INCLUSIVE) run = Op::op(run, v[i]);
         if (base + i < n) out[base + i] = run;
-        run += v[i];
+        if (!INCLUSIVE) run = Op::op(run, v[i]);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = sums[ntiles];
+    if (!INCLUSIVE && blockIdx.x == 0 && threadIdx.x == 0) out[n] = sums[ntiles];
 }
 
 // ------------------------------------------------------------ construction
@@ -233,45 +257,83 @@ __global__ void k_copy_bins(const uint32_t* __restrict__ src_start, const float*
 }
 
 // ------------------------------------------------------------------ prune
-__global__ void k_prune_mark(SliceGeom g, const uint64_t* __restrict__ bits, int W, int H, int TY,
-                             const uint32_t* __restrict__ bin_start, const float* __restrict__ zeros, float mr,
-                             uint32_t* __restrict__ used) {
-    const int a = blockIdx.y;
-    const float ca = __ldg(g.cosv + a), sa = __ldg(g.sinv + a), tr = __ldg(g.trans + a);
-    const int width = __ldg(g.widths + a);
-    const uint32_t sb = __ldg(g.slice_base + a);
+// One slice per launch, one thread per cell in the reference's visiting
+// order (cell = x * H + y).  A cell either skips, marks directly, or -- in
+// the linear-search branch when no zero point is >= x -- reuses the index
+// the last assigning cell of the slice produced (the reference leaves its
+// `index` unassigned there, RangeLib.h:1242-1247, and keeps the stale value).
+// tag[c] = c for cells that assign an index (val[c] = that index), -1 for
+// cells that do not, and -2 for cells that need the stale index.
+__global__ void k_prune_classify(SliceGeom g, int a, const uint64_t* __restrict__ bits, int W, int H, int TY,
+                                 const uint32_t* __restrict__ bin_start, const float* __restrict__ zeros, float mr,
+                                 uint32_t* __restrict__ used, int* __restrict__ tag, int* __restrict__ val,
+                                 unsigned* __restrict__ n_need) {
     const long long ncell = (long long)W * H;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
-         c += (long long)gridDim.x * blockDim.x) {
-        int x = (int)(c / H), y = (int)(c - (long long)x * H);
-        const float fx = __int2float_rn(x) + 0.5f, fy = __int2float_rn(y) + 0.5f;
-        const float lx = __fsub_rn(__fmul_rn(fx, ca), __fmul_rn(fy, sa));
-        const float ly = __fadd_rn(__fadd_rn(__fmul_rn(fx, sa), __fmul_rn(fy, ca)), tr);
-        const unsigned li = (unsigned)__float2int_rz(ly);
-        if (li >= (unsigned)width) continue;
-        const uint32_t b = sb + li;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const float ca = __ldg(g.cosv + a), sa = __ldg(g.sinv + a), tr = __ldg(g.trans + a);
+    int x = (int)(c / H), y = (int)(c - (long long)x * H);
+    int t = -1;
+    const float fx = __int2float_rn(x) + 0.5f, fy = __int2float_rn(y) + 0.5f;
+    const float lx = __fsub_rn(__fmul_rn(fx, ca), __fmul_rn(fy, sa));
+    const float ly = __fadd_rn(__fadd_rn(__fmul_rn(fx, sa), __fmul_rn(fy, ca)), tr);
+    const unsigned li = (unsigned)__float2int_rz(ly);
+    if (li < (unsigned)__ldg(g.widths + a)) {
+        const uint32_t b = __ldg(g.slice_base + a) + li;
         const uint32_t base = __ldg(bin_start + b);
         const int n = (int)(__ldg(bin_start + b + 1) - base);
         const int high = n - 1;
-        if (high == -1) continue;
-        if (occ_bit(bits, TY, x, y)) continue;
-        const float last = __ldg(zeros + base + high);
-        if (last < lx && __fsub_rn(lx, last) < mr) { used[base + high] = 1; continue; }
-        int index = n;
-        if (high > kBinarySearchThreshold) {
-            int l = 0, h = n;   // lower_bound
-            while (l < h) {
-                int mid = (l + h) >> 1;
-                if (__ldg(zeros + base + mid) < lx) l = mid + 1; else h = mid;
+        if (high >= 0 && !occ_bit(bits, TY, x, y)) {
+            const float last = __ldg(zeros + base + high);
+            if (last < lx && __fsub_rn(lx, last) < mr) {
+                used[base + high] = 1;
+            } else {
+                int index = -1;
+                if (high > kBinarySearchThreshold) {
+                    int l = 0, h = n;   // lower_bound
+                    while (l < h) {
+                        int mid = (l + h) >> 1;
+                        if (__ldg(zeros + base + mid) < lx) l = mid + 1; else h = mid;
+                    }
+                    index = l;
+                } else {
+                    for (int i = 0; i < n; ++i)
+                        if (__ldg(zeros + base + i) >= lx) { index = i; break; }
+                }
+                if (index >= 0) {
+                    if (index < n) used[base + index] = 1;
+                    if (index >= 1) used[base + index - 1] = 1;
+                    t = (int)c;
+                    val[c] = index;
+                } else {
+                    t = -2;
+                    atomicAdd(n_need, 1u);
+                }
             }
-            index = l;
-        } else {
-            for (int i = 0; i < n; ++i)
-                if (__ldg(zeros + base + i) >= lx) { index = i; break; }
         }
-        if (index < n) used[base + index] = 1;
-        if (index >= 1) used[base + index - 1] = 1;
     }
+    tag[c] = t;
+}
+
+// cells that need the stale index: last[c] is the last assigning cell <= c
+__global__ void k_prune_stale(SliceGeom g, int a, int W, int H, const uint32_t* __restrict__ bin_start,
+                              const int* __restrict__ tag, const int* __restrict__ last, const int* __restrict__ val,
+                              uint32_t* __restrict__ used) {
+    const long long ncell = (long long)W * H;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell || tag[c] != -2) return;
+    const int p = last[c];
+    const int index = p >= 0 ? val[p] : 0;   // the reference's index starts each slice at 0 here
+    int x = (int)(c / H), y = (int)(c - (long long)x * H);
+    const float ca = __ldg(g.cosv + a), sa = __ldg(g.sinv + a), tr = __ldg(g.trans + a);
+    const float fx = __int2float_rn(x) + 0.5f, fy = __int2float_rn(y) + 0.5f;
+    const float ly = __fadd_rn(__fadd_rn(__fmul_rn(fx, sa), __fmul_rn(fy, ca)), tr);
+    const unsigned li = (unsigned)__float2int_rz(ly);
+    const uint32_t b = __ldg(g.slice_base + a) + li;
+    const uint32_t base = __ldg(bin_start + b);
+    const int n = (int)(__ldg(bin_start + b + 1) - base);
+    if (index >= 0 && index < n) used[base + index] = 1;
+    if (index - 1 >= 0 && index - 1 < n) used[base + index - 1] = 1;
 }
 
 // entries of slices >= nslices are kept (they are empty after construction)
@@ -303,18 +365,24 @@ struct DevBuf {
 
 }  // namespace
 
-cudaError_t scan_exclusive_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, cudaStream_t s) {
+template <class Op, bool INCLUSIVE>
+static cudaError_t scan_impl(const typename Op::T* d_in, typename Op::T* d_out, size_t n, cudaStream_t s) {
     size_t ntiles = (n + kScanTile - 1) / kScanTile;
     if (ntiles == 0) ntiles = 1;
     DevBuf sums;
-    RLC_TRY(sums.alloc((ntiles + 1) * sizeof(uint32_t)));
-    k_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(d_in, n, sums.as<uint32_t>());
+    RLC_TRY(sums.alloc((ntiles + 1) * sizeof(typename Op::T)));
+    k_tile_reduce<Op><<<(unsigned)ntiles, kScanThreads, 0, s>>>(d_in, n, sums.as<typename Op::T>());
     RLC_TRY(cudaGetLastError());
-    k_scan_sums<<<1, kScanThreads, 0, s>>>(sums.as<uint32_t>(), ntiles);
+    k_scan_partials<Op><<<1, kScanThreads, 0, s>>>(sums.as<typename Op::T>(), ntiles);
     RLC_TRY(cudaGetLastError());
-    k_scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(d_in, n, sums.as<uint32_t>(), d_out, ntiles);
+    k_scan_tiles<Op, INCLUSIVE><<<(unsigned)ntiles, kScanThreads, 0, s>>>(d_in, n, sums.as<typename Op::T>(), d_out,
+                                                                         ntiles);
     RLC_TRY(cudaGetLastError());
     return cudaStreamSynchronize(s);   // the temporary is released on return
+}
+
+cudaError_t scan_exclusive_u32(const uint32_t* d_in, uint32_t* d_out, size_t n, cudaStream_t s) {
+    return scan_impl<OpSum, false>(d_in, d_out, n, s);
 }
 
 cudaError_t cddt_build(const uint64_t* d_bits, int W, int H, int TY, unsigned td, const int* d_widths,
@@ -453,12 +521,26 @@ cudaError_t cddt_prune(const uint64_t* d_bits, int W, int H, int TY, unsigned td
     RLC_TRY(cudaMemsetAsync(used.p, 0, ((size_t)nz + 1) * sizeof(uint32_t), s));
     const long long ncell = (long long)W * H;
     if (ncell > 0 && nz > 0) {
-        unsigned gx = blocks_for(ncell, 256);
-        if (gx > 4096) gx = 4096;
-        dim3 grid(gx, nslices);
-        k_prune_mark<<<grid, 256, 0, s>>>(g, d_bits, W, H, TY, tab->bin_start, tab->zeros, max_range,
-                                          used.as<uint32_t>());
-        RLC_TRY(cudaGetLastError());
+        DevBuf tag, val, last, need;
+        RLC_TRY(tag.alloc((size_t)ncell * sizeof(int)));
+        RLC_TRY(val.alloc((size_t)ncell * sizeof(int)));
+        RLC_TRY(last.alloc((size_t)ncell * sizeof(int)));
+        RLC_TRY(need.alloc(sizeof(unsigned)));
+        for (int a = 0; a < nslices; ++a) {
+            RLC_TRY(cudaMemsetAsync(need.p, 0, sizeof(unsigned), s));
+            k_prune_classify<<<blocks_for(ncell, 256), 256, 0, s>>>(g, a, d_bits, W, H, TY, tab->bin_start,
+                                                                    tab->zeros, max_range, used.as<uint32_t>(),
+                                                                    tag.as<int>(), val.as<int>(), need.as<unsigned>());
+            RLC_TRY(cudaGetLastError());
+            unsigned n_need = 0;
+            RLC_TRY(cudaMemcpyAsync(&n_need, need.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+            RLC_TRY(cudaStreamSynchronize(s));
+            if (n_need == 0) continue;
+            RLC_TRY((scan_impl<OpMax, true>(tag.as<int>(), last.as<int>(), (size_t)ncell, s)));
+            k_prune_stale<<<blocks_for(ncell, 256), 256, 0, s>>>(g, a, W, H, tab->bin_start, tag.as<int>(),
+                                                                 last.as<int>(), val.as<int>(), used.as<uint32_t>());
+            RLC_TRY(cudaGetLastError());
+        }
     }
     // slices >= nslices keep all their entries
     uint32_t first_unpruned = 0;

@@ -187,6 +187,21 @@ def _write_png_gray(path: str, gray: np.ndarray) -> None:
                 + chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
 
 
+def png_occupancy(path: str, threshold: float = 128.0) -> np.ndarray:
+    """grid[x][y] of OMap(path, threshold) (RangeLib.h:159-201) as uint8 (width, height).
+
+    The reference reads r = image[idx+2], g = image[idx+1], b = image[idx]
+    from lodepng's RGBA buffer and marks (int)rgb2gray(r, g, b) < threshold
+    occupied, rgb2gray = 0.229 r + 0.587 g + 0.114 b in double (RangeUtils.h:30-32).
+    """
+    rgba = _read_png_rgba(path)
+    r = rgba[..., 2].astype(np.float64)
+    g = rgba[..., 1].astype(np.float64)
+    b = rgba[..., 0].astype(np.float64)
+    gray = (0.229 * r + 0.587 * g + 0.114 * b).astype(np.float32).astype(np.int32)
+    return np.ascontiguousarray((gray < np.float32(threshold)).T, dtype=np.uint8)
+
+
 def _quaternion_yaw(q) -> float:
     x, y, z, w = q.x, q.y, q.z, q.w
     return float(np.arctan2(2.0 * (w * z + x * y), 1.0 - 2.0 * (y * y + z * z)))
@@ -239,18 +254,11 @@ class PyOMap:
 
     def _from_png(self, path: str, threshold: float) -> np.ndarray:
         try:
-            rgba = _read_png_rgba(path)
+            return png_occupancy(path, threshold)
         except (IOError, OSError, KeyError, zlib.error, struct.error) as e:
             print(f"ERROR: {e}")
             self._error = True
             return np.zeros((0, 0), np.uint8)
-        # RangeLib.h:188-197: r = image[idx+2], g = image[idx+1], b = image[idx+0]
-        r = rgba[..., 2].astype(np.float32)
-        g = rgba[..., 1].astype(np.float32)
-        b = rgba[..., 0].astype(np.float32)
-        gray = (0.229 * r.astype(np.float64) + 0.587 * g.astype(np.float64) + 0.114 * b.astype(np.float64))
-        gray = gray.astype(np.float32).astype(np.int32)
-        return np.ascontiguousarray((gray < threshold).T, dtype=np.uint8)   # grid[x][y], x = column
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -1,0 +1,70 @@
+"""The C-ABI library builds, loads and exports everything include/rangelibc.h declares.
+
+No compute calls: only the checks the library makes on the host before it
+touches a device (argument validation) run here.
+"""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "rangelibc.h")
+
+
+def _declared():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"RLC_API\s+[\w\s\*]+?\b(rlc_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    from range_libc_gb300 import _lib
+    return _lib.lib()
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    for must in ("rlc_map_create", "rlc_method_create", "rlc_calc_range_many", "rlc_calc_range_repeat_angles",
+                 "rlc_set_sensor_model", "rlc_eval_sensor_model",
+                 "rlc_calc_range_repeat_angles_eval_sensor_model", "rlc_cddt_prune", "rlc_batch_run",
+                 "rlc_distance_transform_noalloc"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(L):
+    from range_libc_gb300 import _lib
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.library_path()], capture_output=True, text=True)
+    exported = set(re.findall(r"\bT (rlc_\w+)", out.stdout))
+    missing = [n for n in _declared() if n not in exported]
+    assert not missing, missing
+    # and the ctypes table binds every one of them
+    assert set(_declared()) <= set(_lib.SIGNATURES)
+
+
+def test_abi_version(L):
+    assert L.rlc_abi_version() == 1
+
+
+def test_host_side_argument_checks(L):
+    from range_libc_gb300 import _lib
+    out = C.c_void_p()
+    assert L.rlc_map_create(None, 4, 4, C.byref(out)) == _lib.RLC_ERR_ARG
+    assert b"null occupancy" in L.rlc_last_error()
+    occ = (C.c_uint8 * 4)()
+    assert L.rlc_map_create(occ, 0, 4, C.byref(out)) == _lib.RLC_ERR_ARG
+    assert L.rlc_method_create(None, 1, 10.0, 0, C.byref(out)) == _lib.RLC_ERR_ARG
+    assert L.rlc_calc_range_many(None, None, None, 3, 0, None) == _lib.RLC_ERR_ARG
+    assert L.rlc_batch_create(None, 0, 0, C.byref(out)) == _lib.RLC_ERR_ARG
+    assert L.rlc_distance_transform_noalloc(None, 8, 8, None, None) == _lib.RLC_ERR_ARG
+    assert L.rlc_map_destroy(None) == _lib.RLC_OK
+
+
+def test_python_module_fails_loudly_without_a_device(L):
+    import range_libc_gb300.range_libc as rl
+    if rl.device_count() > 0:
+        pytest.skip("a device is visible")
+    with pytest.raises(rl._lib.RangeLibError):
+        rl.PyOMap(4, 4)

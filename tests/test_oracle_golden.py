@@ -1,0 +1,112 @@
+"""The CPU oracle against the golden vectors the reference produced (tests/golden/).
+
+BL and RM use the recorded per-ray cosf/sinf, so these checks hold on any
+IEEE host.  CDDT tables depend on the host's cosf of the slice angles; they
+are compared when this host's libm reproduces the recorded slice trig.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "reference_vectors.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return dict(np.load(GOLDEN))
+
+
+def _names(gold):
+    return sorted({k.split("/")[0] for k in gold if k.endswith("/occ") and k.count("/") == 1 and k != "pf/occ"})
+
+
+def _bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32 if a.dtype == np.float32 else np.uint64)
+
+
+def _host_slice_trig(td):
+    libm = ctypes.CDLL("libm.so.6")
+    libm.cosf.restype = libm.sinf.restype = ctypes.c_float
+    libm.cosf.argtypes = libm.sinf.argtypes = [ctypes.c_float]
+    step = np.float32(6.28318530718 / float(np.float32(td)))
+    ang = np.arange(td).astype(np.float32) * step
+    return np.array([[libm.cosf(float(a)), libm.sinf(float(a))] for a in ang.astype(np.float32)], np.float32)
+
+
+def test_golden_has_cases(gold):
+    assert {"single_pixel", "quad", "small", "rect_96", "corridor_160x120"} <= set(_names(gold))
+
+
+def test_distance_transform_and_edges(gold, oracle_mod):
+    for name in _names(gold):
+        occ = gold[f"{name}/occ"]
+        assert np.array_equal(_bits(oracle_mod.edt(occ)), _bits(gold[f"{name}/dt"])), name
+        assert np.array_equal(oracle_mod.edge_map(occ), gold[f"{name}/edge"]), name
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm"])
+def test_bl_rm_world_frame(gold, oracle_mod, kind):
+    for name in _names(gold):
+        occ = gold[f"{name}/occ"]
+        for wname in ("identity", "ros", "rotated"):
+            key = f"{name}/{wname}"
+            world = tuple(float(v) for v in gold[f"{key}/world"])
+            q = gold[f"{key}/ins_any"]
+            trig = gold[f"{key}/trig_any"]
+            m = oracle_mod.OracleMethod(occ, kind, 60.0, world=world)
+            xyh, _ = oracle_mod.world_rays(world, q)
+            out = np.array([m.calc_range_trig(float(a), float(b), float(c), float(d))
+                            for (a, b, _), (c, d) in zip(xyh, trig)], np.float32) * np.float32(world[0])
+            assert np.array_equal(_bits(out.astype(np.float32)), _bits(gold[f"{key}/{kind}/many"])), (name, wname)
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm"])
+def test_bl_rm_grid_frame(gold, oracle_mod, kind):
+    for name in _names(gold):
+        m = oracle_mod.OracleMethod(gold[f"{name}/occ"], kind, 60.0)
+        q, trig = gold[f"{name}/raw/ins"], gold[f"{name}/raw/trig"]
+        out = np.array([m.calc_range_trig(float(a), float(b), float(c), float(d))
+                        for (a, b, _), (c, d) in zip(q, trig)], np.float32)
+        assert np.array_equal(_bits(out), _bits(gold[f"{name}/raw/{kind}"])), name
+
+
+@pytest.mark.parametrize("kind", ["cddt", "pcddt"])
+def test_cddt_tables_and_queries(gold, oracle_mod, kind):
+    if not np.array_equal(_host_slice_trig(108), gold["rect_96/slice_trig_108"]):
+        pytest.skip("this host's cosf/sinf of the slice angles differ from the recorded ones")
+    for name in _names(gold):
+        occ = gold[f"{name}/occ"]
+        m = oracle_mod.OracleMethod(occ, kind, 60.0, td=108)
+        w, t, bl, z = m.cddt_table()
+        assert np.array_equal(w, gold[f"{name}/{kind}_table/widths"]), name
+        assert np.array_equal(_bits(t), _bits(gold[f"{name}/{kind}_table/trans"])), name
+        assert np.array_equal(bl, gold[f"{name}/{kind}_table/bin_len"]), name
+        assert np.array_equal(_bits(z), _bits(gold[f"{name}/{kind}_table/zeros"])), name
+        assert np.array_equal(_bits(m.calc_range_many_raw(gold[f"{name}/raw/ins_in"])),
+                              _bits(gold[f"{name}/raw/{kind}"])), name
+        for wname in ("identity", "ros"):
+            key = f"{name}/{wname}"
+            world = tuple(float(v) for v in gold[f"{key}/world"])
+            mw = oracle_mod.OracleMethod(occ, kind, 60.0, td=108, world=world)
+            assert np.array_equal(_bits(mw.calc_range_many(gold[f"{key}/ins_in"])),
+                                  _bits(gold[f"{key}/{kind}/many"])), (name, wname)
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm", "cddt", "pcddt"])
+def test_particle_filter_step(gold, oracle_mod, kind):
+    if kind in ("cddt", "pcddt") and not np.array_equal(_host_slice_trig(108), gold["pf/slice_trig_108"]):
+        pytest.skip("this host's cosf/sinf of the slice angles differ from the recorded ones")
+    world = tuple(float(v) for v in gold["pf/world"])
+    m = oracle_mod.OracleMethod(gold["pf/occ"], kind, 100.0, td=108, world=world)
+    m.set_sensor_model(gold["pf/table"])
+    ins, ang, obs = gold["pf/ins"], gold["pf/angles"], gold["pf/obs"]
+    n, na = len(ins), len(ang)
+    r = m.calc_range_repeat_angles(ins, ang)
+    assert np.array_equal(_bits(r), _bits(gold[f"pf/{kind}/ranges"]))
+    assert np.array_equal(_bits(m.eval_sensor_model(obs, r, na, n)), _bits(gold[f"pf/{kind}/eval"]))
+    assert np.array_equal(_bits(m.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs)),
+                          _bits(gold[f"pf/{kind}/fused"]))

@@ -1,0 +1,102 @@
+"""The CPU oracle against the reference itself, compiled from its sources (oracle/_ref).
+
+Runs only where the reference sources are present (the harness cannot be
+built elsewhere).  Larger and more varied than the golden vectors: several
+maps and world frames, every method, sensor tables up to K = 201 and beams
+up to 1,081 (weights reach subnormals and zero).
+"""
+import numpy as np
+import pytest
+
+from range_libc_gb300 import workloads as W
+
+
+@pytest.fixture(scope="module")
+def O():
+    import oracle
+    if not oracle.ref_available():
+        try:
+            oracle.build(reference=True)
+        except Exception as e:  # noqa: BLE001
+            pytest.skip(f"reference harness unavailable: {e}")
+    if not oracle.ref_available():
+        pytest.skip("reference sources not present")
+    return oracle
+
+
+def _bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32 if a.dtype == np.float32 else np.uint64)
+
+
+MAPS = {
+    "rect_512": lambda: W.rect_disk_map(512, 1000),
+    "corridor_384x256": lambda: np.ascontiguousarray(W.corridor_map(512, 2000)[:384, :256]),
+    "rect_2048": lambda: W.rect_disk_map(2048, 3000),
+}
+
+
+@pytest.mark.parametrize("name", list(MAPS))
+def test_distance_transform(O, name):
+    occ = MAPS[name]()
+    assert np.array_equal(_bits(O.edt(occ)), _bits(O.RefMap(occ).dt()))
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm", "cddt", "pcddt"])
+@pytest.mark.parametrize("world", [(1.0, 0.0, 0.0, 0.0), (0.05, 0.0, -12.5, -7.5), (0.07, 1.1, 3.0, 2.0)])
+def test_queries(O, kind, world):
+    occ = MAPS["rect_512"]()
+    w = O.world_tuple(*world)
+    q = W.free_cell_queries(occ, 20000, 5)
+    q[:, 0], q[:, 1] = W.grid_to_world(q[:, 0].astype(np.float64), q[:, 1].astype(np.float64), w)
+    if kind in ("cddt", "pcddt") and world[1] != 0.0:
+        pytest.skip("rotated worlds land CDDT queries off the map (undefined in the reference)")
+    ref = O.RefMethod(O.RefMap(occ, world=w), kind, 300.0, 108)
+    orc = O.OracleMethod(occ, kind, 300.0, td=108, world=w)
+    assert np.array_equal(_bits(orc.calc_range_many(q)), _bits(ref.calc_range_many(q)))
+    if kind in ("bl", "rm"):
+        rng = np.random.default_rng(8)
+        qa = np.stack([rng.uniform(-20, 530, 5000) * world[0], rng.uniform(-20, 530, 5000) * world[0],
+                       rng.uniform(-20, 20, 5000)], 1).astype(np.float32)
+        assert np.array_equal(_bits(orc.calc_range_many(qa)), _bits(ref.calc_range_many(qa)))
+
+
+@pytest.mark.parametrize("td", [108, 216, 37])
+def test_cddt_tables(O, td):
+    occ = MAPS["corridor_384x256"]()
+    for kind in ("cddt", "pcddt"):
+        ref = O.RefMethod(O.RefMap(occ), kind, 200.0, td)
+        orc = O.OracleMethod(occ, kind, 200.0, td=td)
+        for a, b in zip(orc.cddt_table(), ref.cddt_table()):
+            assert np.array_equal(_bits(a) if a.dtype == np.float32 else a, _bits(b) if b.dtype == np.float32 else b)
+
+
+@pytest.mark.parametrize("kind", ["rm", "bl", "cddt"])
+@pytest.mark.parametrize("beams", [61, 1081])
+def test_sensor_model_paths(O, kind, beams):
+    wl = W.particle_filter_step(side=512, n_particles=300, n_beams=beams, max_range_px=200.0, seed=44)
+    w = tuple(float(np.float32(v)) for v in wl.world)
+    ref = O.RefMethod(O.RefMap(wl.occ, world=w), kind, 200.0, 108)
+    orc = O.OracleMethod(wl.occ, kind, 200.0, td=108, world=w)
+    ref.set_sensor_model(wl.table)
+    orc.set_sensor_model(wl.table)
+    obs = np.resize(wl.obs, beams).astype(np.float32)
+    n, na = len(wl.ins), len(wl.angles)
+    r_ref = ref.calc_range_repeat_angles(wl.ins, wl.angles)
+    assert np.array_equal(_bits(orc.calc_range_repeat_angles(wl.ins, wl.angles)), _bits(r_ref))
+    assert np.array_equal(_bits(orc.eval_sensor_model(obs, r_ref, na, n)),
+                          _bits(ref.eval_sensor_model(obs, r_ref, na, n)))
+    wf = ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, obs)
+    assert np.array_equal(_bits(orc.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, obs)), _bits(wf))
+    if beams == 1081:
+        assert np.any(wf == 0.0) or np.any(wf < 2.3e-308)   # underflow is exercised
+
+
+def test_multithreaded_oracle_equals_single(O):
+    wl = W.particle_filter_step(side=512, n_particles=500, n_beams=61, max_range_px=200.0, seed=45)
+    w = tuple(float(np.float32(v)) for v in wl.world)
+    orc = O.OracleMethod(wl.occ, "rm", 200.0, world=w)
+    orc.set_sensor_model(wl.table)
+    a = orc.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=1)
+    b = orc.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=7)
+    assert np.array_equal(a, b)
