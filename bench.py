@@ -200,7 +200,11 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="fused", choices=["fused", "plain"])
+    ap.add_argument("--workload", default="fused", choices=["fused", "plain", "batch", "cddt"])
+    ap.add_argument("--td", type=int, default=108, help="cddt workload: theta discretization")
+    ap.add_argument("--prune", action="store_true", help="cddt workload: pruned table (PCDDT)")
+    ap.add_argument("--filters", type=int, default=32, help="batch workload: number of filters")
+    ap.add_argument("--no-plain", action="store_true", help="batch workload: skip the per-call comparisons")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
     args = ap.parse_args()
@@ -208,6 +212,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "cddt":
+        return run_cddt(args)
 
     import torch
     import range_libc_gb300.range_libc as rl
@@ -238,8 +246,7 @@ def main():
 
     # autotune the schedule on this workload, then warm up
     if args.workload == "fused":
-        rl._lib.call("rlc_method_autotune", method.handle, ins.data_ptr(), angles.data_ptr(), obs.data_ptr(),
-                     weights.data_ptr(), n, na, rl._stream_of(ins))
+        method.autotune(ins, angles, obs, weights)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -333,7 +340,7 @@ def main():
                                    f"201x201 f64 sensor table",
                        "particles": n, "beams": na, "map": "2048x2048 corridor, seed 2000",
                        "l2": "flushed before every step (256 MiB write)",
-                       "schedule": dict(zip(("dt_layout", "block"), method.schedule()))},
+                       "schedule": dict(zip(("dt_layout", "block", "prefetch", "tile"), method.schedule()))},
             "particle_updates_per_s": value / na,
             "e2e": {"value": e2e, "unit": "rays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "particle_updates_per_s": e2e / na},
@@ -349,6 +356,196 @@ def main():
                 f.write(s + "\n")
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+def _event_steps(torch, stream, steps, flush, step_fn):
+    """CUDA-event time of each step (ms), L2 flushed before every step; returns (times, launches)."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    launches = 0
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.fill_(float(k))
+        starts[k].record(stream)
+        launches += step_fn()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in zip(starts, ends)], launches
+
+
+def run_batch(args):
+    """32 uneven particle filters (maps 512-4096 px, 500-20,000 particles, 30-1,081 beams,
+    max_range 100-400 px) updated by one persistent launch replayed as a CUDA graph, against
+    per-filter plain calls (cast to ranges, then the sensor model, host buffers -- the
+    reference's per-call pattern) and per-filter fused device calls."""
+    import torch
+    import range_libc_gb300.range_libc as rl
+    from range_libc_gb300 import workloads as W
+
+    rank, ws, dist = dist_init()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    specs = W.uneven_batch_specs()[: args.filters]
+    filters, host, keep = [], [], []
+    t0 = time.perf_counter()
+    for spec in specs:
+        wl = W.batch_filter(spec)
+        omap = rl.PyOMap(np.ascontiguousarray(wl.occ.T))
+        m = rl.PyRayMarching(omap, wl.max_range)
+        m.set_sensor_model(wl.table)
+        t = [torch.from_numpy(a).to(dev) for a in (wl.ins, wl.angles, wl.obs)]
+        w = torch.zeros(len(wl.ins), dtype=torch.float64, device=dev)
+        filters.append((m, t[0], t[1], t[2], w))
+        host.append(wl)
+        keep.append(omap)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    rays = sum(len(wl.ins) * len(wl.angles) for wl in host)
+    particles = sum(len(wl.ins) for wl in host)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # per-filter schedules: autotune each filter's fused kernel on its own workload
+    for m, ins, ang, obs, w in filters:
+        m.autotune(ins, ang, obs, w)
+    batch = rl.PyFilterBatch(filters)
+
+    def batched():
+        batch.run()
+        return 1
+
+    def per_filter_fused():
+        for m, ins, ang, obs, w in filters:
+            m.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs, w)
+        return len(filters)
+
+    for _ in range(args.warmup):
+        batched()
+    barrier(dist)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    tb, launches = _event_steps(torch, stream, args.steps, flush, batched)
+    clk = clocks.stop()
+    ref_w = [f[4].cpu().numpy().copy() for f in filters]
+    if args.no_plain:
+        total_b = max_over_ranks(dist, sum(tb))
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": ws * rays * args.steps / (total_b / 1e3), "unit": "rays/s",
+                              "ms_per_step": total_b / args.steps, "filters": len(filters), "rays_per_step": rays,
+                              "gpu_launches": launches}))
+        return 0
+    for _ in range(args.warmup):
+        per_filter_fused()
+    tf, _ = _event_steps(torch, stream, args.steps, flush, per_filter_fused)
+    same = all(np.array_equal(f[4].cpu().numpy(), r) for f, r in zip(filters, ref_w))
+
+    # plain per-filter calls through host buffers: cast to ranges, then the sensor model
+    hbuf = [(wl.ins, wl.angles, wl.obs, np.empty(len(wl.ins) * len(wl.angles), np.float32),
+             np.empty(len(wl.ins), np.float64)) for wl in host]
+
+    def plain_host():
+        for (m, *_), (hi, ha, ho, hr, hw) in zip(filters, hbuf):
+            m.calc_range_repeat_angles(hi, ha, hr)
+            m.eval_sensor_model(ho, hr, hw, len(ha), len(hi))
+
+    plain_host()
+    plain_steps = max(2, min(args.steps, 5))
+    tp = 0.0
+    for k in range(plain_steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        plain_host()
+        tp += time.perf_counter() - a
+    same_plain = all(np.array_equal(h[4], r) for h, r in zip(hbuf, ref_w))
+
+    total_b = max_over_ranks(dist, sum(tb))
+    value = ws * rays * args.steps / (total_b / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_b / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
+        "config": {"workload": "32 uneven filters (maps 512-4096 px, RM), one persistent launch as a CUDA graph",
+                   "filters": len(filters), "rays_per_step": rays, "particles_per_step": particles,
+                   "l2": "flushed before every step (256 MiB write); maps total > L2"},
+        "particle_updates_per_s": ws * particles * args.steps / (total_b / 1e3),
+        "per_filter_fused_rays_per_s": rays * args.steps / (sum(tf) / 1e3),
+        "plain_per_call_rays_per_s": rays * plain_steps / tp,
+        "batched_over_plain": (rays * args.steps / (sum(tb) / 1e3)) / (rays * plain_steps / tp),
+        "weights_equal_per_filter_fused": same, "weights_equal_plain": same_plain,
+        "gpu_launches": launches, "setup_s": setup_s, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(json.dumps(line) + "\n")
+    return 0
+
+
+def run_cddt(args):
+    """CDDT (or pruned CDDT) queries on a 2048^2 rectangles-and-disks map: GPU table build
+    time and 1M-query throughput."""
+    import torch
+    import range_libc_gb300.range_libc as rl
+    from range_libc_gb300 import workloads as W
+
+    rank, ws, dist = dist_init()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    wl = W.cddt_queries(td=args.td)
+    omap = rl.PyOMap(np.ascontiguousarray(wl.occ.T))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m = rl.PyCDDTCast(omap, wl.max_range, args.td)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    prune_s = None
+    if args.prune:
+        t0 = time.perf_counter()
+        m.prune()
+        torch.cuda.synchronize()
+        prune_s = time.perf_counter() - t0
+    _, _, bin_len, zeros = m.table()
+    ins = torch.from_numpy(wl.ins).to(dev)
+    outs = torch.empty(len(wl.ins), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        m.calc_range_many(ins, outs)
+        return 1
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t, launches = _event_steps(torch, stream, args.steps, flush, step)
+    clk = clocks.stop()
+    total = max_over_ranks(dist, sum(t))
+    n = len(wl.ins)
+    value = ws * n * args.steps / (total / 1e3)
+    h_out = np.empty(n, np.float32)
+    t0 = time.perf_counter()
+    m.calc_range_many(wl.ins, h_out)
+    e2e_s = time.perf_counter() - t0
+    same = np.array_equal(h_out, outs.cpu().numpy())
+    line = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{'PCDDT' if args.prune else 'CDDT'} td {args.td}, 2048^2 rect/disk map, "
+                               f"{n} free-cell queries", "l2": "flushed before every step (256 MiB write)"},
+        "table": {"build_s": build_s, "prune_s": prune_s, "bins": int(len(bin_len)), "zeros": int(len(zeros)),
+                  "mean_bin": float(np.mean(bin_len)), "max_bin": int(np.max(bin_len))},
+        "e2e": {"value": n / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": wl.ins.nbytes,
+                "d2h_bytes_per_step": h_out.nbytes},
+        "host_equals_device": same, "gpu_launches": launches, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(json.dumps(line) + "\n")
     return 0
 
 

@@ -164,10 +164,14 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
                             unsigned flags, int64_t* total_steps);
 
 /* ---- tuning ------------------------------------------------------------ */
-/* Distance-transform layout for RM: 0 = linear x-major, 1 = 8x8 tiles; -1 = autotune on
- * the next fused call.  block = threads per block of the fused kernel (0 = default). */
-RLC_API int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block);
-RLC_API int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_block);
+/* Schedule of the kernels: dt_layout 0 = linear x-major distance transform, 1 = 8x8 tiles
+ * (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
+ * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray; tile =
+ * particles per tile of the fused and batched kernels (0 = automatic).  Results are identical
+ * under every schedule. */
+RLC_API int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile);
+RLC_API int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_block, int* prefetch,
+                                    int* tile);
 /* Time the schedule candidates on a workload (device pointers) and keep the fastest. */
 RLC_API int rlc_method_autotune(rlc_method* m, const float* d_ins, const float* d_angles, const float* d_obs,
                                 double* d_weights, int n, int num_angles, void* stream);

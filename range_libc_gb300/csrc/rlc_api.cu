@@ -126,7 +126,9 @@ struct rlc_method {
     int64_t trig_count = 0;
     // schedule
     int layout = DT_LINEAR;
+    int prefetch = 0;
     int fused_block = 256;
+    int tile = 0;             // particles per tile of the fused kernels (0 = auto)
     bool autotune_pending = false;
 
     ~rlc_method() {
@@ -530,14 +532,14 @@ int rlc_calc_range_many(rlc_method* m, const float* ins, float* outs, int n, uns
     CastParams p = m->params();
     bool world = !(flags & RLC_NO_WORLD);
     if (flags & RLC_DEVICE_PTRS)
-        return finish_launch(launch_calc_range_many(p, m->layout, world, ins, outs, n, s), "calc_range_many");
+        return finish_launch(launch_calc_range_many(p, m->layout, m->prefetch, world, ins, outs, n, s), "calc_range_many");
     size_t bin = align256((size_t)n * 3 * sizeof(float));
     void* st;
     if (int rc = m->stage(bin + (size_t)n * sizeof(float), &st)) return rc;
     float* d_in = (float*)st;
     float* d_out = (float*)((char*)st + bin);
     CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
-    CUDA_OR_FAIL(launch_calc_range_many(p, m->layout, world, d_in, d_out, n, s), "calc_range_many");
+    CUDA_OR_FAIL(launch_calc_range_many(p, m->layout, m->prefetch, world, d_in, d_out, n, s), "calc_range_many");
     CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
     CUDA_OR_FAIL(cudaStreamSynchronize(s), "calc_range_many");
     return RLC_OK;
@@ -554,7 +556,7 @@ int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* a
     cudaStream_t s = (cudaStream_t)stream;
     CastParams p = m->params();
     if (flags & RLC_DEVICE_PTRS)
-        return finish_launch(launch_repeat_angles(p, m->layout, ins, angles, outs, n, na, s), "repeat_angles");
+        return finish_launch(launch_repeat_angles(p, m->layout, m->prefetch, ins, angles, outs, n, na, s), "repeat_angles");
     size_t b0 = align256((size_t)n * 3 * sizeof(float));
     size_t b1 = align256((size_t)na * sizeof(float));
     void* st;
@@ -564,7 +566,7 @@ int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* a
     float* d_out = (float*)((char*)st + b0 + b1);
     CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
     CUDA_OR_FAIL(cudaMemcpyAsync(d_ang, angles, (size_t)na * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
-    CUDA_OR_FAIL(launch_repeat_angles(p, m->layout, d_in, d_ang, d_out, n, na, s), "repeat_angles");
+    CUDA_OR_FAIL(launch_repeat_angles(p, m->layout, m->prefetch, d_in, d_ang, d_out, n, na, s), "repeat_angles");
     CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, (size_t)n * na * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
     CUDA_OR_FAIL(cudaStreamSynchronize(s), "repeat_angles");
     return RLC_OK;
@@ -657,7 +659,8 @@ static int fused_device(rlc_method* m, const float* ins, const float* angles, co
     }
     CastParams p = m->params();
     SensorDev sm{m->d_table, m->K};
-    return finish_launch(launch_fused(p, m->layout, sm, ins, angles, obs, w, n, na, m->fused_block, s),
+    return finish_launch(launch_fused(p, m->layout, m->prefetch, sm, ins, angles, obs, w, n, na, m->fused_block,
+                                      m->tile, s),
                          "fused sensor model");
 }
 
@@ -692,24 +695,35 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
     return RLC_OK;
 }
 
-int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block) {
+int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile) {
     if (int rc = check_method(m)) return rc;
     if (dt_layout < -1 || dt_layout > 1) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0 or 1");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
-    if (dt_layout == -1) m->autotune_pending = true;
-    else m->layout = dt_layout;
+    if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
+    if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
+    if (dt_layout == -1) {
+        m->autotune_pending = true;
+    } else {
+        m->layout = dt_layout;
+        m->prefetch = prefetch;
+        m->tile = tile;
+    }
     if (fused_block) m->fused_block = fused_block;
     return RLC_OK;
 }
 
-int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_block) {
+int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_block, int* prefetch, int* tile) {
     if (int rc = check_method(m)) return rc;
     if (dt_layout) *dt_layout = m->layout;
     if (fused_block) *fused_block = m->fused_block;
+    if (prefetch) *prefetch = m->prefetch;
+    if (tile) *tile = m->tile;
     return RLC_OK;
 }
 
+// Times every schedule candidate (distance-transform layout x RM prefetch x
+// block size) on the caller's workload with CUDA events and keeps the fastest.
 int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
                         int na, void* stream) {
     if (int rc = check_method(m)) return rc;
@@ -719,31 +733,41 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
     cudaEvent_t e0, e1;
     CUDA_OR_FAIL(cudaEventCreate(&e0), "autotune");
     CUDA_OR_FAIL(cudaEventCreate(&e1), "autotune");
-    const int layouts[2] = {DT_LINEAR, DT_TILED};
     const int blocks[3] = {128, 256, 512};
+    const int tiles[3] = {0, 16, 32};
     float best = 1e30f;
-    int best_layout = m->layout, best_block = m->fused_block;
+    int best_layout = m->layout, best_block = m->fused_block, best_pf = m->prefetch, best_tile = m->tile;
     SensorDev sm{m->d_table, m->K};
     cudaError_t err = cudaSuccess;
-    for (int li = 0; li < (m->dkind == K_RM ? 2 : 1) && err == cudaSuccess; ++li) {
-        for (int bi = 0; bi < 3 && err == cudaSuccess; ++bi) {
-            m->layout = layouts[li];
-            CastParams p = m->params();
-            float total = 0.0f;
-            for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
-                err = launch_fused(p, m->layout, sm, ins, angles, obs, w, n, na, blocks[bi], s);   // warm
-                if (err == cudaSuccess) err = cudaEventRecord(e0, s);
-                if (err == cudaSuccess) err = launch_fused(p, m->layout, sm, ins, angles, obs, w, n, na, blocks[bi], s);
-                if (err == cudaSuccess) err = cudaEventRecord(e1, s);
-                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-                float ms = 0.0f;
-                if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-                if (rep > 0) total += ms;
-            }
-            if (err == cudaSuccess && total < best) {
-                best = total;
-                best_layout = layouts[li];
-                best_block = blocks[bi];
+    const bool rm = m->dkind == K_RM;
+    for (int li = 0; li < (rm ? 2 : 1) && err == cudaSuccess; ++li) {
+        for (int pf = 0; pf < (rm ? 2 : 1) && err == cudaSuccess; ++pf) {
+            for (int bi = 0; bi < 3 && err == cudaSuccess; ++bi) {
+                for (int ti = 0; ti < 3 && err == cudaSuccess; ++ti) {
+                    if (ti > 0 && tile_particles(na, blocks[bi], tiles[ti]) == tile_particles(na, blocks[bi], 0))
+                        continue;   // same tile as the automatic choice
+                    m->layout = li;
+                    CastParams p = m->params();
+                    float total = 0.0f;
+                    for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+                        err = launch_fused(p, li, pf, sm, ins, angles, obs, w, n, na, blocks[bi], tiles[ti], s);
+                        if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+                        if (err == cudaSuccess)
+                            err = launch_fused(p, li, pf, sm, ins, angles, obs, w, n, na, blocks[bi], tiles[ti], s);
+                        if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+                        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                        float ms = 0.0f;
+                        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+                        if (rep > 0) total += ms;
+                    }
+                    if (err == cudaSuccess && total < best) {
+                        best = total;
+                        best_layout = li;
+                        best_block = blocks[bi];
+                        best_pf = pf;
+                        best_tile = tiles[ti];
+                    }
+                }
             }
         }
     }
@@ -751,6 +775,8 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
     cudaEventDestroy(e1);
     m->layout = best_layout;
     m->fused_block = best_block;
+    m->prefetch = best_pf;
+    m->tile = best_tile;
     if (err != cudaSuccess) return cuda_fail(err, "autotune");
     return RLC_OK;
 }
@@ -805,6 +831,7 @@ int rlc_batch_create(const rlc_filter_desc* fd, int nf, int block, rlc_batch** o
         Item it{};
         it.f.p = m->params();
         it.f.layout = m->layout;
+        it.f.prefetch = m->prefetch;
         it.f.sm = SensorDev{m->d_table, m->K};
         it.f.ins = d.ins;
         it.f.angles = d.angles;
@@ -813,10 +840,10 @@ int rlc_batch_create(const rlc_filter_desc* fd, int nf, int block, rlc_batch** o
         it.f.weights = d.weights;
         it.f.n = d.n_particles;
         it.f.na = d.n_angles;
-        it.f.ppb = d.n_angles >= block ? 1 : (d.n_angles > 0 ? block / d.n_angles : block);
+        it.f.ppb = tile_particles(d.n_angles, block, m->tile > 0 ? m->tile : 32);
         // heavier tiles first: rays per tile x march length
         it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
-        smem = std::max(smem, (size_t)it.f.ppb * d.n_angles * sizeof(double));
+        smem = std::max(smem, tile_smem_bytes(it.f.ppb, d.n_angles));
         rays += (long long)d.n_particles * d.n_angles;
         items.push_back(it);
     }

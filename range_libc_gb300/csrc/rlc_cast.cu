@@ -20,6 +20,7 @@ constexpr double kM2Pi = 6.28318530718;           // RangeLib.h:61 M_2PI
 constexpr double kMPi = 3.14159265358979323846;   // <cmath> M_PI
 constexpr int kBinarySearchThreshold = 64;         // RangeLib.h:62
 constexpr int kMaxWrap = 100000;                   // bound on discretize_theta's loops
+constexpr int kPrefetch = 8;                        // RM prefetch distance (px) of the prefetching schedule
 
 __device__ __forceinline__ float ref_maxf(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float ref_minf(float a, float b) { return (b < a) ? b : a; }
@@ -32,6 +33,17 @@ __device__ __forceinline__ float dt_at(const MapDev& m, int x, int y) {
     return __ldg(m.dt + (size_t)x * m.H + y);
 }
 
+template <int LAYOUT>
+__device__ __forceinline__ const float* dt_ptr(const MapDev& m, int x, int y) {
+    if (LAYOUT == DT_TILED)
+        return m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7);
+    return m.dt + (size_t)x * m.H + y;
+}
+
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ bool occ_at(const MapDev& m, int x, int y) {
     if ((unsigned)x >= (unsigned)m.W || (unsigned)y >= (unsigned)m.H) return false;
     uint64_t w = __ldg(m.bits + (size_t)(x >> 3) * m.tiles_y + (y >> 3));
@@ -41,7 +53,12 @@ __device__ __forceinline__ bool occ_at(const MapDev& m, int x, int y) {
 // ------------------------------------------------------- ray marching (RM)
 // RangeLib.h:927-962 (RayMarching::calc_range).  t grows by >= 1 per step,
 // so the loop runs at most ceil(max_range) + 1 times.
-template <int LAYOUT>
+//
+// PF > 0: every step also issues an L1 prefetch of the cell PF pixels
+// further along the ray.  Near walls the march advances ~1 px per step, so
+// the cell a later step reads is already on its way when that step starts;
+// the prefetch is a hint and never changes a result.
+template <int LAYOUT, int PF = 0>
 __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps = nullptr) {
     if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
     float t = 0.0f;
@@ -49,6 +66,11 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
         int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
         int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
         if ((unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H) return mr;
+        if (PF > 0) {
+            const float tp = t + (float)PF;
+            const int qx = __float2int_rz(x0 + c * tp), qy = __float2int_rz(y0 + s * tp);
+            if ((unsigned)qx < (unsigned)m.W && (unsigned)qy < (unsigned)m.H) prefetch_l1(dt_ptr<LAYOUT>(m, qx, qy));
+        }
         float d = dt_at<LAYOUT>(m, px, py);
         if (steps) ++*steps;
         if (d <= 0.0f) {
@@ -218,7 +240,7 @@ __device__ float cddt_cast(const CastParams& p, float x, float y, float heading)
 }
 
 // ------------------------------------------------------------- dispatch
-template <int KIND, int LAYOUT>
+template <int KIND, int LAYOUT, int PF = 0>
 __device__ __forceinline__ float cast_one(const CastParams& p, float x, float y, float h, long long ray) {
     if (KIND == K_CDDT) return cddt_cast(p, x, y, h);
     float c, s;
@@ -228,7 +250,7 @@ __device__ __forceinline__ float cast_one(const CastParams& p, float x, float y,
     } else {
         sincosf(h, &s, &c);
     }
-    if (KIND == K_RM) return rm_cast<LAYOUT>(p.map, p.mr, x, y, c, s);
+    if (KIND == K_RM) return rm_cast<LAYOUT, PF>(p.map, p.mr, x, y, c, s);
     return bl_cast(p.map, p.mr, x, y, c, s, p.err);
 }
 
@@ -254,7 +276,7 @@ __device__ __forceinline__ int sensor_bin(float v, int K, unsigned* err) {
 }
 
 // ---------------------------------------------------------------- kernels
-template <int KIND, int LAYOUT, bool WORLD>
+template <int KIND, int LAYOUT, int PF, bool WORLD>
 __global__ void __launch_bounds__(256) k_calc_range_many(CastParams p, const float* __restrict__ ins,
                                                          float* __restrict__ outs, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -263,14 +285,14 @@ __global__ void __launch_bounds__(256) k_calc_range_many(CastParams p, const flo
     if (WORLD) {
         float ax, ay, th;
         world_to_grid(p.world, q0, q1, q2, ax, ay, th);
-        outs[i] = __fmul_rn(cast_one<KIND, LAYOUT>(p, ax, ay, th, i), p.world.s);
+        outs[i] = __fmul_rn(cast_one<KIND, LAYOUT, PF>(p, ax, ay, th, i), p.world.s);
     } else {
-        outs[i] = cast_one<KIND, LAYOUT>(p, q0, q1, q2, i);
+        outs[i] = cast_one<KIND, LAYOUT, PF>(p, q0, q1, q2, i);
     }
 }
 
 // RangeLib.h:482-520: rays are particle-major, ray = i * na + a
-template <int KIND, int LAYOUT>
+template <int KIND, int LAYOUT, int PF>
 __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float* __restrict__ ins,
                                                        const float* __restrict__ angles,
                                                        float* __restrict__ outs, int n, int na) {
@@ -281,83 +303,113 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
     float ax, ay, th;
     world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
                   __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
-    float r = cast_one<KIND, LAYOUT>(p, ax, ay, __fsub_rn(th, __ldg(angles + a)), g);
+    float r = cast_one<KIND, LAYOUT, PF>(p, ax, ay, __fsub_rn(th, __ldg(angles + a)), g);
     outs[g] = __fmul_rn(r, p.world.s);
 }
 
-// RangeLib.h:533-555: the weight is the product over beams in beam order
-__global__ void __launch_bounds__(512) k_eval_sensor(CastParams p, SensorDev sm, const float* __restrict__ obs,
-                                                     const float* __restrict__ ranges, double* __restrict__ outs,
-                                                     int na, int n, int ppb) {
-    extern __shared__ double fac[];
-    const int first = blockIdx.x * ppb;
-    const int nr = ppb * na;
-    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
-        int li = r / na, a = r - li * na, i = first + li;
-        if (i < n) {
-            int ri = sensor_bin(__fmul_rn(__ldg(obs + a), p.world.inv_s), sm.K, p.err);
-            int di = sensor_bin(__fmul_rn(__ldg(ranges + (size_t)i * na + a), p.world.inv_s), sm.K, p.err);
-            fac[r] = __ldg(sm.table + (size_t)ri * sm.K + di);
-        }
-    }
-    __syncthreads();
-    for (int li = threadIdx.x; li < ppb; li += blockDim.x) {
-        int i = first + li;
+// ------------------------------------------------------------ sensor model
+// The weight of a particle is the product of its beams' table values in beam
+// order (RangeLib.h:533-555, 558-612), in double, exactly as the reference
+// multiplies -- so weights are bit-identical.  A tile holds P particles;
+// its rays store their 16-bit range bin in shared memory (sdi, particle-
+// major), the beams' observation bins are in sri, and the products run one
+// particle per lane: each double multiply instruction then serves up to 32
+// particles instead of one.  Shared memory per block: (P * na + na) * 2 bytes.
+__device__ __forceinline__ void tile_products(const SensorDev& sm, const uint16_t* sdi, const uint16_t* sri, int na,
+                                              int P, int first, int n, double* __restrict__ weights) {
+    for (int li = threadIdx.x; li < P; li += blockDim.x) {
+        const int i = first + li;
         if (i >= n) continue;
+        const uint16_t* row = sdi + (size_t)li * na;
         double w = 1.0;
-        for (int a = 0; a < na; ++a) w = __dmul_rn(w, fac[li * na + a]);
-        outs[i] = w;
+#pragma unroll 8
+        for (int a = 0; a < na; ++a) w = __dmul_rn(w, __ldg(sm.table + (size_t)sri[a] * sm.K + row[a]));
+        weights[i] = w;
     }
 }
 
-// RangeLib.h:558-612: ranges stay in pixels; factors are staged in shared
-// memory and multiplied in beam order so the weight is bit-identical.
-template <int KIND, int LAYOUT>
-__global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
-                                               const float* __restrict__ angles, const float* __restrict__ obs,
-                                               double* __restrict__ weights, int n, int na, int ppb) {
-    extern __shared__ double fac[];
-    const int first = blockIdx.x * ppb;
-    const int nr = ppb * na;
+__device__ __forceinline__ void tile_obs_bins(const CastParams& p, const SensorDev& sm, const float* __restrict__ obs,
+                                              int na, uint16_t* sri) {
+    for (int a = threadIdx.x; a < na; a += blockDim.x)
+        sri[a] = (uint16_t)sensor_bin(__fmul_rn(__ldg(obs + a), p.world.inv_s), sm.K, p.err);
+}
+
+// RangeLib.h:533-555 on given ranges (world units)
+__global__ void __launch_bounds__(512) k_eval_sensor(CastParams p, SensorDev sm, const float* __restrict__ obs,
+                                                     const float* __restrict__ ranges, double* __restrict__ outs,
+                                                     int na, int n, int P) {
+    extern __shared__ uint16_t smem_u16[];
+    uint16_t* sdi = smem_u16;
+    uint16_t* sri = smem_u16 + (size_t)P * na;
+    const int first = blockIdx.x * P;
+    tile_obs_bins(p, sm, obs, na, sri);
+    const int nr = P * na;
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+        int li = r / na, a = r - li * na, i = first + li;
+        if (i < n) sdi[r] = (uint16_t)sensor_bin(__fmul_rn(__ldg(ranges + (size_t)i * na + a), p.world.inv_s), sm.K, p.err);
+    }
+    __syncthreads();
+    tile_products(sm, sdi, sri, na, P, first, n, outs);
+}
+
+// one tile of the fused update: cast P particles x na beams (ranges in
+// pixels, RangeLib.h:558-612), bin them, multiply per particle
+template <int KIND, int LAYOUT, int PF>
+__device__ __forceinline__ void fused_tile(const CastParams& p, const SensorDev& sm, const float* __restrict__ ins,
+                                           const float* __restrict__ angles, const float* __restrict__ obs,
+                                           double* __restrict__ weights, float* __restrict__ ranges, int n, int na,
+                                           int P, int first, uint16_t* sdi, uint16_t* sri, int layout, int pf) {
+    tile_obs_bins(p, sm, obs, na, sri);
+    const int nr = P * na;
     for (int r = threadIdx.x; r < nr; r += blockDim.x) {
         int li = r / na, a = r - li * na, i = first + li;
         if (i < n) {
             float ax, ay, th;
             world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
                           __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
-            float d = cast_one<KIND, LAYOUT>(p, ax, ay, __fsub_rn(th, __ldg(angles + a)), (long long)i * na + a);
-            int di = sensor_bin(d, sm.K, p.err);
-            int ri = sensor_bin(__fmul_rn(__ldg(obs + a), p.world.inv_s), sm.K, p.err);
-            fac[r] = __ldg(sm.table + (size_t)ri * sm.K + di);
+            const long long ray = (long long)i * na + a;
+            const float h = __fsub_rn(th, __ldg(angles + a));
+            float d;
+            if (KIND >= 0) {
+                d = cast_one<KIND, LAYOUT, PF>(p, ax, ay, h, ray);
+            } else {   // runtime dispatch (persistent multi-filter kernel)
+                if (p.kind == K_RM) {
+                    if (pf) d = layout == DT_TILED ? cast_one<K_RM, DT_TILED, kPrefetch>(p, ax, ay, h, ray)
+                                                   : cast_one<K_RM, DT_LINEAR, kPrefetch>(p, ax, ay, h, ray);
+                    else d = layout == DT_TILED ? cast_one<K_RM, DT_TILED, 0>(p, ax, ay, h, ray)
+                                                : cast_one<K_RM, DT_LINEAR, 0>(p, ax, ay, h, ray);
+                } else if (p.kind == K_BL) {
+                    d = cast_one<K_BL, DT_LINEAR, 0>(p, ax, ay, h, ray);
+                } else {
+                    d = cast_one<K_CDDT, DT_LINEAR, 0>(p, ax, ay, h, ray);
+                }
+            }
+            if (ranges) ranges[ray] = d;
+            sdi[r] = (uint16_t)sensor_bin(d, sm.K, p.err);
         }
     }
     __syncthreads();
-    for (int li = threadIdx.x; li < ppb; li += blockDim.x) {
-        int i = first + li;
-        if (i >= n) continue;
-        double w = 1.0;
-        for (int a = 0; a < na; ++a) w = __dmul_rn(w, fac[li * na + a]);
-        weights[i] = w;
-    }
+    tile_products(sm, sdi, sri, na, P, first, n, weights);
 }
 
+template <int KIND, int LAYOUT, int PF>
+__global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
+                                               const float* __restrict__ angles, const float* __restrict__ obs,
+                                               double* __restrict__ weights, int n, int na, int P) {
+    extern __shared__ uint16_t smem_u16[];
+    fused_tile<KIND, LAYOUT, PF>(p, sm, ins, angles, obs, weights, nullptr, n, na, P, blockIdx.x * P, smem_u16,
+                                 smem_u16 + (size_t)P * na, LAYOUT, PF);
+}
 
 // ------------------------------------------------- persistent multi-filter
-__device__ __forceinline__ float cast_dyn(const CastParams& p, int layout, float x, float y, float h, long long ray) {
-    if (p.kind == K_RM)
-        return layout == DT_TILED ? cast_one<K_RM, DT_TILED>(p, x, y, h, ray) : cast_one<K_RM, DT_LINEAR>(p, x, y, h, ray);
-    if (p.kind == K_BL) return cast_one<K_BL, DT_LINEAR>(p, x, y, h, ray);
-    return cast_one<K_CDDT, DT_LINEAR>(p, x, y, h, ray);
-}
-
 // Every block loops: take the next tile index from the device queue, cast
-// the tile's rays (whole particles of one filter) into shared memory, then
-// multiply each particle's factors in beam order.  Filters are stored in
-// descending per-tile cost, so heavy tiles are handed out first.  There is
-// no waiting on other blocks: a block that finds the queue exhausted exits.
+// the tile's rays (P particles of one filter) and multiply each particle's
+// factors in beam order.  Filters are stored in descending per-tile cost, so
+// heavy tiles are handed out first.  There is no waiting on other blocks: a
+// block that finds the queue exhausted exits.
 __global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
                                                unsigned* __restrict__ queue) {
-    extern __shared__ double fac[];
+    extern __shared__ uint16_t smem_u16[];
     __shared__ unsigned s_tile;
     __shared__ int s_f;
     for (;;) {
@@ -375,32 +427,10 @@ __global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ fil
         const unsigned t = s_tile;
         if (t >= total_tiles) break;
         const FilterDev& F = filters[s_f];
-        const int na = F.na, ppb = F.ppb;
-        const int first = (int)(t - F.tile_begin) * ppb;
-        const int nr = ppb * na;
-        for (int r = threadIdx.x; r < nr; r += blockDim.x) {
-            int li = r / na, a = r - li * na, i = first + li;
-            if (i < F.n) {
-                float ax, ay, th;
-                world_to_grid(F.p.world, __ldg(F.ins + 3 * (size_t)i), __ldg(F.ins + 3 * (size_t)i + 1),
-                              __ldg(F.ins + 3 * (size_t)i + 2), ax, ay, th);
-                long long ray = (long long)i * na + a;
-                float d = cast_dyn(F.p, F.layout, ax, ay, __fsub_rn(th, __ldg(F.angles + a)), ray);
-                if (F.ranges) F.ranges[ray] = d;
-                int di = sensor_bin(d, F.sm.K, F.p.err);
-                int ri = sensor_bin(__fmul_rn(__ldg(F.obs + a), F.p.world.inv_s), F.sm.K, F.p.err);
-                fac[r] = __ldg(F.sm.table + (size_t)ri * F.sm.K + di);
-            }
-        }
-        __syncthreads();
-        for (int li = threadIdx.x; li < ppb; li += blockDim.x) {
-            int i = first + li;
-            if (i >= F.n) continue;
-            double w = 1.0;
-            for (int a = 0; a < na; ++a) w = __dmul_rn(w, fac[li * na + a]);
-            F.weights[i] = w;
-        }
-        __syncthreads();
+        const int P = F.ppb;
+        fused_tile<-1, 0, 0>(F.p, F.sm, F.ins, F.angles, F.obs, F.weights, F.ranges, F.n, F.na, P,
+                             (int)(t - F.tile_begin) * P, smem_u16, smem_u16 + (size_t)P * F.na, F.layout, F.prefetch);
+        __syncthreads();   // before the next tile reuses shared memory and s_tile
     }
 }
 
@@ -429,44 +459,58 @@ __global__ void __launch_bounds__(256) k_count_steps(CastParams p, const float* 
 
 inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-template <template <int, int> class F, class... Args>
-cudaError_t dispatch(int kind, int layout, Args... args) {
+template <template <int, int, int> class F, class... Args>
+cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
     if (kind == K_RM) {
-        if (layout == DT_TILED) return F<K_RM, DT_TILED>::run(args...);
-        return F<K_RM, DT_LINEAR>::run(args...);
+        if (pf) {
+            if (layout == DT_TILED) return F<K_RM, DT_TILED, kPrefetch>::run(args...);
+            return F<K_RM, DT_LINEAR, kPrefetch>::run(args...);
+        }
+        if (layout == DT_TILED) return F<K_RM, DT_TILED, 0>::run(args...);
+        return F<K_RM, DT_LINEAR, 0>::run(args...);
     }
-    if (kind == K_BL) return F<K_BL, DT_LINEAR>::run(args...);
-    return F<K_CDDT, DT_LINEAR>::run(args...);
+    if (kind == K_BL) return F<K_BL, DT_LINEAR, 0>::run(args...);
+    return F<K_CDDT, DT_LINEAR, 0>::run(args...);
 }
 
-template <int KIND, int LAYOUT>
+template <int KIND, int LAYOUT, int PF>
 struct RunMany {
     static cudaError_t run(const CastParams& p, bool world, const float* ins, float* outs, int n, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
-        if (world) k_calc_range_many<KIND, LAYOUT, true><<<blocks_for(n, 256), 256, 0, s>>>(p, ins, outs, n);
-        else k_calc_range_many<KIND, LAYOUT, false><<<blocks_for(n, 256), 256, 0, s>>>(p, ins, outs, n);
+        if (world) k_calc_range_many<KIND, LAYOUT, PF, true><<<blocks_for(n, 256), 256, 0, s>>>(p, ins, outs, n);
+        else k_calc_range_many<KIND, LAYOUT, PF, false><<<blocks_for(n, 256), 256, 0, s>>>(p, ins, outs, n);
         return cudaGetLastError();
     }
 };
 
-template <int KIND, int LAYOUT>
+template <int KIND, int LAYOUT, int PF>
 struct RunAngles {
     static cudaError_t run(const CastParams& p, const float* ins, const float* angles, float* outs, int n, int na,
                            cudaStream_t s) {
         long long total = (long long)n * na;
         if (total <= 0) return cudaSuccess;
-        k_repeat_angles<KIND, LAYOUT><<<blocks_for(total, 256), 256, 0, s>>>(p, ins, angles, outs, n, na);
+        k_repeat_angles<KIND, LAYOUT, PF><<<blocks_for(total, 256), 256, 0, s>>>(p, ins, angles, outs, n, na);
         return cudaGetLastError();
     }
 };
 
-// particles per block and block size for the product kernels
-inline void product_shape(int na, int block, int& ppb, int& threads) {
+// Shared memory per block of the product kernels: P * na + na 16-bit bins.
+inline size_t tile_smem(int P, int na) { return (((size_t)P * na + (size_t)na) * sizeof(uint16_t) + 15) & ~(size_t)15; }
+
+// particles per tile (P) and threads per block: P = tile if given, else the
+// most particles whose rays fit one ray per thread; P is capped so that the
+// tile's bins fit kTileSmem bytes
+constexpr size_t kTileSmem = 48 * 1024;
+inline void product_shape(int na, int block, int tile, int& P, int& threads) {
     if (block <= 0) block = 256;
-    if (na <= 0) { ppb = block; threads = block; return; }   // empty product: weight 1.0
-    ppb = na >= block ? 1 : block / na;
-    int nr = ppb * na;
+    if (na <= 0) { P = block; threads = block; return; }   // empty product: weight 1.0
+    P = tile > 0 ? tile : (na >= block ? 1 : block / na);
+    int cap = (int)((kTileSmem / sizeof(uint16_t) - (size_t)na) / (size_t)na);
+    if (cap < 1) cap = 1;
+    if (P > cap) P = cap;
+    int nr = P * na;
     threads = nr >= block ? block : ((nr + 31) / 32) * 32;
+    if (threads < 32) threads = 32;
 }
 
 template <class K>
@@ -475,50 +519,58 @@ cudaError_t set_smem(K kernel, size_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <int KIND, int LAYOUT>
+template <int KIND, int LAYOUT, int PF>
 struct RunFused {
     static cudaError_t run(const CastParams& p, const SensorDev& sm, const float* ins, const float* angles,
-                           const float* obs, double* w, int n, int na, int block, cudaStream_t s) {
+                           const float* obs, double* w, int n, int na, int block, int tile, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
-        int ppb, threads;
-        product_shape(na, block, ppb, threads);
-        size_t smem = (size_t)ppb * na * sizeof(double);
-        cudaError_t e = set_smem(k_fused<KIND, LAYOUT>, smem);
+        int P, threads;
+        product_shape(na, block, tile, P, threads);
+        size_t smem = tile_smem(P, na);
+        cudaError_t e = set_smem(k_fused<KIND, LAYOUT, PF>, smem);
         if (e != cudaSuccess) return e;
-        k_fused<KIND, LAYOUT><<<blocks_for(n, ppb), threads, smem, s>>>(p, sm, ins, angles, obs, w, n, na, ppb);
+        k_fused<KIND, LAYOUT, PF><<<blocks_for(n, P), threads, smem, s>>>(p, sm, ins, angles, obs, w, n, na, P);
         return cudaGetLastError();
     }
 };
 
 }  // namespace
 
-cudaError_t launch_calc_range_many(const CastParams& p, int layout, bool world, const float* ins, float* outs,
-                                   int n, cudaStream_t s) {
-    return dispatch<RunMany>(p.kind, layout, p, world, ins, outs, n, s);
+cudaError_t launch_calc_range_many(const CastParams& p, int layout, int pf, bool world, const float* ins,
+                                   float* outs, int n, cudaStream_t s) {
+    return dispatch<RunMany>(p.kind, layout, pf, p, world, ins, outs, n, s);
 }
 
-cudaError_t launch_repeat_angles(const CastParams& p, int layout, const float* ins, const float* angles,
+cudaError_t launch_repeat_angles(const CastParams& p, int layout, int pf, const float* ins, const float* angles,
                                  float* outs, int n, int na, cudaStream_t s) {
-    return dispatch<RunAngles>(p.kind, layout, p, ins, angles, outs, n, na, s);
+    return dispatch<RunAngles>(p.kind, layout, pf, p, ins, angles, outs, n, na, s);
 }
 
 cudaError_t launch_eval_sensor(const CastParams& p, const SensorDev& sm, const float* obs, const float* ranges,
                                double* outs, int na, int n, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    int ppb, threads;
-    product_shape(na, 256, ppb, threads);
-    size_t smem = (size_t)ppb * na * sizeof(double);
+    int P, threads;
+    product_shape(na, 256, 0, P, threads);
+    size_t smem = tile_smem(P, na);
     cudaError_t e = set_smem(k_eval_sensor, smem);
     if (e != cudaSuccess) return e;
-    k_eval_sensor<<<blocks_for(n, ppb), threads, smem, s>>>(p, sm, obs, ranges, outs, na, n, ppb);
+    k_eval_sensor<<<blocks_for(n, P), threads, smem, s>>>(p, sm, obs, ranges, outs, na, n, P);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fused(const CastParams& p, int layout, const SensorDev& sm, const float* ins,
-                         const float* angles, const float* obs, double* weights, int n, int na, int block,
+cudaError_t launch_fused(const CastParams& p, int layout, int pf, const SensorDev& sm, const float* ins,
+                         const float* angles, const float* obs, double* weights, int n, int na, int block, int tile,
                          cudaStream_t s) {
-    return dispatch<RunFused>(p.kind, layout, p, sm, ins, angles, obs, weights, n, na, block, s);
+    return dispatch<RunFused>(p.kind, layout, pf, p, sm, ins, angles, obs, weights, n, na, block, tile, s);
 }
+
+int tile_particles(int na, int block, int tile) {
+    int P, threads;
+    product_shape(na, block, tile, P, threads);
+    return P;
+}
+
+size_t tile_smem_bytes(int P, int na) { return tile_smem(P, na); }
 
 cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,
                                unsigned long long* total, cudaStream_t s) {

@@ -81,15 +81,20 @@ cudaError_t launch_edge_map(const uint64_t* d_bits, int W, int H, int tiles_y, u
 cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_occ, cudaStream_t s);
 
 // ---- casting (rlc_cast.cu) ----
-cudaError_t launch_calc_range_many(const CastParams& p, int layout, bool world, const float* ins,
+// layout: DtLayout of the distance transform; pf: 1 = RM prefetching schedule
+cudaError_t launch_calc_range_many(const CastParams& p, int layout, int pf, bool world, const float* ins,
                                    float* outs, int n, cudaStream_t s);
-cudaError_t launch_repeat_angles(const CastParams& p, int layout, const float* ins, const float* angles,
+cudaError_t launch_repeat_angles(const CastParams& p, int layout, int pf, const float* ins, const float* angles,
                                  float* outs, int n, int na, cudaStream_t s);
 cudaError_t launch_eval_sensor(const CastParams& p, const SensorDev& sm, const float* obs,
                                const float* ranges, double* outs, int na, int n, cudaStream_t s);
-cudaError_t launch_fused(const CastParams& p, int layout, const SensorDev& sm, const float* ins,
+// block: threads per block (0 = 256); tile: particles per tile (0 = auto)
+cudaError_t launch_fused(const CastParams& p, int layout, int pf, const SensorDev& sm, const float* ins,
                          const float* angles, const float* obs, double* weights, int n, int na,
-                         int block, cudaStream_t s);
+                         int block, int tile, cudaStream_t s);
+// particles per tile the fused kernels use, and the shared memory of such a tile
+int tile_particles(int na, int block, int tile);
+size_t tile_smem_bytes(int P, int na);
 
 // march steps of world-frame repeat-angle rays (RM and BL), summed into *total
 cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,
@@ -99,6 +104,7 @@ cudaError_t launch_count_steps(const CastParams& p, const float* ins, const floa
 struct FilterDev {
     CastParams p;
     int layout;
+    int prefetch;
     SensorDev sm;
     const float* ins;
     const float* angles;

@@ -418,13 +418,25 @@ class _RangeMethod:
         call("rlc_count_steps", self._h, pi, pa, ins.shape[0], angles.shape[0], flags, C.byref(tot))
         return tot.value
 
-    def set_schedule(self, dt_layout: int = 0, fused_block: int = 0) -> None:
-        call("rlc_method_set_schedule", self._h, int(dt_layout), int(fused_block))
+    def set_schedule(self, dt_layout: int = 0, fused_block: int = 0, prefetch: int = 0, tile: int = 0) -> None:
+        """dt_layout 0 linear / 1 tiled (-1: autotune on the next fused call), threads per block
+        of the fused kernel (0 keeps it), prefetch 0/1, particles per tile (0 automatic).
+        Results do not depend on the schedule."""
+        call("rlc_method_set_schedule", self._h, int(dt_layout), int(fused_block), int(prefetch), int(tile))
 
     def schedule(self):
-        a, b = C.c_int(), C.c_int()
-        call("rlc_method_get_schedule", self._h, C.byref(a), C.byref(b))
-        return a.value, b.value
+        """(dt_layout, fused_block, prefetch, tile)"""
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        call("rlc_method_get_schedule", self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d))
+        return a.value, b.value, c.value, d.value
+
+    def autotune(self, ins, angles, obs, weights) -> None:
+        """Time the schedule candidates on this workload (CUDA tensors) and keep the fastest."""
+        ptrs = [_arg(a, dt, nd, nm) for a, dt, nd, nm in ((ins, np.float32, 2, "ins"), (angles, np.float32, 1, "angles"),
+                                                          (obs, np.float32, 1, "obs"), (weights, np.float64, 1, "weights"))]
+        if not all(d for _, d in ptrs):
+            raise ValueError("autotune takes CUDA tensors")
+        call("rlc_method_autotune", self._h, *[p for p, _ in ptrs], ins.shape[0], angles.shape[0], _stream_of(ins))
 
 
 class PyBresenhamsLine(_RangeMethod):

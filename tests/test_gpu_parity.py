@@ -375,3 +375,34 @@ def test_batch_matches_per_filter_calls(rl, oracle_mod):
         for f, (w, r) in zip(filters, expect):
             assert np.array_equal(f[4].cpu().numpy(), w)
             assert np.array_equal(f[5].cpu().numpy(), r)
+
+
+def test_results_do_not_depend_on_the_schedule(rl):
+    """Every schedule (DT layout x prefetch x block size) gives bit-identical ranges and weights."""
+    torch = pytest.importorskip("torch")
+    wl = _pf(n=700, side=1024)
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyRayMarching(m, wl.max_range)
+    g.set_sensor_model(wl.table)
+    base_w = np.empty(len(wl.ins), np.float64)
+    base_r = np.empty(len(wl.ins) * len(wl.angles), np.float32)
+    g.set_schedule(0, 256, 0, 0)
+    g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, base_w)
+    g.calc_range_repeat_angles(wl.ins, wl.angles, base_r)
+    for layout in (0, 1):
+        for pf in (0, 1):
+            for block in (64, 128, 512):
+                for tile in (0, 1, 7, 32):
+                    g.set_schedule(layout, block, pf, tile)
+                    w = np.empty_like(base_w)
+                    r = np.empty_like(base_r)
+                    g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, w)
+                    g.calc_range_repeat_angles(wl.ins, wl.angles, r)
+                    assert np.array_equal(w, base_w) and np.array_equal(r, base_r), (layout, pf, block, tile)
+    dev = torch.device("cuda:0")
+    ins, ang, obs = (torch.from_numpy(a).to(dev) for a in (wl.ins, wl.angles, wl.obs))
+    w = torch.empty(len(wl.ins), dtype=torch.float64, device=dev)
+    g.autotune(ins, ang, obs, w)
+    g.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs, w)
+    torch.cuda.synchronize()
+    assert np.array_equal(w.cpu().numpy(), base_w)
