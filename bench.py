@@ -405,10 +405,11 @@ def run_batch(args):
     particles = sum(len(wl.ins) for wl in host)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    # per-filter schedules: autotune each filter's fused kernel on its own workload
+    # per-filter schedules for the per-filter comparison, one batch schedule for the batch
     for m, ins, ang, obs, w in filters:
         m.autotune(ins, ang, obs, w)
     batch = rl.PyFilterBatch(filters)
+    batch.autotune()
 
     def batched():
         batch.run()
@@ -467,6 +468,7 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
         "config": {"workload": "32 uneven filters (maps 512-4096 px, RM), one persistent launch as a CUDA graph",
                    "filters": len(filters), "rays_per_step": rays, "particles_per_step": particles,
+                   "schedule": dict(zip(("dt_layout", "prefetch", "block", "tile"), batch.schedule())),
                    "l2": "flushed before every step (256 MiB write); maps total > L2"},
         "particle_updates_per_s": ws * particles * args.steps / (total_b / 1e3),
         "per_filter_fused_rays_per_s": rays * args.steps / (sum(tf) / 1e3),

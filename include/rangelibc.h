@@ -164,8 +164,8 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
                             unsigned flags, int64_t* total_steps);
 
 /* ---- tuning ------------------------------------------------------------ */
-/* Schedule of the kernels: dt_layout 0 = linear x-major distance transform, 1 = 8x8 tiles
- * (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
+/* Schedule of the kernels: dt_layout 0 = linear x-major distance transform, 1 = 8x8 tiles,
+ * 2 = compact 16-bit squared distances (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
  * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray; tile =
  * particles per tile of the fused and batched kernels (0 = automatic).  Results are identical
  * under every schedule. */
@@ -211,6 +211,13 @@ typedef struct rlc_filter_desc {
 /* The methods must outlive the batch.  block = threads per block (0 = 256). */
 RLC_API int rlc_batch_create(const rlc_filter_desc* filters, int n_filters, int block, rlc_batch** out);
 RLC_API int rlc_batch_run(rlc_batch* b, void* stream);
+/* Schedule of the persistent launch: distance-transform layout (0 linear, 1 tiled, 2 compact
+ * 16-bit) and prefetch of every ray-marching filter, threads per block, particles per tile
+ * (0 = 32).  Results are identical under every schedule. */
+RLC_API int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile);
+RLC_API int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, int* block, int* tile);
+/* Run the batch under each schedule candidate on `stream` and keep the fastest. */
+RLC_API int rlc_batch_autotune(rlc_batch* b, void* stream);
 RLC_API int rlc_batch_destroy(rlc_batch* b);
 /* rays = sum of n_particles * n_angles; tiles = work items of the device queue */
 RLC_API int rlc_batch_info(const rlc_batch* b, int64_t* rays, int64_t* tiles);

@@ -58,6 +58,7 @@ struct rlc_map {
     uint64_t* d_bits = nullptr;
     float* d_dt = nullptr;
     float* d_dt_tiled = nullptr;
+    uint16_t* d_dt16 = nullptr;
     std::atomic<int> refs{1};
     std::mutex mu;
 
@@ -65,6 +66,7 @@ struct rlc_map {
         cudaFree(d_bits);
         cudaFree(d_dt);
         cudaFree(d_dt_tiled);
+        cudaFree(d_dt16);
     }
     // distance transform on first use (RayMarching constructor, RangeLib.h:924)
     int ensure_dt() {
@@ -74,22 +76,27 @@ struct rlc_map {
         size_t tiled = (size_t)((W + 7) >> 3) * TY * 64;
         float* dt = nullptr;
         float* dtt = nullptr;
+        uint16_t* dt16 = nullptr;
         void* scratch = nullptr;
         size_t sb = edt_scratch_bytes(W, H);
         cudaError_t e = cudaMalloc(&dt, (n ? n : 1) * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&dtt, (tiled ? tiled : 1) * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&dt16, (tiled ? tiled : 1) * sizeof(uint16_t));
         if (e == cudaSuccess) e = cudaMalloc(&scratch, sb);
         if (e == cudaSuccess) e = launch_edt(d_bits, W, H, TY, dt, scratch, sb, 0);
         if (e == cudaSuccess) e = launch_dt_to_tiled(dt, W, H, dtt, 0);
+        if (e == cudaSuccess) e = launch_dt_to_u16(dt, W, H, dt16, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         cudaFree(scratch);
         if (e != cudaSuccess) {
             cudaFree(dt);
             cudaFree(dtt);
+            cudaFree(dt16);
             return cuda_fail(e, "distance transform");
         }
         d_dt = dt;
         d_dt_tiled = dtt;
+        d_dt16 = dt16;
         return RLC_OK;
     }
     void retain() { refs.fetch_add(1); }
@@ -154,6 +161,7 @@ struct rlc_method {
         p.map.H = map->H;
         p.map.tiles_y = map->TY;
         p.map.dt = layout == DT_TILED ? map->d_dt_tiled : map->d_dt;
+        p.map.dt16 = map->d_dt16;
         p.map.bits = map->d_bits;
         p.cddt.td = td;
         p.cddt.td_div_2pi = td_div_2pi;
@@ -697,7 +705,7 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
 
 int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile) {
     if (int rc = check_method(m)) return rc;
-    if (dt_layout < -1 || dt_layout > 1) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0 or 1");
+    if (dt_layout < -1 || dt_layout > 2) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1 or 2");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
     if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
@@ -740,7 +748,7 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
     SensorDev sm{m->d_table, m->K};
     cudaError_t err = cudaSuccess;
     const bool rm = m->dkind == K_RM;
-    for (int li = 0; li < (rm ? 2 : 1) && err == cudaSuccess; ++li) {
+    for (int li = 0; li < (rm ? 3 : 1) && err == cudaSuccess; ++li) {
         for (int pf = 0; pf < (rm ? 2 : 1) && err == cudaSuccess; ++pf) {
             for (int bi = 0; bi < 3 && err == cudaSuccess; ++bi) {
                 for (int ti = 0; ti < 3 && err == cudaSuccess; ++ti) {
@@ -785,22 +793,116 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
 
 // ============================================================ batched filters
 struct rlc_batch {
+    std::vector<rlc_filter_desc> descs;
+    bool rm_only = true;
+    // schedule
+    int layout = DT_LINEAR, prefetch = 0, block = 256, tile = 0;
+    // built state
     int nf = 0;
     FilterDev* d_filters = nullptr;
     unsigned* d_queue = nullptr;
     unsigned total_tiles = 0;
     long long rays = 0;
-    int block = 256, grid = 0;
+    int grid = 0;
     size_t smem = 0;
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    ~rlc_batch() {
+
+    void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+    ~rlc_batch() {
+        drop_graph();
         if (cap) cudaStreamDestroy(cap);
         cudaFree(d_filters);
         cudaFree(d_queue);
+    }
+
+    // (re)build the device filter table for the current schedule
+    int build() {
+        drop_graph();
+        struct Item { FilterDev f; double cost; };
+        std::vector<Item> items;
+        size_t sm_bytes = 0;
+        for (const rlc_filter_desc& d : descs) {
+            rlc_method* m = d.method;
+            Item it{};
+            CastParams p = m->params();
+            if (m->dkind == K_RM) {   // the batch schedule's layout for every ray-marching filter
+                p.map.dt = layout == DT_TILED ? m->map->d_dt_tiled : m->map->d_dt;
+            }
+            it.f.p = p;
+            it.f.layout = layout;
+            it.f.prefetch = prefetch;
+            it.f.sm = SensorDev{m->d_table, m->K};
+            it.f.ins = d.ins;
+            it.f.angles = d.angles;
+            it.f.obs = d.obs;
+            it.f.ranges = d.ranges;
+            it.f.weights = d.weights;
+            it.f.n = d.n_particles;
+            it.f.na = d.n_angles;
+            it.f.ppb = tile_particles(d.n_angles, block, tile > 0 ? tile : 32);
+            // heavier tiles first: rays per tile x march length
+            it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
+            sm_bytes = std::max(sm_bytes, tile_smem_bytes(it.f.ppb, d.n_angles));
+            items.push_back(it);
+        }
+        std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
+        unsigned long long tiles = 0;
+        std::vector<FilterDev> hf;
+        for (auto& it : items) {
+            it.f.tile_begin = (unsigned)tiles;
+            tiles += (unsigned long long)((it.f.n + it.f.ppb - 1) / it.f.ppb);
+            if (tiles >= 0xffffffffull) return fail(RLC_ERR_ARG, "too many tiles in one batch");
+            hf.push_back(it.f);
+        }
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = batch_occupancy(block, sm_bytes, rm_only, layout, prefetch, &per_sm);
+        if (e == cudaSuccess && per_sm <= 0) e = cudaErrorInvalidConfiguration;
+        if (e == cudaSuccess && !d_filters) e = cudaMalloc(&d_filters, descs.size() * sizeof(FilterDev));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_filters, hf.data(), hf.size() * sizeof(FilterDev), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && !d_queue) e = cudaMalloc(&d_queue, sizeof(unsigned));
+        if (e == cudaSuccess && !cap) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail(e, "batch setup");
+        nf = (int)hf.size();
+        total_tiles = (unsigned)tiles;
+        smem = sm_bytes;
+        long long g = (long long)sms * per_sm;
+        if (g > (long long)tiles) g = (long long)tiles;
+        grid = (int)(g > 0 ? g : 1);
+        return RLC_OK;
+    }
+
+    // queue reset + persistent kernel, captured once as a CUDA graph
+    int launch(cudaStream_t stream) {
+        if (total_tiles == 0) return RLC_OK;
+        if (!exec) {
+            CUDA_OR_FAIL(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "batch capture");
+            cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned), cap);
+            if (e == cudaSuccess)
+                e = launch_batch(d_filters, nf, total_tiles, d_queue, grid, block, smem, rm_only, layout, prefetch,
+                                 cap);
+            cudaGraph_t g = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+            if (e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                exec = nullptr;
+                return cuda_fail(e, "batch graph");
+            }
+            graph = g;
+        }
+        CUDA_OR_FAIL(cudaGraphLaunch(exec, stream), "batch launch");
+        return RLC_OK;
     }
 };
 
@@ -812,10 +914,8 @@ int rlc_batch_create(const rlc_filter_desc* fd, int nf, int block, rlc_batch** o
     if (nf <= 0 || !fd) return fail(RLC_ERR_ARG, "a batch needs at least one filter");
     if (block == 0) block = 256;
     if (block < 32 || block > 512 || block % 32) return fail(RLC_ERR_ARG, "block must be a multiple of 32 in [32, 512]");
-    struct Item { FilterDev f; double cost; };
-    std::vector<Item> items;
     long long rays = 0;
-    size_t smem = 0;
+    bool rm_only = true;
     for (int i = 0; i < nf; ++i) {
         const rlc_filter_desc& d = fd[i];
         rlc_method* m = d.method;
@@ -828,82 +928,96 @@ int rlc_batch_create(const rlc_filter_desc* fd, int nf, int block, rlc_batch** o
         if ((long long)d.n_particles * d.n_angles > (1ll << 31) - 1) return fail(RLC_ERR_ARG, "filter %d: too many rays", i);
         if (m->d_trig && m->trig_count < (long long)d.n_particles * d.n_angles)
             return fail(RLC_ERR_ARG, "filter %d: trig override too short", i);
-        Item it{};
-        it.f.p = m->params();
-        it.f.layout = m->layout;
-        it.f.prefetch = m->prefetch;
-        it.f.sm = SensorDev{m->d_table, m->K};
-        it.f.ins = d.ins;
-        it.f.angles = d.angles;
-        it.f.obs = d.obs;
-        it.f.ranges = d.ranges;
-        it.f.weights = d.weights;
-        it.f.n = d.n_particles;
-        it.f.na = d.n_angles;
-        it.f.ppb = tile_particles(d.n_angles, block, m->tile > 0 ? m->tile : 32);
-        // heavier tiles first: rays per tile x march length
-        it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
-        smem = std::max(smem, tile_smem_bytes(it.f.ppb, d.n_angles));
         rays += (long long)d.n_particles * d.n_angles;
-        items.push_back(it);
-    }
-    std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
-    unsigned long long tiles = 0;
-    std::vector<FilterDev> hf;
-    for (auto& it : items) {
-        it.f.tile_begin = (unsigned)tiles;
-        tiles += (unsigned long long)((it.f.n + it.f.ppb - 1) / it.f.ppb);
-        if (tiles >= 0xffffffffull) return fail(RLC_ERR_ARG, "too many tiles in one batch");
-        hf.push_back(it.f);
+        if (m->dkind != K_RM) rm_only = false;
     }
     rlc_batch* b = new rlc_batch();
-    b->nf = nf;
-    b->total_tiles = (unsigned)tiles;
-    b->rays = rays;
+    b->descs.assign(fd, fd + nf);
+    b->rm_only = rm_only;
     b->block = block;
-    b->smem = smem;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = batch_occupancy(block, smem, &per_sm);
-    if (e == cudaSuccess && per_sm <= 0) e = cudaErrorInvalidConfiguration;
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_filters, hf.size() * sizeof(FilterDev));
-    if (e == cudaSuccess) e = cudaMemcpy(b->d_filters, hf.data(), hf.size() * sizeof(FilterDev), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
-    if (e != cudaSuccess) {
+    b->rays = rays;
+    if (int rc = b->build()) {
         delete b;
-        return cuda_fail(e, "batch setup");
+        return rc;
     }
-    long long g = (long long)sms * per_sm;
-    if (g > (long long)tiles) g = (long long)tiles;
-    b->grid = (int)(g > 0 ? g : 1);
     *out = b;
     return RLC_OK;
 }
 
+int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile) {
+    if (!b) return fail(RLC_ERR_ARG, "null batch handle");
+    if (dt_layout < 0 || dt_layout > 2) return fail(RLC_ERR_ARG, "dt_layout must be 0, 1 or 2");
+    if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
+    if (block != 0 && (block < 32 || block > 512 || block % 32)) return fail(RLC_ERR_ARG, "block must be a multiple of 32 in [32, 512]");
+    if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
+    b->layout = dt_layout;
+    b->prefetch = prefetch;
+    if (block) b->block = block;
+    b->tile = tile;
+    return b->build();
+}
+
+int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, int* block, int* tile) {
+    if (!b) return fail(RLC_ERR_ARG, "null batch handle");
+    if (dt_layout) *dt_layout = b->layout;
+    if (prefetch) *prefetch = b->prefetch;
+    if (block) *block = b->block;
+    if (tile) *tile = b->tile;
+    return RLC_OK;
+}
+
+// Runs the batch under each schedule candidate (outputs are overwritten with
+// identical values), keeps the fastest.
+int rlc_batch_autotune(rlc_batch* b, void* stream) {
+    if (!b) return fail(RLC_ERR_ARG, "null batch handle");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    CUDA_OR_FAIL(cudaEventCreate(&e0), "batch autotune");
+    CUDA_OR_FAIL(cudaEventCreate(&e1), "batch autotune");
+    const int blocks[2] = {256, 512};
+    const int tiles[3] = {8, 16, 32};
+    float best = 1e30f;
+    int bl = b->layout, bp = b->prefetch, bb = b->block, bt = b->tile;
+    int rc = RLC_OK;
+    for (int li = 0; li < 3 && !rc; ++li)
+        for (int pf = 0; pf < 2 && !rc; ++pf)
+            for (int bi = 0; bi < 2 && !rc; ++bi)
+                for (int ti = 0; ti < 3 && !rc; ++ti) {
+                    if (!b->rm_only && (li != 0 || pf != 0)) continue;
+                    b->layout = li;
+                    b->prefetch = pf;
+                    b->block = blocks[bi];
+                    b->tile = tiles[ti];
+                    if ((rc = b->build())) break;
+                    if ((rc = b->launch(s))) break;   // warm (and graph capture)
+                    cudaEventRecord(e0, s);
+                    for (int rep = 0; rep < 2 && !rc; ++rep) rc = b->launch(s);
+                    cudaEventRecord(e1, s);
+                    cudaError_t e = cudaEventSynchronize(e1);
+                    float ms = 0.0f;
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                    if (e != cudaSuccess) rc = cuda_fail(e, "batch autotune");
+                    if (!rc && ms < best) {
+                        best = ms;
+                        bl = li;
+                        bp = pf;
+                        bb = blocks[bi];
+                        bt = tiles[ti];
+                    }
+                }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->layout = bl;
+    b->prefetch = bp;
+    b->block = bb;
+    b->tile = bt;
+    int rc2 = b->build();
+    return rc ? rc : rc2;
+}
+
 int rlc_batch_run(rlc_batch* b, void* stream) {
     if (!b) return fail(RLC_ERR_ARG, "null batch handle");
-    if (b->total_tiles == 0) return RLC_OK;
-    if (!b->exec) {
-        // capture [queue reset, persistent kernel] once; later runs replay the graph
-        CUDA_OR_FAIL(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal), "batch capture");
-        cudaError_t e = cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned), b->cap);
-        if (e == cudaSuccess)
-            e = launch_batch(b->d_filters, b->nf, b->total_tiles, b->d_queue, b->grid, b->block, b->smem, b->cap);
-        cudaGraph_t g = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(b->cap, &g);
-        if (e == cudaSuccess) e = e2;
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
-        if (e != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            b->exec = nullptr;
-            return cuda_fail(e, "batch graph");
-        }
-        b->graph = g;
-    }
-    CUDA_OR_FAIL(cudaGraphLaunch(b->exec, (cudaStream_t)stream), "batch launch");
-    return RLC_OK;
+    return b->launch((cudaStream_t)stream);
 }
 
 int rlc_batch_destroy(rlc_batch* b) {

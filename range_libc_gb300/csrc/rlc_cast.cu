@@ -21,20 +21,33 @@ constexpr double kMPi = 3.14159265358979323846;   // <cmath> M_PI
 constexpr int kBinarySearchThreshold = 64;         // RangeLib.h:62
 constexpr int kMaxWrap = 100000;                   // bound on discretize_theta's loops
 constexpr int kPrefetch = 8;                        // RM prefetch distance (px) of the prefetching schedule
+constexpr int kAnyKind = -1;                        // fused_tile: kind, layout and prefetch chosen per filter
+constexpr int kRmOnly = -2;                         // fused_tile: every filter ray-marches (LAYOUT, PF given)
 
 __device__ __forceinline__ float ref_maxf(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float ref_minf(float a, float b) { return (b < a) ? b : a; }
 
 // ---------------------------------------------------------------- map access
+__device__ __forceinline__ size_t u16_index(const MapDev& m, int x, int y) {
+    return ((((size_t)(x >> 3) * m.tiles_y + (y >> 3))) << 6) + ((((x >> 2) & 1) << 1 | ((y >> 2) & 1)) << 4) +
+           (((x & 3) << 2) | (y & 3));
+}
+
 template <int LAYOUT>
 __device__ __forceinline__ float dt_at(const MapDev& m, int x, int y) {
+    if (LAYOUT == DT_U16) {
+        const unsigned v = __ldg(m.dt16 + u16_index(m, x, y));
+        if (v == 0xFFFFu) return __ldg(m.dt + (size_t)x * m.H + y);   // d^2 >= 65535: the float itself
+        return __fsqrt_rn(__uint2float_rn(v));                         // == sqrtf(D) of the distance transform
+    }
     if (LAYOUT == DT_TILED)
         return __ldg(m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7));
     return __ldg(m.dt + (size_t)x * m.H + y);
 }
 
 template <int LAYOUT>
-__device__ __forceinline__ const float* dt_ptr(const MapDev& m, int x, int y) {
+__device__ __forceinline__ const void* dt_ptr(const MapDev& m, int x, int y) {
+    if (LAYOUT == DT_U16) return m.dt16 + u16_index(m, x, y);
     if (LAYOUT == DT_TILED)
         return m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7);
     return m.dt + (size_t)x * m.H + y;
@@ -372,12 +385,16 @@ __device__ __forceinline__ void fused_tile(const CastParams& p, const SensorDev&
             float d;
             if (KIND >= 0) {
                 d = cast_one<KIND, LAYOUT, PF>(p, ax, ay, h, ray);
-            } else {   // runtime dispatch (persistent multi-filter kernel)
+            } else if (KIND == kRmOnly) {   // persistent kernel, every filter ray-marches
+                d = cast_one<K_RM, LAYOUT, PF>(p, ax, ay, h, ray);
+            } else {   // persistent kernel, mixed kinds: dispatch at run time
                 if (p.kind == K_RM) {
-                    if (pf) d = layout == DT_TILED ? cast_one<K_RM, DT_TILED, kPrefetch>(p, ax, ay, h, ray)
-                                                   : cast_one<K_RM, DT_LINEAR, kPrefetch>(p, ax, ay, h, ray);
-                    else d = layout == DT_TILED ? cast_one<K_RM, DT_TILED, 0>(p, ax, ay, h, ray)
-                                                : cast_one<K_RM, DT_LINEAR, 0>(p, ax, ay, h, ray);
+                    if (layout == DT_U16) d = pf ? cast_one<K_RM, DT_U16, kPrefetch>(p, ax, ay, h, ray)
+                                                 : cast_one<K_RM, DT_U16, 0>(p, ax, ay, h, ray);
+                    else if (layout == DT_TILED) d = pf ? cast_one<K_RM, DT_TILED, kPrefetch>(p, ax, ay, h, ray)
+                                                        : cast_one<K_RM, DT_TILED, 0>(p, ax, ay, h, ray);
+                    else d = pf ? cast_one<K_RM, DT_LINEAR, kPrefetch>(p, ax, ay, h, ray)
+                                : cast_one<K_RM, DT_LINEAR, 0>(p, ax, ay, h, ray);
                 } else if (p.kind == K_BL) {
                     d = cast_one<K_BL, DT_LINEAR, 0>(p, ax, ay, h, ray);
                 } else {
@@ -407,6 +424,7 @@ __global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const
 // factors in beam order.  Filters are stored in descending per-tile cost, so
 // heavy tiles are handed out first.  There is no waiting on other blocks: a
 // block that finds the queue exhausted exits.
+template <int MODE, int LAYOUT, int PF>
 __global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
                                                unsigned* __restrict__ queue) {
     extern __shared__ uint16_t smem_u16[];
@@ -428,7 +446,7 @@ __global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ fil
         if (t >= total_tiles) break;
         const FilterDev& F = filters[s_f];
         const int P = F.ppb;
-        fused_tile<-1, 0, 0>(F.p, F.sm, F.ins, F.angles, F.obs, F.weights, F.ranges, F.n, F.na, P,
+        fused_tile<MODE, LAYOUT, PF>(F.p, F.sm, F.ins, F.angles, F.obs, F.weights, F.ranges, F.n, F.na, P,
                              (int)(t - F.tile_begin) * P, smem_u16, smem_u16 + (size_t)P * F.na, F.layout, F.prefetch);
         __syncthreads();   // before the next tile reuses shared memory and s_tile
     }
@@ -463,9 +481,11 @@ template <template <int, int, int> class F, class... Args>
 cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
     if (kind == K_RM) {
         if (pf) {
+            if (layout == DT_U16) return F<K_RM, DT_U16, kPrefetch>::run(args...);
             if (layout == DT_TILED) return F<K_RM, DT_TILED, kPrefetch>::run(args...);
             return F<K_RM, DT_LINEAR, kPrefetch>::run(args...);
         }
+        if (layout == DT_U16) return F<K_RM, DT_U16, 0>::run(args...);
         if (layout == DT_TILED) return F<K_RM, DT_TILED, 0>::run(args...);
         return F<K_RM, DT_LINEAR, 0>::run(args...);
     }
@@ -582,18 +602,34 @@ cudaError_t launch_count_steps(const CastParams& p, const float* ins, const floa
     return cudaGetLastError();
 }
 
-cudaError_t batch_occupancy(int block, size_t smem, int* blocks_per_sm) {
-    cudaError_t e = set_smem(k_batch, smem);
+// batch kernel variant for (rm_only, layout, pf)
+typedef void (*BatchKernel)(const FilterDev*, int, unsigned, unsigned*);
+static BatchKernel batch_kernel(bool rm_only, int layout, int pf) {
+    if (!rm_only) return k_batch<kAnyKind, 0, 0>;
+    if (pf) {
+        if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, kPrefetch>;
+        if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, kPrefetch>;
+        return k_batch<kRmOnly, DT_LINEAR, kPrefetch>;
+    }
+    if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, 0>;
+    if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, 0>;
+    return k_batch<kRmOnly, DT_LINEAR, 0>;
+}
+
+cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, int* blocks_per_sm) {
+    BatchKernel k = batch_kernel(rm_only, layout, pf);
+    cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch, block, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, block, smem);
 }
 
 cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tiles, unsigned* queue, int grid,
-                         int block, size_t smem, cudaStream_t s) {
+                         int block, size_t smem, bool rm_only, int layout, int pf, cudaStream_t s) {
     if (total_tiles == 0 || nf == 0) return cudaSuccess;
-    cudaError_t e = set_smem(k_batch, smem);
+    BatchKernel k = batch_kernel(rm_only, layout, pf);
+    cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
-    k_batch<<<grid, block, smem, s>>>(d_filters, nf, total_tiles, queue);
+    k<<<grid, block, smem, s>>>(d_filters, nf, total_tiles, queue);
     return cudaGetLastError();
 }
 

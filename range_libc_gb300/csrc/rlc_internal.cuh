@@ -8,7 +8,11 @@
 //     bit ((x & 7) << 3 | (y & 7)) of word (x >> 3) * tiles_y + (y >> 3).
 //   * distance transform: float, either linear x-major (x * height + y,
 //     the reference's kernels.cu:15-17 layout) or 8x8 tiles of 64 floats
-//     (256 B, two 128-B lines) in the same tile order.
+//     (256 B, two 128-B lines) in the same tile order; or the compact form:
+//     the integer squared distance d^2 as uint16 in 8x8 tiles of 128 B whose
+//     four 32-B sectors hold 4x4 cells each, 0xFFFF meaning "d^2 >= 65535,
+//     read the float".  Every DT value is sqrtf of an integer below 2^24, so
+//     sqrtf(d^2) reproduces it exactly.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -26,12 +30,13 @@ enum DevFlag : unsigned {
     F_NAN_INDEX = 8u,      // NaN range/observation mapped to sensor bin 0
 };
 
-enum DtLayout : int { DT_LINEAR = 0, DT_TILED = 1 };
+enum DtLayout : int { DT_LINEAR = 0, DT_TILED = 1, DT_U16 = 2 };
 
 struct MapDev {
     int W, H;
     int tiles_y;              // ceil(H / 8)
-    const float* dt;          // distance transform (layout per DtLayout)
+    const float* dt;          // distance transform (DT_LINEAR / DT_TILED; linear for DT_U16)
+    const uint16_t* dt16;     // compact squared distances (DT_U16)
     const uint64_t* bits;     // occupancy bit tiles
 };
 
@@ -77,6 +82,7 @@ constexpr size_t edt_scratch_bound(size_t cells, size_t side) {
     return ((cells * 4 + 255) & ~(size_t)255) + cells * 4 + (cells + side) * 8 + 256;
 }
 cudaError_t launch_dt_to_tiled(const float* d_lin, int W, int H, float* d_tiled, cudaStream_t s);
+cudaError_t launch_dt_to_u16(const float* d_lin, int W, int H, uint16_t* d_u16, cudaStream_t s);
 cudaError_t launch_edge_map(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_edge, cudaStream_t s);
 cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_occ, cudaStream_t s);
 
@@ -115,10 +121,13 @@ struct FilterDev {
     unsigned tile_begin;      // first global tile of this filter
 };
 // Persistent launch: `grid` blocks of `block` threads draw tiles from *queue
-// (which must be zero) until all `total_tiles` are done.
+// (which must be zero) until all `total_tiles` are done.  rm_only selects the
+// kernel specialised for batches whose filters all ray-march, with the
+// distance-transform layout and prefetch given; otherwise every filter's own
+// kind, layout and prefetch are dispatched at run time.
 cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tiles, unsigned* queue, int grid,
-                         int block, size_t smem, cudaStream_t s);
-cudaError_t batch_occupancy(int block, size_t smem, int* blocks_per_sm);
+                         int block, size_t smem, bool rm_only, int layout, int pf, cudaStream_t s);
+cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, int* blocks_per_sm);
 
 // ---- CDDT table (rlc_cddt.cu) ----
 struct CddtBuild {

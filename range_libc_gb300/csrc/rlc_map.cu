@@ -122,6 +122,27 @@ __global__ void k_dt_to_tiled(const float* __restrict__ lin, int W, int H, int T
     tiled[i] = (x < W && y < H) ? lin[(size_t)x * H + y] : 0.0f;
 }
 
+// compact distance transform: uint16 d^2 in 8x8 tiles, 4x4 cells per 32-B sector
+__global__ void k_dt_to_u16(const float* __restrict__ lin, int W, int H, int TY, uint16_t* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int TX = (W + 7) >> 3;
+    if (i >= (long long)TX * TY * 64) return;
+    long long tile = i >> 6;
+    int within = (int)(i & 63);
+    int sector = within >> 4, cell = within & 15;
+    int tx = (int)(tile / TY), ty = (int)(tile - (long long)tx * TY);
+    int x = (tx << 3) + ((sector >> 1) << 2) + (cell >> 2);
+    int y = (ty << 3) + ((sector & 1) << 2) + (cell & 3);
+    uint16_t v = 0xFFFF;
+    if (x < W && y < H) {
+        // dt = sqrtf(D) for an integer D; D is recovered exactly while D < 2^22
+        double d = (double)lin[(size_t)x * H + y];
+        double d2 = rint(d * d);
+        if (d2 < 65535.0 && __fsqrt_rn((float)d2) == (float)d) v = (uint16_t)d2;
+    }
+    out[i] = v;
+}
+
 // RangeLib.h:293-312: an occupied cell with any in-grid free 8-neighbour.
 __global__ void k_edge_map(const uint64_t* __restrict__ bits, int W, int H, int TY, uint8_t* __restrict__ edge) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -192,6 +213,14 @@ cudaError_t launch_dt_to_tiled(const float* d_lin, int W, int H, float* d_tiled,
     long long n = (long long)TX * TY * 64;
     if (n == 0) return cudaSuccess;
     k_dt_to_tiled<<<blocks_for(n, 256), 256, 0, s>>>(d_lin, W, H, TY, d_tiled);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dt_to_u16(const float* d_lin, int W, int H, uint16_t* d_u16, cudaStream_t s) {
+    int TY = (H + 7) >> 3, TX = (W + 7) >> 3;
+    long long n = (long long)TX * TY * 64;
+    if (n == 0) return cudaSuccess;
+    k_dt_to_u16<<<blocks_for(n, 256), 256, 0, s>>>(d_lin, W, H, TY, d_u16);
     return cudaGetLastError();
 }
 

@@ -545,6 +545,19 @@ class PyFilterBatch:
     def run(self) -> None:
         call("rlc_batch_run", self._h, _stream_of(self._keep[0][1]))
 
+    def set_schedule(self, dt_layout: int = 0, prefetch: int = 0, block: int = 0, tile: int = 0) -> None:
+        call("rlc_batch_set_schedule", self._h, int(dt_layout), int(prefetch), int(block), int(tile))
+
+    def schedule(self):
+        """(dt_layout, prefetch, block, tile)"""
+        v = [C.c_int() for _ in range(4)]
+        call("rlc_batch_get_schedule", self._h, *[C.byref(x) for x in v])
+        return tuple(x.value for x in v)
+
+    def autotune(self) -> None:
+        """Run the batch under each schedule candidate and keep the fastest (outputs are rewritten)."""
+        call("rlc_batch_autotune", self._h, _stream_of(self._keep[0][1]))
+
     def info(self):
         r, t = C.c_int64(), C.c_int64()
         call("rlc_batch_info", self._h, C.byref(r), C.byref(t))

@@ -367,14 +367,49 @@ def test_batch_matches_per_filter_calls(rl, oracle_mod):
     batch = rl.PyFilterBatch(filters)
     rays, tiles = batch.info()
     assert rays == sum(len(f[1]) * len(f[2]) for f in filters) and tiles > 0
-    for _ in range(3):   # graph replays
-        for f in filters:
-            f[4].zero_()
-        batch.run()
-        torch.cuda.synchronize()
-        for f, (w, r) in zip(filters, expect):
-            assert np.array_equal(f[4].cpu().numpy(), w)
-            assert np.array_equal(f[5].cpu().numpy(), r)
+    for sched in ((0, 0, 256, 0), (1, 1, 128, 8), (2, 1, 512, 32), (2, 0, 256, 3)):
+        batch.set_schedule(*sched)
+        for _ in range(2):   # graph replays
+            for f in filters:
+                f[4].zero_()
+                f[5].zero_()
+            batch.run()
+            torch.cuda.synchronize()
+            for f, (w, r) in zip(filters, expect):
+                assert np.array_equal(f[4].cpu().numpy(), w), sched
+                assert np.array_equal(f[5].cpu().numpy(), r), sched
+    batch.autotune()
+    batch.run()
+    torch.cuda.synchronize()
+    for f, (w, r) in zip(filters, expect):
+        assert np.array_equal(f[4].cpu().numpy(), w)
+
+
+def test_batch_of_ray_marchers_schedules(rl):
+    """The ray-marching-only persistent kernel: every layout and prefetch gives the per-filter weights."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    filters, expect, keep = [], [], []
+    for spec in (W.FilterSpec(512, 400, 61, 200.0, 61), W.FilterSpec(1024, 90, 900, 350.0, 62),
+                 W.FilterSpec(256, 1200, 33, 120.0, 63)):
+        wl = W.batch_filter(spec)
+        m = _pymap(rl, wl.occ)
+        g = rl.PyRayMarching(m, wl.max_range)
+        g.set_sensor_model(wl.table)
+        w = np.empty(len(wl.ins), np.float64)
+        g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, w)
+        expect.append(w)
+        t = [torch.from_numpy(a).to(dev) for a in (wl.ins, wl.angles, wl.obs)]
+        filters.append((g, t[0], t[1], t[2], torch.zeros(len(wl.ins), dtype=torch.float64, device=dev)))
+        keep.append(m)
+    batch = rl.PyFilterBatch(filters)
+    for layout in (0, 1, 2):
+        for pf in (0, 1):
+            batch.set_schedule(layout, pf, 256, 16)
+            batch.run()
+            torch.cuda.synchronize()
+            for f, w in zip(filters, expect):
+                assert np.array_equal(f[4].cpu().numpy(), w), (layout, pf)
 
 
 def test_results_do_not_depend_on_the_schedule(rl):
@@ -389,7 +424,7 @@ def test_results_do_not_depend_on_the_schedule(rl):
     g.set_schedule(0, 256, 0, 0)
     g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, base_w)
     g.calc_range_repeat_angles(wl.ins, wl.angles, base_r)
-    for layout in (0, 1):
+    for layout in (0, 1, 2):
         for pf in (0, 1):
             for block in (64, 128, 512):
                 for tile in (0, 1, 7, 32):
