@@ -200,7 +200,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="fused", choices=["fused", "plain", "batch", "cddt"])
+    ap.add_argument("--workload", default="fused", choices=["fused", "plain", "batch", "cddt", "learned"])
+    ap.add_argument("--train-rays", type=int, default=64_000_000, help="learned workload: training rays")
     ap.add_argument("--td", type=int, default=108, help="cddt workload: theta discretization")
     ap.add_argument("--prune", action="store_true", help="cddt workload: pruned table (PCDDT)")
     ap.add_argument("--filters", type=int, default=32, help="batch workload: number of filters")
@@ -216,6 +217,8 @@ def main():
         return run_batch(args)
     if args.workload == "cddt":
         return run_cddt(args)
+    if args.workload == "learned":
+        return run_learned(args)
 
     import torch
     import range_libc_gb300.range_libc as rl
@@ -542,6 +545,113 @@ def run_cddt(args):
         "e2e": {"value": n / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": wl.ins.nbytes,
                 "d2h_bytes_per_step": h_out.nbytes},
         "host_equals_device": same, "gpu_launches": launches, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(json.dumps(line) + "\n")
+    return 0
+
+
+def run_learned(args):
+    """Learned range surrogate on a 4096^2 rectangles-and-disks map: train on rays from the
+    exact marcher, then 10,000 particles x 108 beams through the learned query (accept check +
+    exact recast) against the exact path; range and weight errors on the same queries."""
+    import torch
+    import range_libc_gb300.range_libc as rl
+    from range_libc_gb300 import workloads as W
+
+    rank, ws, dist = dist_init()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    mr = 300.0
+    occ = W.rect_disk_map(4096, 5000)
+    omap = rl.PyOMap(np.ascontiguousarray(occ.T))
+    rm = rl.PyRayMarching(omap, mr)
+    K = int(mr) + 1
+    table = W.sensor_table(K)
+    rm.set_sensor_model(table)
+    model = rl.PyLearnedRM(rm, seed=1)
+    batch = 8192
+    steps = max(1, args.train_rays // batch)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = model.train(steps=steps, batch=batch, lr=2e-3, seed=2)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+
+    # held-out rays: hit-parameter error of the raw predictions
+    xyt, t_true, _ = model.sample_rays(2_000_000, first_id=4_000_000_000 // 2, seed=77)
+    pred = model.predict(xyt)
+    e_t = (pred - t_true).abs().cpu().numpy()
+
+    # the query workload: 10,000 particles x 108 beams, free-cell poses, uniform headings
+    fs = W.free_cell_queries(occ, 10_000, 5001)
+    ins_np = np.stack([fs[:, 1], fs[:, 0], fs[:, 2]], 1).astype(np.float32)   # world frame, identity map world
+    ang_np = np.linspace(-np.pi, np.pi, 108, endpoint=False).astype(np.float32)
+    obs_np = np.random.default_rng(5002).uniform(0, mr, 108).astype(np.float32)
+    ins, ang, obs = (torch.from_numpy(a).to(dev) for a in (ins_np, ang_np, obs_np))
+    n, na = len(ins_np), len(ang_np)
+    out_l = torch.empty(n * na, dtype=torch.float32, device=dev)
+    out_e = torch.empty(n * na, dtype=torch.float32, device=dev)
+    acc = torch.empty(n * na, dtype=torch.uint8, device=dev)
+    w_l = torch.empty(n, dtype=torch.float64, device=dev)
+    w_e = torch.empty(n, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    rm.autotune(ins, ang, obs, w_e)
+
+    def exact_step():
+        rm.calc_range_repeat_angles(ins, ang, out_e)
+        return 1
+
+    def exact_fused():
+        rm.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs, w_e)
+        return 1
+
+    n_recast = [0]
+
+    def learned_step():
+        n_recast[0] = model.calc_range_repeat_angles(ins, ang, out_l, acc)
+        return 1
+
+    for f in (exact_step, exact_fused, learned_step):
+        for _ in range(args.warmup):
+            f()
+    te, _ = _event_steps(torch, stream, args.steps, flush, exact_step)
+    tf, _ = _event_steps(torch, stream, args.steps, flush, exact_fused)
+    tl, _ = _event_steps(torch, stream, args.steps, flush, learned_step)
+    rm.eval_sensor_model(obs, out_l, w_l, na, n)
+    torch.cuda.synchronize()
+    ol, oe = out_l.cpu().numpy(), out_e.cpu().numpy()
+    a = acc.cpu().numpy().astype(bool)
+    err = np.abs(ol - oe)
+    wl_, we_ = w_l.cpu().numpy(), w_e.cpu().numpy()
+    pos = (we_ > 0) & (wl_ > 0)
+    rel_w = np.abs(wl_[pos] - we_[pos]) / we_[pos]
+    logw = np.abs(np.log(wl_[pos]) - np.log(we_[pos]))
+    rays = n * na
+    line = {
+        "metric": METRIC, "value": rays * args.steps / (sum(tl) / 1e3), "unit": "rays/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(tl) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 MLP (fp32 accumulate) + f32 exact recast",
+        "data": "synthetic",
+        "config": {"workload": "learned surrogate, 4096^2 rect/disk map, RM max_range 300 px, 10,000 particles x 108 "
+                               "beams; MLP 512 Fourier features -> 4 x 256 GELU -> 1",
+                   "train_rays": steps * batch, "train_batch": batch, "train_s": train_s, "final_loss": loss},
+        "exact_repeat_angles_rays_per_s": rays * args.steps / (sum(te) / 1e3),
+        "exact_fused_rays_per_s": rays * args.steps / (sum(tf) / 1e3),
+        "learned_over_exact": (sum(te) / sum(tl)),
+        "fallback_rate": n_recast[0] / rays,
+        "heldout_t_error_px": {"median": float(np.median(e_t)), "p99": float(np.percentile(e_t, 99))},
+        "range_error_px_all": {"median": float(np.median(err)), "p99": float(np.percentile(err, 99))},
+        "range_error_px_accepted": {"median": float(np.median(err[a])) if a.any() else None,
+                                    "p99": float(np.percentile(err[a], 99)) if a.any() else None,
+                                    "exact_fraction": float(np.mean(err[a] == 0)) if a.any() else None},
+        "weight_error": {"median_rel": float(np.median(rel_w)) if len(rel_w) else None,
+                         "p99_rel": float(np.percentile(rel_w, 99)) if len(rel_w) else None,
+                         "median_abs_log": float(np.median(logw)) if len(logw) else None},
+        "gpu_launches": None,
     }
     if rank == 0:
         print(json.dumps(line))

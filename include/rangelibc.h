@@ -222,6 +222,36 @@ RLC_API int rlc_batch_destroy(rlc_batch* b);
 /* rays = sum of n_particles * n_angles; tiles = work items of the device queue */
 RLC_API int rlc_batch_info(const rlc_batch* b, int64_t* rays, int64_t* tiles);
 
+/* ---- learned range surrogate (no reference counterpart) ----------------------
+ * A per-map MLP (512 Fourier features of x/W, y/H, cos, sin -> 4 x 256 GELU -> 1) predicting
+ * where a ray reaches its hit cell, trained on the GPU (tcgen05 BF16 GEMMs, FP32 accumulation,
+ * Adam) on rays cast by the exact ray marcher of an RM method.  Queries accept a prediction
+ * whose cell is occupied while the cell one pixel before is free, returning the reference's
+ * distance to that cell's corner; every other ray is recast exactly.  Device pointers. */
+typedef struct rlc_learned rlc_learned;
+RLC_API int rlc_learned_create(const rlc_method* ray_marching, unsigned seed, rlc_learned** out);
+RLC_API int rlc_learned_destroy(rlc_learned* l);
+RLC_API int64_t rlc_learned_param_count(void);
+RLC_API int rlc_learned_get_params(rlc_learned* l, float* host_params);
+RLC_API int rlc_learned_set_params(rlc_learned* l, const float* host_params);
+/* n rays from uniform free-cell poses: grid-frame (x, y, theta) [n][3], hit parameter t, exact range */
+RLC_API int rlc_learned_sample_rays(rlc_learned* l, long long first_id, unsigned seed, int n, float* d_xyt,
+                                    float* d_t, float* d_range, void* stream);
+RLC_API int rlc_learned_train(rlc_learned* l, int steps, int batch, float lr, unsigned seed, float* final_loss,
+                              void* stream);
+RLC_API int rlc_learned_predict(rlc_learned* l, const float* d_xyt, int n, float* d_pred, void* stream);
+RLC_API int rlc_learned_calc_range_repeat_angles(rlc_learned* l, const float* d_ins, const float* d_angles,
+                                                 float* d_outs, int n, int num_angles, uint8_t* d_accepted,
+                                                 int64_t* n_recast, void* stream);
+/* testing: features of grid-frame rays (bf16 [n][512]); gradients of the mean Huber loss over n
+ * (a multiple of 128) rays into host_grads [rlc_learned_param_count()]; a tensor-core GEMM
+ * C[M x N] = A . B^T (bf16 in, fp32 out; A is K x M when a_t, B is K x N when b_t). */
+RLC_API int rlc_learned_features(rlc_learned* l, const float* d_xyt, int n, void* d_out);
+RLC_API int rlc_learned_gradients(rlc_learned* l, const float* d_xyt, const float* d_t, int n, float* host_grads,
+                                  float* host_loss);
+RLC_API int rlc_tc_gemm(const void* d_a, const void* d_b, float* d_c, int M, int N, int K, int a_t, int b_t,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,18 @@ SIGNATURES = {
     "rlc_method_get_schedule": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p]),
     "rlc_method_autotune": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "rlc_distance_transform_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "rlc_learned_create": (C.c_int, [_vp, C.c_uint, C.POINTER(_vp)]),
+    "rlc_learned_destroy": (C.c_int, [_vp]),
+    "rlc_learned_param_count": (C.c_int64, []),
+    "rlc_learned_get_params": (C.c_int, [_vp, _f32p]),
+    "rlc_learned_set_params": (C.c_int, [_vp, _f32p]),
+    "rlc_learned_sample_rays": (C.c_int, [_vp, C.c_longlong, C.c_uint, C.c_int, _vp, _vp, _vp, _vp]),
+    "rlc_learned_train": (C.c_int, [_vp, C.c_int, C.c_int, C.c_float, C.c_uint, _f32p, _vp]),
+    "rlc_learned_predict": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "rlc_learned_calc_range_repeat_angles": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp, _i64p, _vp]),
+    "rlc_learned_features": (C.c_int, [_vp, _vp, C.c_int, _vp]),
+    "rlc_learned_gradients": (C.c_int, [_vp, _vp, _vp, C.c_int, _f32p, _f32p]),
+    "rlc_tc_gemm": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp]),
     "rlc_batch_create": (C.c_int, [C.POINTER(FilterDesc), C.c_int, C.c_int, C.POINTER(_vp)]),
     "rlc_batch_run": (C.c_int, [_vp, _vp]),
     "rlc_batch_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),

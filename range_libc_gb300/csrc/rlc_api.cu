@@ -193,6 +193,17 @@ struct rlc_method {
     }
 };
 
+int rlc::method_map_view(const rlc_method* m, MapDev* map, WorldDev* world, float* max_range) {
+    if (!m) return fail(RLC_ERR_ARG, "null method handle");
+    if (m->dkind != K_RM) return fail(RLC_ERR_ARG, "the learned surrogate is built on a ray-marching method");
+    CastParams p = m->params();
+    p.map.dt = m->map->d_dt;
+    *map = p.map;
+    *world = p.world;
+    *max_range = m->mr;
+    return RLC_OK;
+}
+
 namespace {
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }

@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+struct rlc_method;
+
 namespace rlc {
 
 enum Kind : int { K_BL = 0, K_RM = 1, K_CDDT = 2 };
@@ -145,6 +147,10 @@ cudaError_t cddt_build(const uint64_t* d_bits, int W, int H, int tiles_y, unsign
 cudaError_t cddt_prune(const uint64_t* d_bits, int W, int H, int tiles_y, unsigned td, float max_range,
                        const int* d_widths, const float* d_trans, const float* d_cos, const float* d_sin,
                        CddtBuild* tab, cudaStream_t s);
+
+// the device view of a ray-marching method's map (linear DT), world frame and
+// max_range; RLC_ERR_* on a null or non-RM method (rlc_api.cu)
+int method_map_view(const struct ::rlc_method* m, MapDev* map, WorldDev* world, float* max_range);
 
 // ---- error reporting (rlc_api.cu) ----
 // records `msg` as the calling thread's rlc_last_error() text and returns `code`

@@ -1,0 +1,914 @@
+// Learned range surrogate: a per-map MLP that predicts where a ray meets a
+// wall, trained on rays cast by the exact GPU ray marcher, with hand-written
+// tcgen05 (TMEM-accumulating) BF16 GEMMs for the forward and backward passes
+// and an Adam kernel.  No counterpart in the reference.
+//
+// Model: the grid-frame ray (x, y, theta) becomes u = (x/W, y/H, cos, sin);
+// each of the 4 inputs is expanded by 64 sinusoidal frequencies f_k =
+// fmax^(k/63) (sin and cos of pi f_k u) into 512 features, then four hidden
+// layers of width 256 with GELU (tanh form), then one linear output: the
+// march parameter t at which the exact marcher reaches its hit cell (pixels).
+// Weights and activations are BF16, accumulation and the output layer FP32.
+//
+// A prediction t^ is accepted when the cell at x0 + t^ dir is occupied and
+// the cell at x0 + (t^ - 1) dir is free; the range returned is then the
+// reference's distance to that cell's corner, otherwise the ray is recast
+// exactly (compacted into a dense second pass).
+#include "rangelibc.h"
+#include "rlc_internal.cuh"
+#include "rlc_tc.cuh"
+
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace rlc {
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kFeat = 512;      // 4 inputs x 64 frequencies x {sin, cos}
+constexpr int kHidden = 256;
+constexpr int kLayers = 4;      // hidden layers
+constexpr int kBM = 128;        // GEMM tile rows (TMEM lanes)
+constexpr int kBN = 256;        // GEMM tile columns (TMEM columns)
+
+// flat fp32 parameter layout
+constexpr size_t kW0 = (size_t)kHidden * kFeat;              // layer 0: 256 x 512 (out x in)
+constexpr size_t kWh = (size_t)kHidden * kHidden;            // layers 1-3: 256 x 256
+constexpr size_t kParamCount = kW0 + kHidden + 3 * (kWh + kHidden) + kHidden + 1;
+
+__host__ __device__ inline size_t w_offset(int l) { return l == 0 ? 0 : kW0 + kHidden + (size_t)(l - 1) * (kWh + kHidden); }
+__host__ __device__ inline size_t b_offset(int l) { return w_offset(l) + (l == 0 ? kW0 : kWh); }
+__host__ __device__ inline int layer_in(int l) { return l == 0 ? kFeat : kHidden; }
+constexpr size_t kOutW = kW0 + kHidden + 3 * (kWh + kHidden);  // output weights [256], then bias [1]
+
+// -------------------------------------------------------------------- GEMM
+enum Epi : int { EPI_F32 = 0, EPI_FWD = 1, EPI_BWD = 2 };
+
+struct GemmArgs {
+    const bf16* A;   // a_t ? A[k * lda + m] : A[m * lda + k]
+    const bf16* B;   // b_t ? B[k * ldb + n] : B[n * ldb + k]
+    int lda, ldb, a_t, b_t;
+    int M, N, K;
+    int epi;
+    int ldc;
+    float* C32;         // EPI_F32: C[m * ldc + n]
+    const float* bias;  // EPI_FWD
+    bf16* Zout;         // EPI_FWD: pre-activation
+    bf16* Hout;         // EPI_FWD: GELU(z)
+    const bf16* Zin;    // EPI_BWD: pre-activation of the layer below
+    bf16* dZ;           // EPI_BWD: acc * GELU'(Zin)
+    unsigned* err;
+};
+
+__device__ __forceinline__ float gelu(float z) {
+    const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+    return 0.5f * z * (1.0f + tanhf(k0 * (z + k1 * z * z * z)));
+}
+
+__device__ __forceinline__ float gelu_grad(float z) {
+    const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+    float u = k0 * (z + k1 * z * z * z);
+    float th = tanhf(u);
+    return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * k0 * (1.0f + 3.0f * k1 * z * z);
+}
+
+// load one K chunk (64) of `rows` rows of an operand into the core-matrix layout
+__device__ __forceinline__ void load_tile(uint8_t* dst, const bf16* src, int ld, int trans, int r0, int rows, int k0) {
+    const int nvec = rows * 8;   // 16-byte vectors of 8 elements
+    if (!trans) {
+        for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
+            const int row = v >> 3, kv = v & 7;
+            const uint4 val = *reinterpret_cast<const uint4*>(src + (size_t)(r0 + row) * ld + k0 + kv * 8);
+            *reinterpret_cast<uint4*>(dst + tc::core_offset(row, kv * 8)) = val;
+        }
+    } else {
+        const int rvecs = rows >> 3;
+        for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
+            const int k = v / rvecs, rv = v - k * rvecs;
+            const uint4 val = *reinterpret_cast<const uint4*>(src + (size_t)(k0 + k) * ld + r0 + rv * 8);
+            const bf16* e = reinterpret_cast<const bf16*>(&val);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) *reinterpret_cast<bf16*>(dst + tc::core_offset(rv * 8 + i, k)) = e[i];
+        }
+    }
+}
+
+// C tile [128 x 256] at (blockIdx.y * 128, blockIdx.x * 256): two smem stages of
+// A (16 KB) and B (32 KB), MMA issued by thread 0, accumulator in 256 TMEM columns.
+__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    uint8_t* sA[2] = {smem, smem + 16384};
+    uint8_t* sB[2] = {smem + 32768, smem + 65536};
+    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_addr(&mbar[0]), 1);
+        tc::mbar_init(tc::smem_addr(&mbar[1]), 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = tc::make_idesc(kBM, kBN);
+    const int nchunks = g.K / tc::kKChunk;
+    bool ok = true;
+    for (int c = 0; c < nchunks && ok; ++c) {
+        const int s = c & 1;
+        if (c >= 2) {   // stage s is free once the MMAs of chunk c - 2 completed
+            const bool w = tc::mbar_wait(tc::smem_addr(&mbar[s]), ((c - 2) >> 1) & 1);
+            ok = __syncthreads_and(w) != 0;
+            if (!ok) break;
+        }
+        load_tile(sA[s], g.A, g.lda, g.a_t, m0, kBM, c * tc::kKChunk);
+        load_tile(sB[s], g.B, g.ldb, g.b_t, n0, kBN, c * tc::kKChunk);
+        tc::fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tc::fence_after_sync();
+            const uint32_t a0 = tc::smem_addr(sA[s]), b0 = tc::smem_addr(sB[s]);
+#pragma unroll
+            for (int ks = 0; ks < tc::kKChunk / 16; ++ks) {
+                const uint64_t ad = tc::make_desc(a0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
+                const uint64_t bd = tc::make_desc(b0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
+                tc::mma_bf16(tmem, ad, bd, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+            }
+            tc::mma_commit(tc::smem_addr(&mbar[s]));
+        }
+    }
+    if (ok && nchunks > 0) {
+        const int cl = nchunks - 1;
+        const bool w = tc::mbar_wait(tc::smem_addr(&mbar[cl & 1]), (cl >> 1) & 1);
+        ok = __syncthreads_and(w) != 0;
+    }
+    tc::fence_after_sync();
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(g.err, 16u);
+    } else {
+        // epilogue: warp w owns TMEM lanes (rows) 32w..32w+31
+        const int row = m0 + warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int cb = 0; cb < kBN; cb += 32) {
+            float v[32];
+            tc::tmem_ld32(lane_addr + cb, v);
+            const int col0 = n0 + cb;
+            if (g.epi == EPI_F32) {
+                float* out = g.C32 + (size_t)row * g.ldc + col0;
+#pragma unroll
+                for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            } else if (g.epi == EPI_FWD) {
+                bf16* zo = g.Zout + (size_t)row * g.ldc + col0;
+                bf16* ho = g.Hout + (size_t)row * g.ldc + col0;
+#pragma unroll
+                for (int i = 0; i < 32; i += 2) {
+                    const float z0 = v[i] + __ldg(g.bias + col0 + i), z1 = v[i + 1] + __ldg(g.bias + col0 + i + 1);
+                    const __nv_bfloat162 zb = __floats2bfloat162_rn(z0, z1);
+                    *reinterpret_cast<__nv_bfloat162*>(zo + i) = zb;
+                    const float2 zf = __bfloat1622float2(zb);   // GELU of the stored (rounded) pre-activation
+                    *reinterpret_cast<__nv_bfloat162*>(ho + i) = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
+                }
+            } else {
+                const bf16* zi = g.Zin + (size_t)row * g.ldc + col0;
+                bf16* dz = g.dZ + (size_t)row * g.ldc + col0;
+#pragma unroll
+                for (int i = 0; i < 32; i += 2) {
+                    const float2 z = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(zi + i));
+                    *reinterpret_cast<__nv_bfloat162*>(dz + i) =
+                        __floats2bfloat162_rn(v[i] * gelu_grad(z.x), v[i + 1] * gelu_grad(z.y));
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+}
+
+constexpr size_t kGemmSmem = 2 * (16384 + 32768);
+
+cudaError_t gemm(const GemmArgs& g, cudaStream_t s) {
+    if (g.M % kBM || g.N % kBN || g.K % tc::kKChunk || g.K <= 0) return cudaErrorInvalidValue;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    dim3 grid(g.N / kBN, g.M / kBM);
+    k_gemm<<<grid, 128, kGemmSmem, s>>>(g);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- features
+struct FeatParams {
+    float inv_w, inv_h;
+    float freq[64];
+};
+
+__device__ __forceinline__ void ray_features(const FeatParams& fp, float x, float y, float th, bf16* out) {
+    float s, c;
+    sincosf(th, &s, &c);
+    const float u[4] = {x * fp.inv_w, y * fp.inv_h, c, s};
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        for (int k = 0; k < 64; k += 2) {
+            float s0, c0, s1, c1;
+            sincospif(fp.freq[k] * u[d], &s0, &c0);
+            sincospif(fp.freq[k + 1] * u[d], &s1, &c1);
+            __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(out + d * 128 + k * 2);
+            o[0] = __floats2bfloat162_rn(s0, c0);
+            o[1] = __floats2bfloat162_rn(s1, c1);
+        }
+    }
+}
+
+// rays given as grid-frame (x, y, theta) triples
+__global__ void k_features(FeatParams fp, const float* __restrict__ xyt, int n, int n_pad, bf16* __restrict__ X) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_pad) return;
+    bf16* out = X + (size_t)r * kFeat;
+    if (r >= n) {
+        for (int j = 0; j < kFeat; j += 8) *reinterpret_cast<uint4*>(out + j) = make_uint4(0, 0, 0, 0);
+        return;
+    }
+    ray_features(fp, xyt[3 * (size_t)r], xyt[3 * (size_t)r + 1], xyt[3 * (size_t)r + 2], out);
+}
+
+// output layer: y = H . w + b (fp32)
+__global__ void k_out_layer(const bf16* __restrict__ H, const float* __restrict__ params, int n, float* __restrict__ y) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const bf16* h = H + (size_t)warp * kHidden;
+    const float* w = params + kOutW;
+    float acc = 0.0f;
+    for (int j = lane; j < kHidden; j += 32) acc += __bfloat162float(h[j]) * w[j];
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[warp] = acc + w[kHidden];
+}
+
+// --------------------------------------------------------------- training
+// Huber loss (delta 1 px) against the target, mean over the batch; dy per ray.
+__global__ void k_loss(const float* __restrict__ y, const float* __restrict__ t, int n, float* __restrict__ dy,
+                       float* __restrict__ loss_sum) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (r < n) {
+        const float e = y[r] - t[r];
+        const float ae = fabsf(e);
+        l = ae <= 1.0f ? 0.5f * e * e : ae - 0.5f;
+        dy[r] = (ae <= 1.0f ? e : copysignf(1.0f, e)) / (float)n;
+    }
+    for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0 && l != 0.0f) atomicAdd(loss_sum, l);
+}
+
+// dZ of the last hidden layer = dy * w_out * GELU'(Z)
+__global__ void k_out_backward(const float* __restrict__ dy, const bf16* __restrict__ Z,
+                               const float* __restrict__ params, int n, bf16* __restrict__ dZ) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const float g = dy[warp];
+    const float* w = params + kOutW;
+    for (int j = lane; j < kHidden; j += 32) {
+        const size_t idx = (size_t)warp * kHidden + j;
+        dZ[idx] = __float2bfloat16_rn(g * w[j] * gelu_grad(__bfloat162float(Z[idx])));
+    }
+}
+
+// output-layer gradients: d w_out[j] = sum_r dy[r] H[r][j], d b_out = sum_r dy[r]
+__global__ void k_out_wgrad(const float* __restrict__ dy, const bf16* __restrict__ H, int n, float* __restrict__ grads) {
+    const int col = threadIdx.x;   // 256 threads
+    float acc = 0.0f, accb = 0.0f;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        const float g = dy[r];
+        acc += g * __bfloat162float(H[(size_t)r * kHidden + col]);
+        accb += g;
+    }
+    atomicAdd(grads + kOutW + col, acc);
+    if (col == 0) atomicAdd(grads + kOutW + kHidden, accb);
+}
+
+// column sums of dZ [n x 256] -> bias gradient
+__global__ void k_bias_grad(const bf16* __restrict__ dZ, int n, float* __restrict__ gb) {
+    const int col = threadIdx.x;   // 256 threads
+    float acc = 0.0f;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) acc += __bfloat162float(dZ[(size_t)r * kHidden + col]);
+    atomicAdd(gb + col, acc);
+}
+
+// transpose-free add of a weight gradient tile computed as fp32 [out x in]
+__global__ void k_add(const float* __restrict__ src, float* __restrict__ dst, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] += src[i];
+}
+
+// Adam (bias-corrected), fp32 master weights; refreshes the bf16 copies
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ g, size_t n, float lr, float b1, float b2, float eps, float c1,
+                       float c2, bf16* __restrict__ wbf) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    p[i] = pi;
+    wbf[i] = __float2bfloat16_rn(pi);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ src, bf16* __restrict__ dst, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = __float2bfloat16_rn(src[i]);
+}
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ float u01(uint32_t a, uint32_t b) {
+    return (hash32(a * 0x9e3779b9u ^ hash32(b)) >> 8) * (1.0f / 16777216.0f);
+}
+
+// uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases, output bias = init_bias
+__global__ void k_init_params(float* __restrict__ p, uint32_t seed, float init_bias) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParamCount) return;
+    float val = 0.0f;
+    for (int l = 0; l < kLayers; ++l) {
+        size_t w0 = w_offset(l), nw = (size_t)kHidden * layer_in(l);
+        if (i >= w0 && i < w0 + nw) val = (2.0f * u01(seed, (uint32_t)i) - 1.0f) * rsqrtf((float)layer_in(l)) * 1.7f;
+    }
+    if (i >= kOutW && i < kOutW + kHidden) val = (2.0f * u01(seed, (uint32_t)i) - 1.0f) * rsqrtf((float)kHidden);
+    if (i == kOutW + kHidden) val = init_bias;
+    p[i] = val;
+}
+
+// ---------------------------------------------------- rays from the marcher
+// The exact march (RangeLib.h:927-962) also reporting t at the hit step;
+// t = max_range when the ray leaves the map or runs out of range.
+__device__ float march_t(const MapDev& m, float mr, float x0, float y0, float c, float s, float* range) {
+    float t = 0.0f;
+    while (t < mr) {
+        int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
+        int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
+        if ((unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H) break;
+        float d = __ldg(m.dt + (size_t)px * m.H + py);
+        if (d <= 0.0f) {
+            float xd = __fsub_rn(__int2float_rn(px), x0), yd = __fsub_rn(__int2float_rn(py), y0);
+            *range = __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+            return t;
+        }
+        t = __fadd_rn(t, fmaxf(__fmul_rn(d, 0.999f), 1.0f));
+    }
+    *range = mr;
+    return mr;
+}
+
+// random free-cell poses, uniform heading; xyt (grid frame), t target, exact range
+__global__ void k_sample_rays(MapDev m, float mr, const uint32_t* __restrict__ free_cells, uint32_t n_free,
+                              uint32_t seed, long long base, int n, float* __restrict__ xyt, float* __restrict__ t,
+                              float* __restrict__ range) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const uint32_t id = (uint32_t)(base + r);
+    const uint32_t cell = free_cells[hash32(id ^ hash32(seed)) % n_free];
+    const int cx = (int)(cell / (uint32_t)m.H), cy = (int)(cell - (uint32_t)cx * (uint32_t)m.H);
+    const float x = (float)cx + u01(id, seed ^ 0x1u), y = (float)cy + u01(id, seed ^ 0x2u);
+    const float th = 6.2831853f * u01(id, seed ^ 0x3u);
+    xyt[3 * (size_t)r] = x;
+    xyt[3 * (size_t)r + 1] = y;
+    xyt[3 * (size_t)r + 2] = th;
+    float s, c, rg;
+    sincosf(th, &s, &c);
+    t[r] = march_t(m, mr, x, y, c, s, &rg);
+    if (range) range[r] = rg;
+}
+
+__global__ void k_free_flags(const uint64_t* __restrict__ bits, int W, int H, int TY, uint32_t* __restrict__ f) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)W * H) return;
+    int x = (int)(i / H), y = (int)(i - (long long)x * H);
+    uint64_t w = bits[(size_t)(x >> 3) * TY + (y >> 3)];
+    f[i] = ((w >> (((x & 7) << 3) | (y & 7))) & 1ull) ? 0u : 1u;
+}
+
+__global__ void k_compact_free(const uint32_t* __restrict__ f, const uint32_t* __restrict__ pos, long long n,
+                               uint32_t* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && f[i]) out[pos[i]] = (uint32_t)i;
+}
+
+// ------------------------------------------------------- learned inference
+__device__ __forceinline__ bool occ_cell(const MapDev& m, int x, int y) {
+    if ((unsigned)x >= (unsigned)m.W || (unsigned)y >= (unsigned)m.H) return false;
+    uint64_t w = __ldg(m.bits + (size_t)(x >> 3) * m.tiles_y + (y >> 3));
+    return (w >> (((x & 7) << 3) | (y & 7))) & 1ull;
+}
+
+// prediction -> accept check -> range (the reference's distance to the hit
+// cell's corner); rejected rays are appended to the recast list
+__global__ void k_accept(MapDev m, float mr, const float* __restrict__ xyt, const float* __restrict__ pred, int n,
+                         float scale, float* __restrict__ outs, uint8_t* __restrict__ accepted,
+                         int* __restrict__ recast, int* __restrict__ n_recast) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float x0 = xyt[3 * (size_t)r], y0 = xyt[3 * (size_t)r + 1], th = xyt[3 * (size_t)r + 2];
+    const float t = pred[r];
+    bool ok = false;
+    float rg = 0.0f;
+    if (t > 1.0f && t < 0.999f * mr && isfinite(t)) {
+        float s, c;
+        sincosf(th, &s, &c);
+        const int hx = __float2int_rz(x0 + c * t), hy = __float2int_rz(y0 + s * t);
+        const int bx = __float2int_rz(x0 + c * (t - 1.0f)), by = __float2int_rz(y0 + s * (t - 1.0f));
+        if (occ_cell(m, hx, hy) && !occ_cell(m, bx, by)) {
+            const float xd = __fsub_rn(__int2float_rn(hx), x0), yd = __fsub_rn(__int2float_rn(hy), y0);
+            rg = __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+            ok = true;
+        }
+    }
+    if (accepted) accepted[r] = ok ? 1 : 0;
+    if (ok) {
+        outs[r] = __fmul_rn(rg, scale);
+    } else {
+        int slot = atomicAdd(n_recast, 1);
+        recast[slot] = r;
+    }
+}
+
+__global__ void k_recast(MapDev m, float mr, const float* __restrict__ xyt, const int* __restrict__ list,
+                         const int* __restrict__ count, float scale, float* __restrict__ outs) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *count) return;
+    const int r = list[j];
+    const float x0 = xyt[3 * (size_t)r], y0 = xyt[3 * (size_t)r + 1], th = xyt[3 * (size_t)r + 2];
+    float s, c, rg;
+    sincosf(th, &s, &c);
+    march_t(m, mr, x0, y0, c, s, &rg);
+    outs[r] = __fmul_rn(rg, scale);
+}
+
+// world-frame particles x beams -> grid-frame rays (RangeLib.h:482-520)
+__global__ void k_world_rays(WorldDev w, const float* __restrict__ ins, const float* __restrict__ angles, int n,
+                             int na, float* __restrict__ xyt) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)n * na) return;
+    int i = (int)(g / na), a = (int)(g - (long long)i * na);
+    float x = __fmul_rn(__fsub_rn(ins[3 * (size_t)i], w.ox), w.inv_s);
+    float y = __fmul_rn(__fsub_rn(ins[3 * (size_t)i + 1], w.oy), w.inv_s);
+    float tmp = x;
+    x = __fsub_rn(__fmul_rn(w.ca, x), __fmul_rn(w.sa, y));
+    y = __fadd_rn(__fmul_rn(w.sa, tmp), __fmul_rn(w.ca, y));
+    const float th = __fsub_rn(__fadd_rn(-ins[3 * (size_t)i + 2], w.rc), angles[a]);
+    xyt[3 * g] = y;   // calc_range(y, x, theta)
+    xyt[3 * g + 1] = x;
+    xyt[3 * g + 2] = th;
+}
+
+inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+#define TRY(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) return _e; } while (0)
+
+}  // namespace
+
+// ================================================================ host side
+struct LearnedModel {
+    MapDev map{};
+    WorldDev world{};
+    float mr = 0.0f;
+    FeatParams fp{};
+    float* params = nullptr;   // fp32 master [kParamCount]
+    float* adam_m = nullptr;
+    float* adam_v = nullptr;
+    float* grads = nullptr;
+    bf16* wbf = nullptr;       // bf16 copy of params (weights used by the GEMMs)
+    unsigned* err = nullptr;
+    long long adam_t = 0;
+    // work buffers for a chunk of `cap` rays
+    int cap = 0;
+    bf16* X = nullptr;                 // [cap x 512]
+    bf16* Z[kLayers] = {};             // pre-activations [cap x 256]
+    bf16* Hh[kLayers] = {};            // activations
+    bf16* dZ[2] = {};                  // ping-pong gradients
+    float* y = nullptr;
+    float* dy = nullptr;
+    float* gtmp = nullptr;             // fp32 [256 x 512] weight gradient tile
+    float* loss = nullptr;
+    uint32_t* free_cells = nullptr;
+    uint32_t n_free = 0;
+
+    void free_work() {
+        cudaFree(X);
+        for (int l = 0; l < kLayers; ++l) { cudaFree(Z[l]); cudaFree(Hh[l]); Z[l] = Hh[l] = nullptr; }
+        cudaFree(dZ[0]); cudaFree(dZ[1]);
+        cudaFree(y); cudaFree(dy); cudaFree(gtmp); cudaFree(loss);
+        X = nullptr; dZ[0] = dZ[1] = nullptr; y = dy = gtmp = loss = nullptr;
+        cap = 0;
+    }
+    ~LearnedModel() {
+        free_work();
+        cudaFree(params); cudaFree(adam_m); cudaFree(adam_v); cudaFree(grads); cudaFree(wbf); cudaFree(err);
+        cudaFree(free_cells);
+    }
+    cudaError_t ensure(int rows) {
+        rows = (rows + kBM - 1) / kBM * kBM;
+        if (rows <= cap) return cudaSuccess;
+        free_work();
+        TRY(cudaMalloc(&X, (size_t)rows * kFeat * sizeof(bf16)));
+        for (int l = 0; l < kLayers; ++l) {
+            TRY(cudaMalloc(&Z[l], (size_t)rows * kHidden * sizeof(bf16)));
+            TRY(cudaMalloc(&Hh[l], (size_t)rows * kHidden * sizeof(bf16)));
+        }
+        TRY(cudaMalloc(&dZ[0], (size_t)rows * kHidden * sizeof(bf16)));
+        TRY(cudaMalloc(&dZ[1], (size_t)rows * kHidden * sizeof(bf16)));
+        TRY(cudaMalloc(&y, (size_t)rows * sizeof(float)));
+        TRY(cudaMalloc(&dy, (size_t)rows * sizeof(float)));
+        TRY(cudaMalloc(&gtmp, kW0 * sizeof(float)));
+        TRY(cudaMalloc(&loss, sizeof(float)));
+        cap = rows;
+        return cudaSuccess;
+    }
+
+    GemmArgs base_args() const {
+        GemmArgs g{};
+        g.err = err;
+        return g;
+    }
+
+    // forward over `rows` rays whose features are in X; predictions in y
+    cudaError_t forward(int rows, cudaStream_t s) {
+        const bf16* in = X;
+        for (int l = 0; l < kLayers; ++l) {
+            GemmArgs g = base_args();
+            g.A = in; g.lda = layer_in(l); g.a_t = 0;
+            g.B = wbf + w_offset(l); g.ldb = layer_in(l); g.b_t = 0;   // W [out x in]: N x K, K-major
+            g.M = rows; g.N = kHidden; g.K = layer_in(l);
+            g.epi = EPI_FWD; g.ldc = kHidden;
+            g.bias = params + b_offset(l);
+            g.Zout = Z[l]; g.Hout = Hh[l];
+            TRY(gemm(g, s));
+            in = Hh[l];
+        }
+        k_out_layer<<<blocks_for((long long)rows * 32, 256), 256, 0, s>>>(Hh[kLayers - 1], params, rows, y);
+        return cudaGetLastError();
+    }
+
+    // backward from dy (rows rays, features in X, forward state in Z/Hh); gradients into grads
+    cudaError_t backward(int rows, cudaStream_t s) {
+        TRY(cudaMemsetAsync(grads, 0, kParamCount * sizeof(float), s));
+        k_out_backward<<<blocks_for((long long)rows * 32, 256), 256, 0, s>>>(dy, Z[kLayers - 1], params, rows, dZ[0]);
+        TRY(cudaGetLastError());
+        k_out_wgrad<<<256, 256, 0, s>>>(dy, Hh[kLayers - 1], rows, grads);
+        TRY(cudaGetLastError());
+        int cur = 0;
+        for (int l = kLayers - 1; l >= 0; --l) {
+            // weight gradient: dW [out x in] = dZ^T . input  (K = rows)
+            const bf16* input = l == 0 ? X : Hh[l - 1];
+            GemmArgs gw = base_args();
+            gw.A = dZ[cur]; gw.lda = kHidden; gw.a_t = 1;           // A[m=out][k=row] = dZ[row][out]
+            gw.B = input; gw.ldb = layer_in(l); gw.b_t = 1;         // B[n=in][k=row] = input[row][in]
+            gw.M = kHidden; gw.N = layer_in(l); gw.K = rows;
+            gw.epi = EPI_F32; gw.ldc = layer_in(l); gw.C32 = gtmp;
+            TRY(gemm(gw, s));
+            const size_t nw = (size_t)kHidden * layer_in(l);
+            k_add<<<blocks_for((long long)nw, 256), 256, 0, s>>>(gtmp, grads + w_offset(l), nw);
+            TRY(cudaGetLastError());
+            k_bias_grad<<<256, 256, 0, s>>>(dZ[cur], rows, grads + b_offset(l));
+            TRY(cudaGetLastError());
+            if (l == 0) break;
+            // input gradient: dH = dZ . W, then times GELU'(Z[l-1])
+            GemmArgs gx = base_args();
+            gx.A = dZ[cur]; gx.lda = kHidden; gx.a_t = 0;           // A[m=row][k=out]
+            gx.B = wbf + w_offset(l); gx.ldb = layer_in(l); gx.b_t = 1;   // B[n=in][k=out] = W[out][in]
+            gx.M = rows; gx.N = layer_in(l); gx.K = kHidden;
+            gx.epi = EPI_BWD; gx.ldc = kHidden;
+            gx.Zin = Z[l - 1]; gx.dZ = dZ[cur ^ 1];
+            TRY(gemm(gx, s));
+            cur ^= 1;
+        }
+        return cudaSuccess;
+    }
+
+    cudaError_t features(const float* xyt, int n, cudaStream_t s) {
+        const int rows = (n + kBM - 1) / kBM * kBM;
+        k_features<<<blocks_for(rows, 128), 128, 0, s>>>(fp, xyt, n, rows, X);
+        return cudaGetLastError();
+    }
+
+    cudaError_t adam_step(float lr, cudaStream_t s) {
+        ++adam_t;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.0f / (1.0f - powf(b1, (float)adam_t)), c2 = 1.0f / (1.0f - powf(b2, (float)adam_t));
+        k_adam<<<blocks_for((long long)kParamCount, 256), 256, 0, s>>>(params, adam_m, adam_v, grads, kParamCount, lr,
+                                                                      b1, b2, 1e-8f, c1, c2, wbf);
+        return cudaGetLastError();
+    }
+};
+
+}  // namespace rlc
+
+// ======================================================================= ABI
+using namespace rlc;
+
+struct rlc_learned {
+    LearnedModel m;
+};
+
+namespace {
+char g_msg[512];
+int lfail(int code, const char* what, cudaError_t e = cudaSuccess) {
+    if (e != cudaSuccess) snprintf(g_msg, sizeof(g_msg), "%s: %s", what, cudaGetErrorString(e));
+    else snprintf(g_msg, sizeof(g_msg), "%s", what);
+    return set_last_error(code, g_msg);
+}
+#define LTRY(expr, what) do { cudaError_t _e = (expr); if (_e != cudaSuccess) return lfail(RLC_ERR_CUDA, what, _e); } while (0)
+}  // namespace
+
+extern "C" {
+
+int rlc_learned_create(const rlc_method* rm, unsigned seed, rlc_learned** out) {
+    if (!out) return lfail(RLC_ERR_ARG, "null output handle");
+    *out = nullptr;
+    MapDev map;
+    WorldDev world;
+    float mr;
+    if (int rc = method_map_view(rm, &map, &world, &mr)) return rc;
+    rlc_learned* L = new rlc_learned();
+    LearnedModel& M = L->m;
+    M.map = map;
+    M.world = world;
+    M.mr = mr;
+    M.fp.inv_w = 1.0f / (float)map.W;
+    M.fp.inv_h = 1.0f / (float)map.H;
+    const double fmax = std::max(2.0, 0.5 * std::max(map.W, map.H));
+    for (int k = 0; k < 64; ++k) M.fp.freq[k] = (float)std::pow(fmax, k / 63.0);
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMalloc(&M.params, kParamCount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.adam_m, kParamCount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.adam_v, kParamCount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.grads, kParamCount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.wbf, kParamCount * sizeof(bf16));
+    if (e == cudaSuccess) e = cudaMalloc(&M.err, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(M.err, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(M.adam_m, 0, kParamCount * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(M.adam_v, 0, kParamCount * sizeof(float));
+    if (e == cudaSuccess) {
+        k_init_params<<<blocks_for((long long)kParamCount, 256), 256>>>(M.params, seed, 0.25f * mr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_to_bf16<<<blocks_for((long long)kParamCount, 256), 256>>>(M.params, M.wbf, kParamCount);
+        e = cudaGetLastError();
+    }
+    // free cells of the map, for sampling training rays
+    if (e == cudaSuccess) {
+        const long long n = (long long)map.W * map.H;
+        uint32_t *f = nullptr, *pos = nullptr;
+        e = cudaMalloc(&f, (n + 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&pos, (n + 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) {
+            k_free_flags<<<blocks_for(n, 256), 256>>>(map.bits, map.W, map.H, map.tiles_y, f);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = scan_exclusive_u32(f, pos, (size_t)n, 0);
+        if (e == cudaSuccess) e = cudaMemcpy(&M.n_free, pos + n, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMalloc(&M.free_cells, (size_t)(M.n_free ? M.n_free : 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) {
+            k_compact_free<<<blocks_for(n, 256), 256>>>(f, pos, n, M.free_cells);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        cudaFree(f);
+        cudaFree(pos);
+    }
+    if (e != cudaSuccess) {
+        delete L;
+        return lfail(RLC_ERR_CUDA, "learned model setup", e);
+    }
+    if (M.n_free == 0) {
+        delete L;
+        return lfail(RLC_ERR_ARG, "the map has no free cell to sample rays from");
+    }
+    *out = L;
+    return RLC_OK;
+}
+
+int rlc_learned_destroy(rlc_learned* L) {
+    delete L;
+    return RLC_OK;
+}
+
+int64_t rlc_learned_param_count(void) { return (int64_t)kParamCount; }
+
+int rlc_learned_get_params(rlc_learned* L, float* host_params) {
+    if (!L || !host_params) return lfail(RLC_ERR_ARG, "null argument");
+    LTRY(cudaMemcpy(host_params, L->m.params, kParamCount * sizeof(float), cudaMemcpyDeviceToHost), "get params");
+    return RLC_OK;
+}
+
+int rlc_learned_set_params(rlc_learned* L, const float* host_params) {
+    if (!L || !host_params) return lfail(RLC_ERR_ARG, "null argument");
+    LTRY(cudaMemcpy(L->m.params, host_params, kParamCount * sizeof(float), cudaMemcpyHostToDevice), "set params");
+    k_to_bf16<<<blocks_for((long long)kParamCount, 256), 256>>>(L->m.params, L->m.wbf, kParamCount);
+    LTRY(cudaGetLastError(), "set params");
+    LTRY(cudaMemset(L->m.adam_m, 0, kParamCount * sizeof(float)), "set params");
+    LTRY(cudaMemset(L->m.adam_v, 0, kParamCount * sizeof(float)), "set params");
+    L->m.adam_t = 0;
+    return RLC_OK;
+}
+
+// Sample rays from the map's free cells with the exact marcher (device buffers, n rays).
+int rlc_learned_sample_rays(rlc_learned* L, long long first_id, unsigned seed, int n, float* d_xyt, float* d_t,
+                            float* d_range, void* stream) {
+    if (!L || n < 0 || (n > 0 && (!d_xyt || !d_t))) return lfail(RLC_ERR_ARG, "bad argument");
+    if (n == 0) return RLC_OK;
+    LearnedModel& M = L->m;
+    k_sample_rays<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(M.map, M.mr, M.free_cells, M.n_free, seed,
+                                                                        first_id, n, d_xyt, d_t, d_range);
+    LTRY(cudaGetLastError(), "sample rays");
+    return RLC_OK;
+}
+
+// Forward only: predicted t for n grid-frame rays (device buffers).
+int rlc_learned_predict(rlc_learned* L, const float* d_xyt, int n, float* d_pred, void* stream) {
+    if (!L || n < 0 || (n > 0 && (!d_xyt || !d_pred))) return lfail(RLC_ERR_ARG, "bad argument");
+    LearnedModel& M = L->m;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int chunk = 65536;
+    LTRY(M.ensure(std::min(n, chunk)), "predict buffers");
+    for (int off = 0; off < n; off += chunk) {
+        const int cnt = std::min(chunk, n - off);
+        const int rows = (cnt + kBM - 1) / kBM * kBM;
+        LTRY(M.features(d_xyt + 3 * (size_t)off, cnt, s), "features");
+        LTRY(M.forward(rows, s), "forward");
+        LTRY(cudaMemcpyAsync(d_pred + off, M.y, cnt * sizeof(float), cudaMemcpyDeviceToDevice, s), "predict");
+    }
+    return RLC_OK;
+}
+
+// Test hook: the bf16 features of n grid-frame rays into d_out [n x 512] (device).
+int rlc_learned_features(rlc_learned* L, const float* d_xyt, int n, void* d_out) {
+    if (!L || n <= 0 || !d_xyt || !d_out) return lfail(RLC_ERR_ARG, "bad argument");
+    k_features<<<blocks_for(n, 128), 128>>>(L->m.fp, d_xyt, n, n, (bf16*)d_out);
+    LTRY(cudaGetLastError(), "features");
+    LTRY(cudaDeviceSynchronize(), "features");
+    return RLC_OK;
+}
+
+// One forward + backward over n rays (device buffers) without an update:
+// host_grads receives the parameter gradients of the mean Huber loss.
+int rlc_learned_gradients(rlc_learned* L, const float* d_xyt, const float* d_t, int n, float* host_grads,
+                          float* host_loss) {
+    if (!L || n <= 0 || !d_xyt || !d_t) return lfail(RLC_ERR_ARG, "bad argument");
+    if (n % kBM) return lfail(RLC_ERR_ARG, "gradients take a multiple of 128 rays");
+    LearnedModel& M = L->m;
+    LTRY(M.ensure(n), "gradient buffers");
+    LTRY(M.features(d_xyt, n, 0), "features");
+    LTRY(M.forward(n, 0), "forward");
+    LTRY(cudaMemset(M.loss, 0, sizeof(float)), "loss");
+    k_loss<<<blocks_for(n, 256), 256>>>(M.y, d_t, n, M.dy, M.loss);
+    LTRY(cudaGetLastError(), "loss");
+    LTRY(M.backward(n, 0), "backward");
+    LTRY(cudaDeviceSynchronize(), "gradients");
+    unsigned err = 0;
+    LTRY(cudaMemcpy(&err, M.err, sizeof(unsigned), cudaMemcpyDeviceToHost), "gradients");
+    if (err) return lfail(RLC_ERR_CUDA, "tensor-core GEMM timed out waiting for its MMAs");
+    if (host_grads) LTRY(cudaMemcpy(host_grads, M.grads, kParamCount * sizeof(float), cudaMemcpyDeviceToHost), "grads");
+    if (host_loss) {
+        float l = 0.0f;
+        LTRY(cudaMemcpy(&l, M.loss, sizeof(float), cudaMemcpyDeviceToHost), "loss");
+        *host_loss = l / (float)n;
+    }
+    return RLC_OK;
+}
+
+// Train on rays drawn by the exact marcher: `steps` Adam steps of `batch` rays
+// (a multiple of 128), cosine-decayed learning rate from lr.  *final_loss gets
+// the mean loss of the last 20 steps.
+int rlc_learned_train(rlc_learned* L, int steps, int batch, float lr, unsigned seed, float* final_loss,
+                      void* stream) {
+    if (!L || steps < 0 || batch <= 0 || batch % kBM) return lfail(RLC_ERR_ARG, "batch must be a positive multiple of 128");
+    LearnedModel& M = L->m;
+    cudaStream_t s = (cudaStream_t)stream;
+    LTRY(M.ensure(batch), "train buffers");
+    float *xyt = nullptr, *tt = nullptr;
+    LTRY(cudaMalloc(&xyt, (size_t)batch * 3 * sizeof(float)), "train buffers");
+    cudaError_t e = cudaMalloc(&tt, (size_t)batch * sizeof(float));
+    float loss_acc = 0.0f;
+    int loss_n = 0;
+    for (int st = 0; st < steps && e == cudaSuccess; ++st) {
+        k_sample_rays<<<blocks_for(batch, 256), 256, 0, s>>>(M.map, M.mr, M.free_cells, M.n_free, seed,
+                                                             (long long)st * batch, batch, xyt, tt, nullptr);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = M.features(xyt, batch, s);
+        if (e == cudaSuccess) e = M.forward(batch, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(M.loss, 0, sizeof(float), s);
+        if (e == cudaSuccess) {
+            k_loss<<<blocks_for(batch, 256), 256, 0, s>>>(M.y, tt, batch, M.dy, M.loss);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = M.backward(batch, s);
+        const float cosine = 0.5f * (1.0f + cosf(3.14159265f * (float)st / (float)(steps > 1 ? steps : 1)));
+        if (e == cudaSuccess) e = M.adam_step(lr * (0.05f + 0.95f * cosine), s);
+        if (e == cudaSuccess && st >= steps - 20) {
+            float l = 0.0f;
+            e = cudaMemcpyAsync(&l, M.loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            loss_acc += l / (float)batch;
+            ++loss_n;
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(xyt);
+    cudaFree(tt);
+    if (e != cudaSuccess) return lfail(RLC_ERR_CUDA, "training", e);
+    unsigned err = 0;
+    LTRY(cudaMemcpy(&err, M.err, sizeof(unsigned), cudaMemcpyDeviceToHost), "training");
+    if (err) return lfail(RLC_ERR_CUDA, "tensor-core GEMM timed out waiting for its MMAs");
+    if (final_loss) *final_loss = loss_n ? loss_acc / loss_n : 0.0f;
+    return RLC_OK;
+}
+
+// Learned calc_range_repeat_angles (world frame, device buffers): predicted
+// hit cells that pass the check give the reference's corner distance, the
+// rest are recast exactly.  accepted (optional) marks accepted rays; *n_recast
+// gets the number of recast rays.
+int rlc_learned_calc_range_repeat_angles(rlc_learned* L, const float* d_ins, const float* d_angles, float* d_outs,
+                                         int n, int na, uint8_t* d_accepted, int64_t* n_recast, void* stream) {
+    if (!L || n < 0 || na < 0) return lfail(RLC_ERR_ARG, "bad argument");
+    const long long rays = (long long)n * na;
+    if (rays == 0) return RLC_OK;
+    if (!d_ins || !d_angles || !d_outs) return lfail(RLC_ERR_ARG, "null array");
+    if (rays > (1ll << 31) - 1) return lfail(RLC_ERR_ARG, "too many rays");
+    LearnedModel& M = L->m;
+    cudaStream_t s = (cudaStream_t)stream;
+    float *xyt = nullptr, *pred = nullptr;
+    int *list = nullptr, *cnt = nullptr;
+    cudaError_t e = cudaMalloc(&xyt, (size_t)rays * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&pred, (size_t)rays * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&list, (size_t)rays * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&cnt, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(int), s);
+    if (e == cudaSuccess) {
+        k_world_rays<<<blocks_for(rays, 256), 256, 0, s>>>(M.world, d_ins, d_angles, n, na, xyt);
+        e = cudaGetLastError();
+    }
+    int rc = RLC_OK;
+    if (e == cudaSuccess) rc = rlc_learned_predict(L, xyt, (int)rays, pred, stream);
+    if (e == cudaSuccess && !rc) {
+        k_accept<<<blocks_for(rays, 256), 256, 0, s>>>(M.map, M.mr, xyt, pred, (int)rays, M.world.s, d_outs,
+                                                       d_accepted, list, cnt);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && !rc) {
+        k_recast<<<blocks_for(rays, 256), 256, 0, s>>>(M.map, M.mr, xyt, list, cnt, M.world.s, d_outs);
+        e = cudaGetLastError();
+    }
+    int h_cnt = 0;
+    if (e == cudaSuccess && !rc) e = cudaMemcpyAsync(&h_cnt, cnt, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && !rc) e = cudaStreamSynchronize(s);
+    cudaFree(xyt);
+    cudaFree(pred);
+    cudaFree(list);
+    cudaFree(cnt);
+    if (rc) return rc;
+    if (e != cudaSuccess) return lfail(RLC_ERR_CUDA, "learned ranges", e);
+    if (n_recast) *n_recast = h_cnt;
+    return RLC_OK;
+}
+
+// Test hook: C[M x N] (fp32, row-major) = A . B^T on the tensor cores, with A
+// [M x K] (or K x M when a_t) and B [N x K] (or K x N when b_t), bf16, device.
+int rlc_tc_gemm(const void* d_a, const void* d_b, float* d_c, int M, int N, int K, int a_t, int b_t, void* stream) {
+    if (!d_a || !d_b || !d_c) return lfail(RLC_ERR_ARG, "null pointer");
+    if (M <= 0 || N <= 0 || K <= 0 || M % kBM || N % kBN || K % tc::kKChunk)
+        return lfail(RLC_ERR_ARG, "M must be a multiple of 128, N of 256, K of 64");
+    unsigned* err = nullptr;
+    LTRY(cudaMalloc(&err, sizeof(unsigned)), "gemm");
+    cudaError_t e = cudaMemset(err, 0, sizeof(unsigned));
+    GemmArgs g{};
+    g.A = (const bf16*)d_a; g.lda = a_t ? M : K; g.a_t = a_t;
+    g.B = (const bf16*)d_b; g.ldb = b_t ? N : K; g.b_t = b_t;
+    g.M = M; g.N = N; g.K = K;
+    g.epi = EPI_F32; g.ldc = N; g.C32 = d_c; g.err = err;
+    if (e == cudaSuccess) e = gemm(g, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    unsigned h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(err);
+    if (e != cudaSuccess) return lfail(RLC_ERR_CUDA, "tensor-core gemm", e);
+    if (h) return lfail(RLC_ERR_CUDA, "tensor-core GEMM timed out waiting for its MMAs");
+    return RLC_OK;
+}
+
+}  // extern "C"

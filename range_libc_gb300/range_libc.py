@@ -570,6 +570,93 @@ class PyFilterBatch:
             self._h = None
 
 
+class PyLearnedRM:
+    """Learned range surrogate of a ray-marching method's map (no reference counterpart).
+
+    A Fourier-feature MLP (512 features, 4 x 256 GELU, BF16 weights, FP32 accumulation) is
+    trained on the GPU, on rays the exact marcher casts, to predict the march parameter of a
+    ray's hit cell.  calc_range_repeat_angles accepts a prediction whose cell is occupied and
+    whose previous cell (one pixel back) is free, returns the reference's distance to that
+    cell's corner, and recasts every other ray exactly.  Arrays are CUDA tensors.
+    """
+
+    def __init__(self, method, seed: int = 0):
+        import torch  # noqa: F401
+        h = C.c_void_p()
+        call("rlc_learned_create", method.handle, int(seed), C.byref(h))
+        self._h = h
+        self.method = method
+        self.n_params = int(lib().rlc_learned_param_count())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.rlc_learned_destroy(h)
+            self._h = None
+
+    def train(self, steps: int, batch: int = 8192, lr: float = 1e-3, seed: int = 1) -> float:
+        loss = C.c_float()
+        call("rlc_learned_train", self._h, int(steps), int(batch), float(lr), int(seed), C.byref(loss), None)
+        return loss.value
+
+    def sample_rays(self, n: int, first_id: int = 0, seed: int = 7):
+        """(xyt [n, 3] grid-frame rays, t [n] hit parameter, range [n] exact range) from the exact marcher."""
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        xyt = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        t = torch.empty(n, dtype=torch.float32, device=dev)
+        r = torch.empty(n, dtype=torch.float32, device=dev)
+        call("rlc_learned_sample_rays", self._h, int(first_id), int(seed), int(n), xyt.data_ptr(), t.data_ptr(),
+             r.data_ptr(), _stream_of(xyt))
+        return xyt, t, r
+
+    def predict(self, xyt):
+        import torch
+        out = torch.empty(xyt.shape[0], dtype=torch.float32, device=xyt.device)
+        call("rlc_learned_predict", self._h, xyt.data_ptr(), int(xyt.shape[0]), out.data_ptr(), _stream_of(xyt))
+        return out
+
+    def features(self, xyt):
+        import torch
+        out = torch.empty((xyt.shape[0], 512), dtype=torch.bfloat16, device=xyt.device)
+        call("rlc_learned_features", self._h, xyt.data_ptr(), int(xyt.shape[0]), out.data_ptr())
+        return out
+
+    def gradients(self, xyt, t):
+        g = np.empty(self.n_params, np.float32)
+        loss = C.c_float()
+        call("rlc_learned_gradients", self._h, xyt.data_ptr(), t.data_ptr(), int(xyt.shape[0]),
+             g.ctypes.data_as(_lib._f32p), C.byref(loss))
+        return g, loss.value
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.n_params, np.float32)
+        call("rlc_learned_get_params", self._h, p.ctypes.data_as(_lib._f32p))
+        return p
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        call("rlc_learned_set_params", self._h, p.ctypes.data_as(_lib._f32p))
+
+    def calc_range_repeat_angles(self, ins, angles, outs, accepted=None) -> int:
+        """World-frame particles x beams (like PyRayMarching.calc_range_repeat_angles); returns
+        the number of rays recast exactly."""
+        nrec = C.c_int64()
+        call("rlc_learned_calc_range_repeat_angles", self._h, ins.data_ptr(), angles.data_ptr(), outs.data_ptr(),
+             int(ins.shape[0]), int(angles.shape[0]), None if accepted is None else accepted.data_ptr(),
+             C.byref(nrec), _stream_of(ins))
+        return nrec.value
+
+
+def tc_gemm(a, b, M, N, K, a_t=False, b_t=False):
+    """C = A . B^T on the tensor cores (bf16 CUDA tensors in, fp32 out); test hook."""
+    import torch
+    c = torch.empty((M, N), dtype=torch.float32, device=a.device)
+    call("rlc_tc_gemm", a.data_ptr(), b.data_ptr(), c.data_ptr(), int(M), int(N), int(K), int(a_t), int(b_t),
+         _stream_of(a))
+    return c
+
+
 def device_count() -> int:
     return lib().rlc_device_count()
 
