@@ -47,16 +47,17 @@ __host__ __device__ inline int layer_in(int l) { return l == 0 ? kFeat : kHidden
 constexpr size_t kOutW = kW0 + kHidden + 3 * (kWh + kHidden);  // output weights [256], then bias [1]
 
 // -------------------------------------------------------------------- GEMM
-enum Epi : int { EPI_F32 = 0, EPI_FWD = 1, EPI_BWD = 2 };
+enum Epi : int { EPI_F32 = 0, EPI_FWD = 1, EPI_BWD = 2, EPI_F32_ADD = 3 };
 
 struct GemmArgs {
     const bf16* A;   // a_t ? A[k * lda + m] : A[m * lda + k]
     const bf16* B;   // b_t ? B[k * ldb + n] : B[n * ldb + k]
     int lda, ldb, a_t, b_t;
     int M, N, K;
+    int ksplit;         // K range of blockIdx.z: [z * ksplit, (z + 1) * ksplit)
     int epi;
     int ldc;
-    float* C32;         // EPI_F32: C[m * ldc + n]
+    float* C32;         // EPI_F32: C[m * ldc + n]; EPI_F32_ADD: C[m * ldc + n] += (split-K partials)
     const float* bias;  // EPI_FWD
     bf16* Zout;         // EPI_FWD: pre-activation
     bf16* Hout;         // EPI_FWD: GELU(z)
@@ -119,7 +120,8 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
     const uint32_t idesc = tc::make_idesc(kBM, kBN);
-    const int nchunks = g.K / tc::kKChunk;
+    const int kbase = blockIdx.z * g.ksplit;
+    const int nchunks = g.ksplit / tc::kKChunk;
     bool ok = true;
     for (int c = 0; c < nchunks && ok; ++c) {
         const int s = c & 1;
@@ -128,8 +130,8 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
             ok = __syncthreads_and(w) != 0;
             if (!ok) break;
         }
-        load_tile(sA[s], g.A, g.lda, g.a_t, m0, kBM, c * tc::kKChunk);
-        load_tile(sB[s], g.B, g.ldb, g.b_t, n0, kBN, c * tc::kKChunk);
+        load_tile(sA[s], g.A, g.lda, g.a_t, m0, kBM, kbase + c * tc::kKChunk);
+        load_tile(sB[s], g.B, g.ldb, g.b_t, n0, kBN, kbase + c * tc::kKChunk);
         tc::fence_async_smem();
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -164,6 +166,10 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
                 float* out = g.C32 + (size_t)row * g.ldc + col0;
 #pragma unroll
                 for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            } else if (g.epi == EPI_F32_ADD) {
+                float* out = g.C32 + (size_t)row * g.ldc + col0;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) atomicAdd(out + i, v[i]);
             } else if (g.epi == EPI_FWD) {
                 bf16* zo = g.Zout + (size_t)row * g.ldc + col0;
                 bf16* ho = g.Hout + (size_t)row * g.ldc + col0;
@@ -194,15 +200,18 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
 
 constexpr size_t kGemmSmem = 2 * (16384 + 32768);
 
-cudaError_t gemm(const GemmArgs& g, cudaStream_t s) {
+cudaError_t gemm(GemmArgs g, cudaStream_t s) {
     if (g.M % kBM || g.N % kBN || g.K % tc::kKChunk || g.K <= 0) return cudaErrorInvalidValue;
+    if (g.ksplit <= 0) g.ksplit = g.K;
+    if (g.K % g.ksplit || g.ksplit % tc::kKChunk) return cudaErrorInvalidValue;
+    if (g.ksplit != g.K && g.epi != EPI_F32_ADD) return cudaErrorInvalidValue;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    dim3 grid(g.N / kBN, g.M / kBM);
+    dim3 grid(g.N / kBN, g.M / kBM, g.K / g.ksplit);
     k_gemm<<<grid, 128, kGemmSmem, s>>>(g);
     return cudaGetLastError();
 }
@@ -302,12 +311,6 @@ __global__ void k_bias_grad(const bf16* __restrict__ dZ, int n, float* __restric
     float acc = 0.0f;
     for (int r = blockIdx.x; r < n; r += gridDim.x) acc += __bfloat162float(dZ[(size_t)r * kHidden + col]);
     atomicAdd(gb + col, acc);
-}
-
-// transpose-free add of a weight gradient tile computed as fp32 [out x in]
-__global__ void k_add(const float* __restrict__ src, float* __restrict__ dst, size_t n) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] += src[i];
 }
 
 // Adam (bias-corrected), fp32 master weights; refreshes the bf16 copies
@@ -502,23 +505,41 @@ struct LearnedModel {
     bf16* dZ[2] = {};                  // ping-pong gradients
     float* y = nullptr;
     float* dy = nullptr;
-    float* gtmp = nullptr;             // fp32 [256 x 512] weight gradient tile
     float* loss = nullptr;
     uint32_t* free_cells = nullptr;
     uint32_t n_free = 0;
+    // query buffers (rays of one learned call)
+    long long qcap = 0;
+    float* q_xyt = nullptr;
+    float* q_pred = nullptr;
+    int* q_list = nullptr;
+    int* q_cnt = nullptr;
+
+    cudaError_t ensure_query(long long rays) {
+        if (rays <= qcap) return cudaSuccess;
+        cudaFree(q_xyt); cudaFree(q_pred); cudaFree(q_list); cudaFree(q_cnt);
+        q_xyt = q_pred = nullptr; q_list = q_cnt = nullptr; qcap = 0;
+        TRY(cudaMalloc(&q_xyt, (size_t)rays * 3 * sizeof(float)));
+        TRY(cudaMalloc(&q_pred, (size_t)rays * sizeof(float)));
+        TRY(cudaMalloc(&q_list, (size_t)rays * sizeof(int)));
+        TRY(cudaMalloc(&q_cnt, sizeof(int)));
+        qcap = rays;
+        return cudaSuccess;
+    }
 
     void free_work() {
         cudaFree(X);
         for (int l = 0; l < kLayers; ++l) { cudaFree(Z[l]); cudaFree(Hh[l]); Z[l] = Hh[l] = nullptr; }
         cudaFree(dZ[0]); cudaFree(dZ[1]);
-        cudaFree(y); cudaFree(dy); cudaFree(gtmp); cudaFree(loss);
-        X = nullptr; dZ[0] = dZ[1] = nullptr; y = dy = gtmp = loss = nullptr;
+        cudaFree(y); cudaFree(dy); cudaFree(loss);
+        X = nullptr; dZ[0] = dZ[1] = nullptr; y = dy = loss = nullptr;
         cap = 0;
     }
     ~LearnedModel() {
         free_work();
         cudaFree(params); cudaFree(adam_m); cudaFree(adam_v); cudaFree(grads); cudaFree(wbf); cudaFree(err);
         cudaFree(free_cells);
+        cudaFree(q_xyt); cudaFree(q_pred); cudaFree(q_list); cudaFree(q_cnt);
     }
     cudaError_t ensure(int rows) {
         rows = (rows + kBM - 1) / kBM * kBM;
@@ -533,10 +554,17 @@ struct LearnedModel {
         TRY(cudaMalloc(&dZ[1], (size_t)rows * kHidden * sizeof(bf16)));
         TRY(cudaMalloc(&y, (size_t)rows * sizeof(float)));
         TRY(cudaMalloc(&dy, (size_t)rows * sizeof(float)));
-        TRY(cudaMalloc(&gtmp, kW0 * sizeof(float)));
         TRY(cudaMalloc(&loss, sizeof(float)));
         cap = rows;
         return cudaSuccess;
+    }
+
+    // K split of the weight-gradient GEMMs: chunks of >= 256 rows, at most 64 splits
+    static int split_k(int rows) {
+        int sp = rows;
+        for (int parts = 64; parts > 1; parts >>= 1)
+            if (rows % (parts * 256) == 0) { sp = rows / parts; break; }
+        return sp;
     }
 
     GemmArgs base_args() const {
@@ -578,11 +606,9 @@ struct LearnedModel {
             gw.A = dZ[cur]; gw.lda = kHidden; gw.a_t = 1;           // A[m=out][k=row] = dZ[row][out]
             gw.B = input; gw.ldb = layer_in(l); gw.b_t = 1;         // B[n=in][k=row] = input[row][in]
             gw.M = kHidden; gw.N = layer_in(l); gw.K = rows;
-            gw.epi = EPI_F32; gw.ldc = layer_in(l); gw.C32 = gtmp;
+            gw.ksplit = split_k(rows);                              // split the batch across CTAs
+            gw.epi = EPI_F32_ADD; gw.ldc = layer_in(l); gw.C32 = grads + w_offset(l);
             TRY(gemm(gw, s));
-            const size_t nw = (size_t)kHidden * layer_in(l);
-            k_add<<<blocks_for((long long)nw, 256), 256, 0, s>>>(gtmp, grads + w_offset(l), nw);
-            TRY(cudaGetLastError());
             k_bias_grad<<<256, 256, 0, s>>>(dZ[cur], rows, grads + b_offset(l));
             TRY(cudaGetLastError());
             if (l == 0) break;
@@ -744,7 +770,7 @@ int rlc_learned_predict(rlc_learned* L, const float* d_xyt, int n, float* d_pred
     if (!L || n < 0 || (n > 0 && (!d_xyt || !d_pred))) return lfail(RLC_ERR_ARG, "bad argument");
     LearnedModel& M = L->m;
     cudaStream_t s = (cudaStream_t)stream;
-    const int chunk = 65536;
+    const int chunk = 262144;
     LTRY(M.ensure(std::min(n, chunk)), "predict buffers");
     for (int off = 0; off < n; off += chunk) {
         const int cnt = std::min(chunk, n - off);
@@ -852,13 +878,12 @@ int rlc_learned_calc_range_repeat_angles(rlc_learned* L, const float* d_ins, con
     if (rays > (1ll << 31) - 1) return lfail(RLC_ERR_ARG, "too many rays");
     LearnedModel& M = L->m;
     cudaStream_t s = (cudaStream_t)stream;
-    float *xyt = nullptr, *pred = nullptr;
-    int *list = nullptr, *cnt = nullptr;
-    cudaError_t e = cudaMalloc(&xyt, (size_t)rays * 3 * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&pred, (size_t)rays * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&list, (size_t)rays * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&cnt, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(int), s);
+    LTRY(M.ensure_query(rays), "learned query buffers");
+    float* xyt = M.q_xyt;
+    float* pred = M.q_pred;
+    int* list = M.q_list;
+    int* cnt = M.q_cnt;
+    cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int), s);
     if (e == cudaSuccess) {
         k_world_rays<<<blocks_for(rays, 256), 256, 0, s>>>(M.world, d_ins, d_angles, n, na, xyt);
         e = cudaGetLastError();
@@ -877,10 +902,6 @@ int rlc_learned_calc_range_repeat_angles(rlc_learned* L, const float* d_ins, con
     int h_cnt = 0;
     if (e == cudaSuccess && !rc) e = cudaMemcpyAsync(&h_cnt, cnt, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && !rc) e = cudaStreamSynchronize(s);
-    cudaFree(xyt);
-    cudaFree(pred);
-    cudaFree(list);
-    cudaFree(cnt);
     if (rc) return rc;
     if (e != cudaSuccess) return lfail(RLC_ERR_CUDA, "learned ranges", e);
     if (n_recast) *n_recast = h_cnt;

@@ -99,10 +99,11 @@ def learned_setup(rl):
     return occ, m, rm
 
 
-def test_gradients_match_cpu_restatement(rl, learned_setup):
+@pytest.mark.parametrize("n", [256, 2048])   # 2048 rays: the weight gradients use split-K
+def test_gradients_match_cpu_restatement(rl, learned_setup, n):
     _, _, rm = learned_setup
     L = rl.PyLearnedRM(rm, seed=3)
-    xyt, t, _ = L.sample_rays(256, seed=11)
+    xyt, t, _ = L.sample_rays(n, seed=11)
     g, loss = L.gradients(xyt, t)
     X = L.features(xyt).float().cpu().numpy()
     exp, exp_loss = cpu_gradients(L.params(), X, t.cpu().numpy())
