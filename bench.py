@@ -520,8 +520,15 @@ def run_cddt(args):
         m.calc_range_many(ins, outs)
         return 1
 
-    for _ in range(args.warmup):
-        step()
+    per_mode = {}
+    for warp_search in (0, 1):   # per-thread and warp-cooperative bin search
+        m.set_schedule(0, 0, warp_search, 0)
+        for _ in range(args.warmup):
+            step()
+        t_mode, _ = _event_steps(torch, stream, args.steps, flush, step)
+        per_mode[warp_search] = sum(t_mode)
+    best = min(per_mode, key=per_mode.get)
+    m.set_schedule(0, 0, best, 0)
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     t, launches = _event_steps(torch, stream, args.steps, flush, step)
@@ -545,6 +552,8 @@ def run_cddt(args):
         "e2e": {"value": n / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": wl.ins.nbytes,
                 "d2h_bytes_per_step": h_out.nbytes},
         "host_equals_device": same, "gpu_launches": launches, "clocks": clk,
+        "search": {"per_thread_rays_per_s": n * args.steps / (per_mode[0] / 1e3),
+                   "warp_cooperative_rays_per_s": n * args.steps / (per_mode[1] / 1e3), "chosen": int(best)},
     }
     if rank == 0:
         print(json.dumps(line))

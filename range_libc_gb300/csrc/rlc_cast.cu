@@ -188,20 +188,59 @@ __device__ __forceinline__ void cddt_discretize(const CddtDev& c, float theta, i
     flipped = fl;
 }
 
-// upper_bound: first index with bin[i] > v
-__device__ __forceinline__ int upper_bound_g(const float* __restrict__ bin, int n, float v) {
+// first index i of the sorted bin with bin[i] > v (upper) or bin[i] >= v (lower); n if none
+__device__ __forceinline__ int bound_g(const float* __restrict__ bin, int n, float v, bool upper) {
     int lo = 0, hi = n;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        if (v < __ldg(bin + mid)) hi = mid; else lo = mid + 1;
+        const float z = __ldg(bin + mid);
+        if (upper ? (v < z) : (v <= z)) hi = mid; else lo = mid + 1;
     }
     return lo;
 }
 
-// RangeLib.h:1342-1516 (CDDTCast::calc_range)
-__device__ float cddt_cast(const CastParams& p, float x, float y, float heading) {
+// The same bound computed by a whole warp for one query: 32 pivots per
+// round, __ballot_sync narrows the range 32x, a last round scans <= 32
+// consecutive zero points in one coalesced load.  All 32 lanes must call it
+// with the same arguments.
+__device__ __forceinline__ int bound_warp(const float* __restrict__ bin, int n, float v, bool upper) {
+    const int lane = threadIdx.x & 31;
+    const float inf = __int_as_float(0x7f800000);
+    int lo = 0, hi = n;   // the answer lies in [lo, hi]
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) >> 5;
+        const int i = lo + lane * step;
+        const float z = i < hi ? __ldg(bin + i) : inf;
+        const unsigned m = __ballot_sync(0xffffffffu, upper ? (v < z) : (v <= z));
+        const int f = m ? __ffs(m) - 1 : 32;
+        const int nlo = f > 0 ? lo + (f - 1) * step + 1 : lo;
+        const int nhi = f < 32 ? min(hi, lo + f * step) : hi;
+        lo = nlo;
+        hi = nhi;
+    }
+    const int i = lo + lane;
+    const float z = i < hi ? __ldg(bin + i) : inf;
+    const unsigned m = __ballot_sync(0xffffffffu, i < hi && (upper ? (v < z) : (v <= z)));
+    return m ? lo + __ffs(m) - 1 : hi;
+}
+
+// A CDDT query up to its bin search (RangeLib.h:1342-1516).  Either the
+// result is final (mode 0) or the bin search is pending:
+//   mode 1  flipped:  the last zero point <= x (upper_bound - 1; the
+//           reference's binary and linear branches agree on it)
+//   mode 2  forward, bin > 65 entries: upper_bound (first > x)
+//   mode 3  forward, bin <= 65 entries: the linear scan's first >= x
+struct CddtPending {
+    const float* bin;
+    int n;
+    float lx;
+    int mode;
+};
+
+__device__ __forceinline__ float cddt_front(const CastParams& p, float x, float y, float heading, CddtPending& q) {
     const CddtDev& c = p.cddt;
     const float mr = p.mr;
+    q.mode = 0;
     if (isnan(x) || isnan(y) || isnan(heading)) return mr;
     int a;
     bool fl;
@@ -219,37 +258,62 @@ __device__ float cddt_cast(const CastParams& p, float x, float y, float heading)
     if (high == -1) return mr;
     const float first = __ldg(bin), last = __ldg(bin + high);
     // grid[x][y] with float indices: the cell under the query point
-    auto occupied = [&]() -> bool {
-        if (!(x > -1.0f) || !(y > -1.0f)) return false;
-        return occ_at(p.map, __float2int_rz(x), __float2int_rz(y));
-    };
+    const bool occ = (x > -1.0f) && (y > -1.0f) && occ_at(p.map, __float2int_rz(x), __float2int_rz(y));
+    q.bin = bin;
+    q.n = n;
+    q.lx = lx;
     if (fl) {
         if (first > lx) return mr;
         if (last < lx) return __fsub_rn(lx, last);
-        if (occupied()) return 0.0f;
-        if (high > kBinarySearchThreshold) {
-            int idx = upper_bound_g(bin, n, lx);
-            return __fsub_rn(lx, __ldg(bin + idx - 1));
-        }
-        for (int i = high; i >= 0; --i) {
-            float z = __ldg(bin + i);
-            if (z <= lx) return __fsub_rn(lx, z);
-        }
+        if (occ) return 0.0f;
+        q.mode = 1;
     } else {
         if (last < lx) return mr;
         if (first > lx) return __fsub_rn(first, lx);
-        if (occupied()) return 0.0f;
-        if (high > kBinarySearchThreshold) {
-            int idx = upper_bound_g(bin, n, lx);
-            if (idx == n) { atomicOr(p.err, F_CDDT_PAST_END); return 0.0f; }
-            return __fsub_rn(__ldg(bin + idx), lx);
-        }
-        for (int i = 0; i < n; ++i) {
-            float z = __ldg(bin + i);
-            if (z >= lx) return __fsub_rn(z, lx);
-        }
+        if (occ) return 0.0f;
+        q.mode = high > kBinarySearchThreshold ? 2 : 3;
     }
-    return -1.0f;
+    return 0.0f;
+}
+
+__device__ __forceinline__ float cddt_finish(const CastParams& p, const CddtPending& q, int idx) {
+    if (q.mode == 1) return __fsub_rn(q.lx, __ldg(q.bin + idx - 1));
+    if (idx == q.n) {   // x equals the last zero point: the reference reads past the bin
+        atomicOr(p.err, F_CDDT_PAST_END);
+        return 0.0f;
+    }
+    return __fsub_rn(__ldg(q.bin + idx), q.lx);
+}
+
+__device__ float cddt_cast(const CastParams& p, float x, float y, float heading) {
+    CddtPending q;
+    const float r = cddt_front(p, x, y, heading, q);
+    if (q.mode == 0) return r;
+    return cddt_finish(p, q, bound_g(q.bin, q.n, q.lx, q.mode != 3));
+}
+
+// warp-cooperative variant: every lane resolves its own query up to the bin,
+// then the warp searches the pending bins one query at a time
+__device__ __forceinline__ float cddt_cast_warp(const CastParams& p, bool active, float x, float y, float heading) {
+    CddtPending q;
+    q.mode = 0;
+    float r = active ? cddt_front(p, x, y, heading, q) : 0.0f;
+    unsigned pending = __ballot_sync(0xffffffffu, q.mode != 0);
+    int my_idx = 0;
+    const int lane = threadIdx.x & 31;
+    while (pending) {
+        const int src = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const unsigned long long bp =
+            __shfl_sync(0xffffffffu, (unsigned long long)reinterpret_cast<uintptr_t>(q.bin), src);
+        const int qn = __shfl_sync(0xffffffffu, q.n, src);
+        const float qlx = __shfl_sync(0xffffffffu, q.lx, src);
+        const int qmode = __shfl_sync(0xffffffffu, q.mode, src);
+        const int idx = bound_warp(reinterpret_cast<const float*>(bp), qn, qlx, qmode != 3);
+        if (lane == src) my_idx = idx;
+    }
+    if (q.mode != 0) r = cddt_finish(p, q, my_idx);
+    return r;
 }
 
 // ------------------------------------------------------------- dispatch
@@ -293,6 +357,21 @@ template <int KIND, int LAYOUT, int PF, bool WORLD>
 __global__ void __launch_bounds__(256) k_calc_range_many(CastParams p, const float* __restrict__ ins,
                                                          float* __restrict__ outs, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (KIND == K_CDDT && PF) {   // warp-cooperative bin search: every lane of the warp takes part
+        const bool act = i < n;
+        float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f;
+        if (act) { q0 = __ldg(ins + 3 * (size_t)i); q1 = __ldg(ins + 3 * (size_t)i + 1); q2 = __ldg(ins + 3 * (size_t)i + 2); }
+        float r;
+        if (WORLD) {
+            float ax, ay, th;
+            world_to_grid(p.world, q0, q1, q2, ax, ay, th);
+            r = __fmul_rn(cddt_cast_warp(p, act, ax, ay, th), p.world.s);
+        } else {
+            r = cddt_cast_warp(p, act, q0, q1, q2);
+        }
+        if (act) outs[i] = r;
+        return;
+    }
     if (i >= n) return;
     float q0 = __ldg(ins + 3 * (size_t)i), q1 = __ldg(ins + 3 * (size_t)i + 1), q2 = __ldg(ins + 3 * (size_t)i + 2);
     if (WORLD) {
@@ -310,6 +389,20 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
                                                        const float* __restrict__ angles,
                                                        float* __restrict__ outs, int n, int na) {
     long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (KIND == K_CDDT && PF) {   // warp-cooperative bin search
+        const bool act = g < (long long)n * na;
+        float ax = 0.0f, ay = 0.0f, h = 0.0f;
+        if (act) {
+            int i = (int)(g / na), a = (int)(g - (long long)i * na);
+            float th;
+            world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
+                          __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
+            h = __fsub_rn(th, __ldg(angles + a));
+        }
+        const float r = cddt_cast_warp(p, act, ax, ay, h);
+        if (act) outs[g] = __fmul_rn(r, p.world.s);
+        return;
+    }
     if (g >= (long long)n * na) return;
     int i = (int)(g / na);
     int a = (int)(g - (long long)i * na);
@@ -490,6 +583,7 @@ cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
         return F<K_RM, DT_LINEAR, 0>::run(args...);
     }
     if (kind == K_BL) return F<K_BL, DT_LINEAR, 0>::run(args...);
+    if (pf) return F<K_CDDT, DT_LINEAR, 1>::run(args...);   // warp-cooperative bin search
     return F<K_CDDT, DT_LINEAR, 0>::run(args...);
 }
 

@@ -161,7 +161,12 @@ def test_repeat_angles_parity(rl, oracle_mod, kind):
         g.set_trig_override(trig)
     out = np.empty(len(ins) * len(angles), np.float32)
     g.calc_range_repeat_angles(ins, angles, out)
-    assert np.array_equal(_bits(out), _bits(ref.calc_range_repeat_angles(ins, angles)))
+    exp = ref.calc_range_repeat_angles(ins, angles)
+    assert np.array_equal(_bits(out), _bits(exp))
+    if kind == "cddt":   # warp-cooperative bin search
+        g.set_schedule(0, 0, 1, 0)
+        g.calc_range_repeat_angles(ins, angles, out)
+        assert np.array_equal(_bits(out), _bits(exp))
 
 
 @pytest.mark.parametrize("name", ["quad", "small_5x6", "rect_128", "rect_200x120", "corridor_512"])
@@ -183,9 +188,12 @@ def test_cddt_table_and_queries(rl, oracle_mod, name, td):
         assert np.array_equal(_bits(gz), _bits(rz))
         q = W.free_cell_queries(occ, 3000, 4) if occ.min() == 0 else _queries(occ, 3000, 4)
         q[:, 2] = np.random.default_rng(td).uniform(-10, 10, len(q))
-        out = np.empty(len(q), np.float32)
-        g.calc_range_many(q, out)
-        assert np.array_equal(_bits(out), _bits(ref.calc_range_many(q)))
+        exp = ref.calc_range_many(q)
+        for warp_search in (0, 1):   # per-thread and warp-cooperative bin search
+            g.set_schedule(0, 0, warp_search, 0)
+            out = np.empty(len(q), np.float32)
+            g.calc_range_many(q, out)
+            assert np.array_equal(_bits(out), _bits(exp)), warp_search
 
 
 def test_cddt_given_table(rl, oracle_mod):
