@@ -165,7 +165,9 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
 
 /* ---- tuning ------------------------------------------------------------ */
 /* Schedule of the kernels: dt_layout 0 = linear x-major distance transform, 1 = 8x8 tiles,
- * 2 = compact 16-bit squared distances (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
+ * 2 = compact 16-bit squared distances, 3 = beam-major fused update that stages each bundle's
+ * window of 8-bit squared distances in shared memory (RM only; tile = particle chunks per beam,
+ * 0 = one block per SM) (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
  * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray, and for CDDT
  * methods a warp-cooperative bin search (32 zero points per step, ballot) in calc_range_many and
  * calc_range_repeat_angles; tile =

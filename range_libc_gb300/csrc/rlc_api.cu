@@ -59,6 +59,7 @@ struct rlc_map {
     float* d_dt = nullptr;
     float* d_dt_tiled = nullptr;
     uint16_t* d_dt16 = nullptr;
+    uint8_t* d_dt8 = nullptr;
     std::atomic<int> refs{1};
     std::mutex mu;
 
@@ -67,6 +68,7 @@ struct rlc_map {
         cudaFree(d_dt);
         cudaFree(d_dt_tiled);
         cudaFree(d_dt16);
+        cudaFree(d_dt8);
     }
     // distance transform on first use (RayMarching constructor, RangeLib.h:924)
     int ensure_dt() {
@@ -77,26 +79,31 @@ struct rlc_map {
         float* dt = nullptr;
         float* dtt = nullptr;
         uint16_t* dt16 = nullptr;
+        uint8_t* dt8 = nullptr;
         void* scratch = nullptr;
         size_t sb = edt_scratch_bytes(W, H);
         cudaError_t e = cudaMalloc(&dt, (n ? n : 1) * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&dtt, (tiled ? tiled : 1) * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&dt16, (tiled ? tiled : 1) * sizeof(uint16_t));
+        if (e == cudaSuccess) e = cudaMalloc(&dt8, (tiled ? tiled : 1) * sizeof(uint8_t));
         if (e == cudaSuccess) e = cudaMalloc(&scratch, sb);
         if (e == cudaSuccess) e = launch_edt(d_bits, W, H, TY, dt, scratch, sb, 0);
         if (e == cudaSuccess) e = launch_dt_to_tiled(dt, W, H, dtt, 0);
         if (e == cudaSuccess) e = launch_dt_to_u16(dt, W, H, dt16, 0);
+        if (e == cudaSuccess) e = launch_dt_to_u8(dt, W, H, dt8, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         cudaFree(scratch);
         if (e != cudaSuccess) {
             cudaFree(dt);
             cudaFree(dtt);
             cudaFree(dt16);
+            cudaFree(dt8);
             return cuda_fail(e, "distance transform");
         }
         d_dt = dt;
         d_dt_tiled = dtt;
         d_dt16 = dt16;
+        d_dt8 = dt8;
         return RLC_OK;
     }
     void retain() { refs.fetch_add(1); }
@@ -131,6 +138,9 @@ struct rlc_method {
     unsigned* d_err = nullptr;
     float* d_trig = nullptr;
     int64_t trig_count = 0;
+    // beam-major range bins of the staged fused update (scratch, n x na)
+    uint16_t* d_bins = nullptr;
+    size_t bins_cap = 0;
     // schedule
     int layout = DT_LINEAR;
     int prefetch = 0;
@@ -150,6 +160,7 @@ struct rlc_method {
         cudaFree(d_stage);
         cudaFree(d_err);
         cudaFree(d_trig);
+        cudaFree(d_bins);
         if (map) map->release();
     }
 
@@ -160,8 +171,9 @@ struct rlc_method {
         p.map.W = map->W;
         p.map.H = map->H;
         p.map.tiles_y = map->TY;
-        p.map.dt = layout == DT_TILED ? map->d_dt_tiled : map->d_dt;
+        p.map.dt = layout == DT_TILED ? map->d_dt_tiled : map->d_dt;   // linear for DT_U16 / DT_STAGED
         p.map.dt16 = map->d_dt16;
+        p.map.dt8 = map->d_dt8;
         p.map.bits = map->d_bits;
         p.cddt.td = td;
         p.cddt.td_div_2pi = td_div_2pi;
@@ -267,6 +279,9 @@ int finish_launch(cudaError_t e, const char* what) {
     if (e != cudaSuccess) return cuda_fail(e, what);
     return RLC_OK;
 }
+
+// layout used by the per-ray kernels (the staged schedule only changes the fused update)
+int cast_layout(const rlc_method* m) { return m->layout == DT_STAGED ? DT_LINEAR : m->layout; }
 
 int check_trig(const rlc_method* m, long long rays) {
     if (m->d_trig && m->trig_count < rays)
@@ -551,14 +566,14 @@ int rlc_calc_range_many(rlc_method* m, const float* ins, float* outs, int n, uns
     CastParams p = m->params();
     bool world = !(flags & RLC_NO_WORLD);
     if (flags & RLC_DEVICE_PTRS)
-        return finish_launch(launch_calc_range_many(p, m->layout, m->prefetch, world, ins, outs, n, s), "calc_range_many");
+        return finish_launch(launch_calc_range_many(p, cast_layout(m), m->prefetch, world, ins, outs, n, s), "calc_range_many");
     size_t bin = align256((size_t)n * 3 * sizeof(float));
     void* st;
     if (int rc = m->stage(bin + (size_t)n * sizeof(float), &st)) return rc;
     float* d_in = (float*)st;
     float* d_out = (float*)((char*)st + bin);
     CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
-    CUDA_OR_FAIL(launch_calc_range_many(p, m->layout, m->prefetch, world, d_in, d_out, n, s), "calc_range_many");
+    CUDA_OR_FAIL(launch_calc_range_many(p, cast_layout(m), m->prefetch, world, d_in, d_out, n, s), "calc_range_many");
     CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
     CUDA_OR_FAIL(cudaStreamSynchronize(s), "calc_range_many");
     return RLC_OK;
@@ -575,7 +590,7 @@ int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* a
     cudaStream_t s = (cudaStream_t)stream;
     CastParams p = m->params();
     if (flags & RLC_DEVICE_PTRS)
-        return finish_launch(launch_repeat_angles(p, m->layout, m->prefetch, ins, angles, outs, n, na, s), "repeat_angles");
+        return finish_launch(launch_repeat_angles(p, cast_layout(m), m->prefetch, ins, angles, outs, n, na, s), "repeat_angles");
     size_t b0 = align256((size_t)n * 3 * sizeof(float));
     size_t b1 = align256((size_t)na * sizeof(float));
     void* st;
@@ -585,7 +600,7 @@ int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* a
     float* d_out = (float*)((char*)st + b0 + b1);
     CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
     CUDA_OR_FAIL(cudaMemcpyAsync(d_ang, angles, (size_t)na * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
-    CUDA_OR_FAIL(launch_repeat_angles(p, m->layout, m->prefetch, d_in, d_ang, d_out, n, na, s), "repeat_angles");
+    CUDA_OR_FAIL(launch_repeat_angles(p, cast_layout(m), m->prefetch, d_in, d_ang, d_out, n, na, s), "repeat_angles");
     CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, (size_t)n * na * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
     CUDA_OR_FAIL(cudaStreamSynchronize(s), "repeat_angles");
     return RLC_OK;
@@ -669,6 +684,16 @@ int rlc_calc_range_repeat_angles_eval_sensor_model(rlc_method* m, const float* i
     return RLC_OK;
 }
 
+static int ensure_bins(rlc_method* m, size_t count) {
+    if (count <= m->bins_cap) return RLC_OK;
+    cudaFree(m->d_bins);
+    m->d_bins = nullptr;
+    m->bins_cap = 0;
+    CUDA_OR_FAIL(cudaMalloc(&m->d_bins, count * sizeof(uint16_t)), "staged update scratch");
+    m->bins_cap = count;
+    return RLC_OK;
+}
+
 static int fused_device(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
                         int na, cudaStream_t s) {
     if (m->autotune_pending) {
@@ -678,7 +703,12 @@ static int fused_device(rlc_method* m, const float* ins, const float* angles, co
     }
     CastParams p = m->params();
     SensorDev sm{m->d_table, m->K};
-    return finish_launch(launch_fused(p, m->layout, m->prefetch, sm, ins, angles, obs, w, n, na, m->fused_block,
+    if (m->layout == DT_STAGED && m->dkind == K_RM) {
+        if (int rc = ensure_bins(m, (size_t)n * na)) return rc;
+        return finish_launch(launch_fused_staged(p, sm, ins, angles, obs, w, n, na, m->tile, m->d_bins, s),
+                             "fused sensor model (staged)");
+    }
+    return finish_launch(launch_fused(p, cast_layout(m), m->prefetch, sm, ins, angles, obs, w, n, na, m->fused_block,
                                       m->tile, s),
                          "fused sensor model");
 }
@@ -716,7 +746,7 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
 
 int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile) {
     if (int rc = check_method(m)) return rc;
-    if (dt_layout < -1 || dt_layout > 2) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1 or 2");
+    if (dt_layout < -1 || dt_layout > 3) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2 or 3");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
     if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
@@ -788,6 +818,32 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
                     }
                 }
             }
+        }
+    }
+    if (rm && err == cudaSuccess) {   // beam-major update with staged windows
+        if (int rc = ensure_bins(m, (size_t)n * na)) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
+        }
+        m->layout = DT_STAGED;
+        CastParams p = m->params();
+        float total = 0.0f;
+        for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+            err = launch_fused_staged(p, sm, ins, angles, obs, w, n, na, 0, m->d_bins, s);
+            if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+            if (err == cudaSuccess) err = launch_fused_staged(p, sm, ins, angles, obs, w, n, na, 0, m->d_bins, s);
+            if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) total += ms;
+        }
+        if (err == cudaSuccess && total < best) {
+            best = total;
+            best_layout = DT_STAGED;
+            best_tile = 0;
+            best_pf = 0;
         }
     }
     cudaEventDestroy(e0);

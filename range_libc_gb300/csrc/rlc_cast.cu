@@ -13,6 +13,8 @@
 // per-ray trig override removes it for parity tests.
 #include "rlc_internal.cuh"
 
+#include <climits>
+
 namespace rlc {
 namespace {
 
@@ -75,25 +77,29 @@ template <int LAYOUT, int PF = 0>
 __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps = nullptr) {
     if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
     float t = 0.0f;
-    while (t < mr) {
-        int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
-        int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
-        if ((unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H) return mr;
+    if (!(t < mr)) return mr;
+    // one exit test per step: an off-grid position reads cell (0, 0) and leaves
+    for (;;) {
+        const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
+        const int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
+        const bool out = (unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H;
         if (PF > 0) {
             const float tp = t + (float)PF;
             const int qx = __float2int_rz(x0 + c * tp), qy = __float2int_rz(y0 + s * tp);
             if ((unsigned)qx < (unsigned)m.W && (unsigned)qy < (unsigned)m.H) prefetch_l1(dt_ptr<LAYOUT>(m, qx, qy));
         }
-        float d = dt_at<LAYOUT>(m, px, py);
-        if (steps) ++*steps;
-        if (d <= 0.0f) {
-            float xd = __fsub_rn(__int2float_rn(px), x0);
-            float yd = __fsub_rn(__int2float_rn(py), y0);
+        const float d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
+        if (steps && !out) ++*steps;
+        const float tn = __fadd_rn(t, ref_maxf(__fmul_rn(d, 0.999f), 1.0f));
+        const bool hit = d <= 0.0f;
+        if (out | hit | !(tn < mr)) {
+            if (out || !hit) return mr;
+            const float xd = __fsub_rn(__int2float_rn(px), x0);
+            const float yd = __fsub_rn(__int2float_rn(py), y0);
             return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
         }
-        t = __fadd_rn(t, ref_maxf(__fmul_rn(d, 0.999f), 1.0f));
+        t = tn;
     }
-    return mr;
 }
 
 // ---------------------------------------------------- Bresenham's line (BL)
@@ -418,20 +424,68 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
 // order (RangeLib.h:533-555, 558-612), in double, exactly as the reference
 // multiplies -- so weights are bit-identical.  A tile holds P particles;
 // its rays store their 16-bit range bin in shared memory (sdi, particle-
-// major), the beams' observation bins are in sri, and the products run one
-// particle per lane: each double multiply instruction then serves up to 32
-// particles instead of one.  Shared memory per block: (P * na + na) * 2 bytes.
-__device__ __forceinline__ void tile_products(const SensorDev& sm, const uint16_t* sdi, const uint16_t* sri, int na,
-                                              int P, int first, int n, double* __restrict__ weights) {
-    for (int li = threadIdx.x; li < P; li += blockDim.x) {
-        const int i = first + li;
-        if (i >= n) continue;
-        const uint16_t* row = sdi + (size_t)li * na;
+// major) and the beams' observation bins are in sri.  The products then run
+// in two phases: every thread of the block gathers table factors of the
+// tile's rays into shared memory (sdv), so that all the gathers are in
+// flight at once, and then one lane per particle multiplies its factors in
+// beam order -- each double multiply instruction serves up to 32 particles
+// and waits on shared memory only.
+struct TileSmem {
+    double* sdv;     // [P * na] table factors
+    uint16_t* sdi;   // [P * na] range bins
+    uint16_t* sri;   // [na] observation bins
+};
+
+__host__ __device__ inline size_t tile_smem(int P, int na) {
+    return ((size_t)P * na * (sizeof(double) + sizeof(uint16_t)) + (size_t)na * sizeof(uint16_t) + 15) & ~(size_t)15;
+}
+
+__device__ __forceinline__ TileSmem tile_layout(unsigned char* base, int P, int na) {
+    TileSmem t;
+    t.sdv = reinterpret_cast<double*>(base);
+    t.sdi = reinterpret_cast<uint16_t*>(base + (size_t)P * na * sizeof(double));
+    t.sri = t.sdi + (size_t)P * na;
+    return t;
+}
+
+// table factor of each of nr rays (ray r: beam r % na, bin sdi[r]) into dst,
+// kBatch independent gathers in flight per thread
+__device__ __forceinline__ void gather_factors(const SensorDev& sm, const uint16_t* sdi, const uint16_t* sri, int na,
+                                               int nr, double* dst) {
+    constexpr int kBatch = 4;
+    for (int r0 = threadIdx.x; r0 < nr; r0 += kBatch * blockDim.x) {
+        double v[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            const int r = r0 + u * blockDim.x;
+            if (r < nr) v[u] = __ldg(sm.table + (size_t)sri[r % na] * sm.K + sdi[r]);
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            const int r = r0 + u * blockDim.x;
+            if (r < nr) dst[r] = v[u];
+        }
+    }
+}
+
+// one lane per particle multiplies its na factors (row-major in sdv) in beam order
+__device__ __forceinline__ void chain_products(const double* sdv, int na, int np, int first,
+                                               double* __restrict__ weights) {
+    for (int li = threadIdx.x; li < np; li += blockDim.x) {
+        const double* row = sdv + (size_t)li * na;
         double w = 1.0;
 #pragma unroll 8
-        for (int a = 0; a < na; ++a) w = __dmul_rn(w, __ldg(sm.table + (size_t)sri[a] * sm.K + row[a]));
-        weights[i] = w;
+        for (int a = 0; a < na; ++a) w = __dmul_rn(w, row[a]);
+        weights[first + li] = w;
     }
+}
+
+__device__ __forceinline__ void tile_products(const SensorDev& sm, const TileSmem& ts, int na, int P, int first,
+                                              int n, double* __restrict__ weights) {
+    const int np = min(P, n - first);
+    if (np > 0) gather_factors(sm, ts.sdi, ts.sri, na, np * na, ts.sdv);
+    __syncthreads();
+    chain_products(ts.sdv, na, np, first, weights);
 }
 
 __device__ __forceinline__ void tile_obs_bins(const CastParams& p, const SensorDev& sm, const float* __restrict__ obs,
@@ -444,28 +498,28 @@ __device__ __forceinline__ void tile_obs_bins(const CastParams& p, const SensorD
 __global__ void __launch_bounds__(512) k_eval_sensor(CastParams p, SensorDev sm, const float* __restrict__ obs,
                                                      const float* __restrict__ ranges, double* __restrict__ outs,
                                                      int na, int n, int P) {
-    extern __shared__ uint16_t smem_u16[];
-    uint16_t* sdi = smem_u16;
-    uint16_t* sri = smem_u16 + (size_t)P * na;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const TileSmem ts = tile_layout(smem_raw, P, na);
     const int first = blockIdx.x * P;
-    tile_obs_bins(p, sm, obs, na, sri);
+    tile_obs_bins(p, sm, obs, na, ts.sri);
     const int nr = P * na;
     for (int r = threadIdx.x; r < nr; r += blockDim.x) {
         int li = r / na, a = r - li * na, i = first + li;
-        if (i < n) sdi[r] = (uint16_t)sensor_bin(__fmul_rn(__ldg(ranges + (size_t)i * na + a), p.world.inv_s), sm.K, p.err);
+        if (i < n) ts.sdi[r] = (uint16_t)sensor_bin(__fmul_rn(__ldg(ranges + (size_t)i * na + a), p.world.inv_s), sm.K, p.err);
     }
     __syncthreads();
-    tile_products(sm, sdi, sri, na, P, first, n, outs);
+    tile_products(sm, ts, na, P, first, n, outs);
 }
 
 // one tile of the fused update: cast P particles x na beams (ranges in
-// pixels, RangeLib.h:558-612), bin them, multiply per particle
+// pixels, RangeLib.h:558-612) and bin them into ts.sdi
 template <int KIND, int LAYOUT, int PF>
-__device__ __forceinline__ void fused_tile(const CastParams& p, const SensorDev& sm, const float* __restrict__ ins,
-                                           const float* __restrict__ angles, const float* __restrict__ obs,
-                                           double* __restrict__ weights, float* __restrict__ ranges, int n, int na,
-                                           int P, int first, uint16_t* sdi, uint16_t* sri, int layout, int pf) {
-    tile_obs_bins(p, sm, obs, na, sri);
+__device__ __forceinline__ void tile_cast(const CastParams& p, const SensorDev& sm, const float* __restrict__ ins,
+                                          const float* __restrict__ angles, const float* __restrict__ obs,
+                                          float* __restrict__ ranges, int n, int na, int P, int first,
+                                          const TileSmem& ts, int layout, int pf) {
+    uint16_t* sdi = ts.sdi;
+    tile_obs_bins(p, sm, obs, na, ts.sri);
     const int nr = P * na;
     for (int r = threadIdx.x; r < nr; r += blockDim.x) {
         int li = r / na, a = r - li * na, i = first + li;
@@ -499,16 +553,26 @@ __device__ __forceinline__ void fused_tile(const CastParams& p, const SensorDev&
         }
     }
     __syncthreads();
-    tile_products(sm, sdi, sri, na, P, first, n, weights);
 }
 
+// cast a tile, then multiply its particles' factors
+template <int KIND, int LAYOUT, int PF>
+__device__ __forceinline__ void fused_tile(const CastParams& p, const SensorDev& sm, const float* __restrict__ ins,
+                                           const float* __restrict__ angles, const float* __restrict__ obs,
+                                           double* __restrict__ weights, float* __restrict__ ranges, int n, int na,
+                                           int P, int first, const TileSmem& ts, int layout, int pf) {
+    tile_cast<KIND, LAYOUT, PF>(p, sm, ins, angles, obs, ranges, n, na, P, first, ts, layout, pf);
+    tile_products(sm, ts, na, P, first, n, weights);
+}
+
+// fused update, one tile of P particles per block
 template <int KIND, int LAYOUT, int PF>
 __global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
                                                const float* __restrict__ angles, const float* __restrict__ obs,
                                                double* __restrict__ weights, int n, int na, int P) {
-    extern __shared__ uint16_t smem_u16[];
-    fused_tile<KIND, LAYOUT, PF>(p, sm, ins, angles, obs, weights, nullptr, n, na, P, blockIdx.x * P, smem_u16,
-                                 smem_u16 + (size_t)P * na, LAYOUT, PF);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    fused_tile<KIND, LAYOUT, PF>(p, sm, ins, angles, obs, weights, nullptr, n, na, P, blockIdx.x * P,
+                                 tile_layout(smem_raw, P, na), LAYOUT, PF);
 }
 
 // ------------------------------------------------- persistent multi-filter
@@ -520,7 +584,7 @@ __global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const
 template <int MODE, int LAYOUT, int PF>
 __global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
                                                unsigned* __restrict__ queue) {
-    extern __shared__ uint16_t smem_u16[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ unsigned s_tile;
     __shared__ int s_f;
     for (;;) {
@@ -540,8 +604,176 @@ __global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ fil
         const FilterDev& F = filters[s_f];
         const int P = F.ppb;
         fused_tile<MODE, LAYOUT, PF>(F.p, F.sm, F.ins, F.angles, F.obs, F.weights, F.ranges, F.n, F.na, P,
-                             (int)(t - F.tile_begin) * P, smem_u16, smem_u16 + (size_t)P * F.na, F.layout, F.prefetch);
+                             (int)(t - F.tile_begin) * P, tile_layout(smem_raw, P, F.na), F.layout, F.prefetch);
         __syncthreads();   // before the next tile reuses shared memory and s_tile
+    }
+}
+
+
+// ------------------------------------------- beam-major fused update (staged)
+// One block per (beam a, chunk of particles): its rays start near the same
+// particle cluster and share a heading, so they sweep one bundle.  The block
+// copies the 8x8 tiles of the 8-bit squared distance transform that cover
+// the bundle's bounding box (capped at kStagedWindow bytes, shrunk around
+// its centre beyond that) into shared memory, with a 256-entry table of the
+// step max(sqrtf(v) * 0.999f, 1) of each d^2 = v.  Cells inside the window
+// with v <= 254 -- those next to walls, where long rays take their many
+// short steps -- are then read from shared memory; v = 255 cells and cells
+// outside the window read the float distance transform.  sqrtf(v) is the
+// distance transform's value exactly, so every step equals the reference's.
+constexpr int kStagedThreads = 1024;
+constexpr int kStagedWindow = 216 * 1024;
+
+__global__ void __launch_bounds__(kStagedThreads, 1) k_bm_cast(CastParams p, SensorDev sm, const float* __restrict__ ins,
+                                                              const float* __restrict__ angles, int n, int na, int P,
+                                                              uint16_t* __restrict__ bins, int cap_tiles) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    float* step_tab = reinterpret_cast<float*>(smem);   // [256]
+    uint8_t* win = smem + 1024;
+    __shared__ int bb[4];
+    const MapDev& m = p.map;
+    const int a = blockIdx.x;
+    const int first = blockIdx.y * P, last = min(n, first + P);
+    const float ang = __ldg(angles + a);
+    for (int v = threadIdx.x; v < 256; v += blockDim.x)
+        step_tab[v] = ref_maxf(__fmul_rn(__fsqrt_rn(__uint2float_rn(v)), 0.999f), 1.0f);
+    if (threadIdx.x == 0) { bb[0] = INT_MAX; bb[1] = INT_MIN; bb[2] = INT_MAX; bb[3] = INT_MIN; }
+    __syncthreads();
+    // bounding box of the bundle's segments [start, start + max_range * dir]
+    int xmn = INT_MAX, xmx = INT_MIN, ymn = INT_MAX, ymx = INT_MIN;
+    for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+        float ax, ay, th;
+        world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
+                      __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
+        float c, s;
+        sincosf(__fsub_rn(th, ang), &s, &c);
+        const float ex = ax + p.mr * c, ey = ay + p.mr * s;
+        if (!(isfinite(ax) && isfinite(ay) && isfinite(ex) && isfinite(ey))) continue;
+        const float lx = fminf(fmaxf(fminf(ax, ex), -1e6f), 1e6f), hx = fminf(fmaxf(fmaxf(ax, ex), -1e6f), 1e6f);
+        const float ly = fminf(fmaxf(fminf(ay, ey), -1e6f), 1e6f), hy = fminf(fmaxf(fmaxf(ay, ey), -1e6f), 1e6f);
+        xmn = min(xmn, (int)floorf(lx) - 1);
+        xmx = max(xmx, (int)ceilf(hx) + 1);
+        ymn = min(ymn, (int)floorf(ly) - 1);
+        ymx = max(ymx, (int)ceilf(hy) + 1);
+    }
+    for (int o = 16; o; o >>= 1) {
+        xmn = min(xmn, __shfl_xor_sync(0xffffffffu, xmn, o));
+        xmx = max(xmx, __shfl_xor_sync(0xffffffffu, xmx, o));
+        ymn = min(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
+        ymx = max(ymx, __shfl_xor_sync(0xffffffffu, ymx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&bb[0], xmn);
+        atomicMax(&bb[1], xmx);
+        atomicMin(&bb[2], ymn);
+        atomicMax(&bb[3], ymx);
+    }
+    __syncthreads();
+    const int TX = (m.W + 7) >> 3, TY = m.tiles_y;
+    int tx0 = max(0, bb[0] >> 3), tx1 = min(TX - 1, bb[1] >> 3);
+    int ty0 = max(0, bb[2] >> 3), ty1 = min(TY - 1, bb[3] >> 3);
+    int ntx = tx1 - tx0 + 1, nty = ty1 - ty0 + 1;
+    if (ntx <= 0 || nty <= 0) { ntx = 0; nty = 0; }
+    if (ntx * nty > cap_tiles) {   // shrink around the box centre
+        const float sc = sqrtf((float)cap_tiles / (float)(ntx * nty));
+        int nx = max(1, min(ntx, (int)(ntx * sc)));
+        int ny = max(1, min(nty, cap_tiles / nx));
+        tx0 += (ntx - nx) / 2;
+        ty0 += (nty - ny) / 2;
+        ntx = nx;
+        nty = ny;
+    }
+    // copy the window's tiles: rows of nty consecutive tiles are contiguous in global memory
+    const int nvec = ntx * nty * 4;
+    for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
+        const int t = v >> 2, part = v & 3;
+        const int ltx = t / nty, lty = t - ltx * nty;
+        const uint4 val = __ldg(reinterpret_cast<const uint4*>(m.dt8 + ((size_t)(tx0 + ltx) * TY + ty0 + lty) * 64) + part);
+        reinterpret_cast<uint4*>(win)[v] = val;
+    }
+    __syncthreads();
+    // march every ray of the block
+    for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+        float x0, y0, th;
+        world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
+                      __ldg(ins + 3 * (size_t)i + 2), x0, y0, th);
+        const long long ray = (long long)i * na + a;
+        float c, s;
+        if (p.trig) { c = p.trig[2 * ray]; s = p.trig[2 * ray + 1]; } else sincosf(__fsub_rn(th, ang), &s, &c);
+        float out = p.mr;
+        if (!(isnan(x0) || isnan(y0) || isnan(c) || isnan(s))) {
+            float t = 0.0f;
+            while (t < p.mr) {
+                const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
+                const int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
+                if ((unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H) break;
+                const int ltx = (px >> 3) - tx0, lty = (py >> 3) - ty0;
+                unsigned v = 255u;
+                if ((unsigned)ltx < (unsigned)ntx && (unsigned)lty < (unsigned)nty)
+                    v = win[((ltx * nty + lty) << 6) | ((px & 7) << 3) | (py & 7)];
+                bool hit;
+                float step;
+                if (v != 255u) {
+                    hit = v == 0u;
+                    step = step_tab[v];
+                } else {
+                    const float d = __ldg(m.dt + (size_t)px * m.H + py);
+                    hit = d <= 0.0f;
+                    step = ref_maxf(__fmul_rn(d, 0.999f), 1.0f);
+                }
+                if (hit) {
+                    const float xd = __fsub_rn(__int2float_rn(px), x0), yd = __fsub_rn(__int2float_rn(py), y0);
+                    out = __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+                    break;
+                }
+                t = __fadd_rn(t, step);
+            }
+        }
+        bins[(size_t)a * n + i] = (uint16_t)sensor_bin(out, sm.K, p.err);
+    }
+}
+
+// per-particle products of the beam-major bins, in beam order: the block
+// gathers the table factors of its PB particles into shared memory (beam-
+// major, all gathers in flight at once), then one lane per particle multiplies
+__global__ void __launch_bounds__(128) k_bm_weights(CastParams p, SensorDev sm, const float* __restrict__ obs,
+                                                    const uint16_t* __restrict__ bins, int n, int na, int PB,
+                                                    double* __restrict__ weights) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* sdv = reinterpret_cast<double*>(smem_raw);
+    uint16_t* sri = reinterpret_cast<uint16_t*>(smem_raw + (size_t)PB * na * sizeof(double));
+    for (int a = threadIdx.x; a < na; a += blockDim.x)
+        sri[a] = (uint16_t)sensor_bin(__fmul_rn(__ldg(obs + a), p.world.inv_s), sm.K, p.err);
+    __syncthreads();
+    const int first = blockIdx.x * PB;
+    const int np = min(PB, n - first);
+    const int nr = np * na;
+    constexpr int kBatch = 4;
+    for (int r0 = threadIdx.x; r0 < nr; r0 += kBatch * blockDim.x) {
+        double v[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            const int r = r0 + u * blockDim.x;
+            if (r < nr) {
+                const int a = r / np, li = r - a * np;
+                v[u] = __ldg(sm.table + (size_t)sri[a] * sm.K + __ldg(bins + (size_t)a * n + first + li));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            const int r = r0 + u * blockDim.x;
+            if (r < nr) {
+                const int a = r / np, li = r - a * np;
+                sdv[(size_t)a * PB + li] = v[u];
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < np) {
+        double w = 1.0;
+#pragma unroll 8
+        for (int a = 0; a < na; ++a) w = __dmul_rn(w, sdv[(size_t)a * PB + threadIdx.x]);
+        weights[first + threadIdx.x] = w;
     }
 }
 
@@ -608,18 +840,15 @@ struct RunAngles {
     }
 };
 
-// Shared memory per block of the product kernels: P * na + na 16-bit bins.
-inline size_t tile_smem(int P, int na) { return (((size_t)P * na + (size_t)na) * sizeof(uint16_t) + 15) & ~(size_t)15; }
-
 // particles per tile (P) and threads per block: P = tile if given, else the
 // most particles whose rays fit one ray per thread; P is capped so that the
-// tile's bins fit kTileSmem bytes
+// tile's bins and factors fit kTileSmem bytes
 constexpr size_t kTileSmem = 48 * 1024;
 inline void product_shape(int na, int block, int tile, int& P, int& threads) {
     if (block <= 0) block = 256;
     if (na <= 0) { P = block; threads = block; return; }   // empty product: weight 1.0
     P = tile > 0 ? tile : (na >= block ? 1 : block / na);
-    int cap = (int)((kTileSmem / sizeof(uint16_t) - (size_t)na) / (size_t)na);
+    int cap = (int)((kTileSmem / sizeof(uint16_t) - (size_t)na) / ((size_t)na * (1 + sizeof(double) / sizeof(uint16_t))));
     if (cap < 1) cap = 1;
     if (P > cap) P = cap;
     int nr = P * na;
@@ -708,6 +937,37 @@ static BatchKernel batch_kernel(bool rm_only, int layout, int pf) {
     if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, 0>;
     if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, 0>;
     return k_batch<kRmOnly, DT_LINEAR, 0>;
+}
+
+cudaError_t launch_fused_staged(const CastParams& p, const SensorDev& sm, const float* ins, const float* angles,
+                                const float* obs, double* weights, int n, int na, int chunks,
+                                uint16_t* bins, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (na <= 0) return launch_fused(p, DT_LINEAR, 0, sm, ins, angles, obs, weights, n, na, 0, 0, s);
+    if (chunks <= 0) {   // one block per SM: beams x chunks ~ SM count
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        chunks = max(1, sms / na);
+    }
+    const int P = (n + chunks - 1) / chunks;
+    const size_t smem = 1024 + kStagedWindow;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_bm_cast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    dim3 grid(na, (n + P - 1) / P);
+    k_bm_cast<<<grid, kStagedThreads, smem, s>>>(p, sm, ins, angles, n, na, P, bins, kStagedWindow / 64);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int PB = max(1, min(32, (int)((kTileSmem - (size_t)na * sizeof(uint16_t)) / ((size_t)na * sizeof(double)))));
+    const size_t wsmem = (((size_t)PB * na * sizeof(double) + (size_t)na * sizeof(uint16_t)) + 15) & ~(size_t)15;
+    e = set_smem(k_bm_weights, wsmem);
+    if (e != cudaSuccess) return e;
+    k_bm_weights<<<blocks_for(n, PB), 128, wsmem, s>>>(p, sm, obs, bins, n, na, PB, weights);
+    return cudaGetLastError();
 }
 
 cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, int* blocks_per_sm) {

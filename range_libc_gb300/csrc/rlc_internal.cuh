@@ -32,13 +32,14 @@ enum DevFlag : unsigned {
     F_NAN_INDEX = 8u,      // NaN range/observation mapped to sensor bin 0
 };
 
-enum DtLayout : int { DT_LINEAR = 0, DT_TILED = 1, DT_U16 = 2 };
+enum DtLayout : int { DT_LINEAR = 0, DT_TILED = 1, DT_U16 = 2, DT_STAGED = 3 };
 
 struct MapDev {
     int W, H;
     int tiles_y;              // ceil(H / 8)
     const float* dt;          // distance transform (DT_LINEAR / DT_TILED; linear for DT_U16)
     const uint16_t* dt16;     // compact squared distances (DT_U16)
+    const uint8_t* dt8;       // 8-bit squared distances (DT_STAGED windows)
     const uint64_t* bits;     // occupancy bit tiles
 };
 
@@ -85,6 +86,7 @@ constexpr size_t edt_scratch_bound(size_t cells, size_t side) {
 }
 cudaError_t launch_dt_to_tiled(const float* d_lin, int W, int H, float* d_tiled, cudaStream_t s);
 cudaError_t launch_dt_to_u16(const float* d_lin, int W, int H, uint16_t* d_u16, cudaStream_t s);
+cudaError_t launch_dt_to_u8(const float* d_lin, int W, int H, uint8_t* d_u8, cudaStream_t s);
 cudaError_t launch_edge_map(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_edge, cudaStream_t s);
 cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_occ, cudaStream_t s);
 
@@ -103,6 +105,15 @@ cudaError_t launch_fused(const CastParams& p, int layout, int pf, const SensorDe
 // particles per tile the fused kernels use, and the shared memory of such a tile
 int tile_particles(int na, int block, int tile);
 size_t tile_smem_bytes(int P, int na);
+
+// beam-major fused particle update with a staged shared-memory window of the
+// 8-bit distance transform (RM only): bins[a * n + i] receives each ray's
+// range bin, then the per-particle products run in a second kernel.
+// The grid is beams x chunks blocks of the particles; chunks = 0 picks
+// max(1, SMs / beams) so that the grid fills the GPU once.
+cudaError_t launch_fused_staged(const CastParams& p, const SensorDev& sm, const float* ins, const float* angles,
+                                const float* obs, double* weights, int n, int na, int chunks,
+                                uint16_t* bins, cudaStream_t s);
 
 // march steps of world-frame repeat-angle rays (RM and BL), summed into *total
 cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,

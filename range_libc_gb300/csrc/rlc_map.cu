@@ -143,6 +143,25 @@ __global__ void k_dt_to_u16(const float* __restrict__ lin, int W, int H, int TY,
     out[i] = v;
 }
 
+// 8-bit squared distance in 8x8 tiles of 64 bytes (x-major within the tile):
+// d^2 <= 254 exactly, 255 = "read the float"
+__global__ void k_dt_to_u8(const float* __restrict__ lin, int W, int H, int TY, uint8_t* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int TX = (W + 7) >> 3;
+    if (i >= (long long)TX * TY * 64) return;
+    long long tile = i >> 6;
+    int within = (int)(i & 63);
+    int tx = (int)(tile / TY), ty = (int)(tile - (long long)tx * TY);
+    int x = (tx << 3) + (within >> 3), y = (ty << 3) + (within & 7);
+    uint8_t v = 0xFF;
+    if (x < W && y < H) {
+        double d = (double)lin[(size_t)x * H + y];
+        double d2 = rint(d * d);
+        if (d2 <= 254.0 && __fsqrt_rn((float)d2) == (float)d) v = (uint8_t)d2;
+    }
+    out[i] = v;
+}
+
 // RangeLib.h:293-312: an occupied cell with any in-grid free 8-neighbour.
 __global__ void k_edge_map(const uint64_t* __restrict__ bits, int W, int H, int TY, uint8_t* __restrict__ edge) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -221,6 +240,14 @@ cudaError_t launch_dt_to_u16(const float* d_lin, int W, int H, uint16_t* d_u16, 
     long long n = (long long)TX * TY * 64;
     if (n == 0) return cudaSuccess;
     k_dt_to_u16<<<blocks_for(n, 256), 256, 0, s>>>(d_lin, W, H, TY, d_u16);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dt_to_u8(const float* d_lin, int W, int H, uint8_t* d_u8, cudaStream_t s) {
+    int TY = (H + 7) >> 3, TX = (W + 7) >> 3;
+    long long n = (long long)TX * TY * 64;
+    if (n == 0) return cudaSuccess;
+    k_dt_to_u8<<<blocks_for(n, 256), 256, 0, s>>>(d_lin, W, H, TY, d_u8);
     return cudaGetLastError();
 }
 

@@ -253,6 +253,37 @@ def test_sensor_model_and_fused_parity(rl, oracle_mod, kind):
     assert np.array_equal(_bits(wf), _bits(ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs)))
 
 
+@pytest.mark.parametrize("side,n,mr", [(512, 256, 200.0), (2048, 500, 1500.0)])
+def test_staged_update_parity(rl, oracle_mod, side, n, mr):
+    """The beam-major update with staged 8-bit windows (dt_layout 3) gives the oracle's weights bit
+    for bit, for any number of particle chunks per beam -- also when the bundle's box exceeds the
+    window (max range 1500 px on 2048^2), and with NaN, infinite and far-off particles."""
+    wl = _pf(side=side, n=n, mr=mr)
+    ins = wl.ins.copy()
+    ins[0] = (np.nan, 1.0, 0.0)
+    ins[1] = (1e30, -1e30, 0.5)
+    ins[2] = (np.inf, 3.0, -1.0)
+    ins[3, 2] = np.nan
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyRayMarching(m, wl.max_range)
+    ref = oracle_mod.OracleMethod(wl.occ, "rm", wl.max_range, world=m.world)
+    g.set_sensor_model(wl.table)
+    ref.set_sensor_model(wl.table)
+    _, trig = oracle_mod.world_rays(m.world, ins, wl.angles)
+    g.set_trig_override(trig)
+    exp = ref.calc_range_repeat_angles_eval_sensor_model(ins, wl.angles, wl.obs)
+    for chunks in (0, 1, 3, 40):
+        g.set_schedule(3, 0, 0, chunks)
+        assert g.schedule()[0] == 3 and g.schedule()[3] == chunks
+        w = np.empty(len(ins), np.float64)
+        g.calc_range_repeat_angles_eval_sensor_model(ins, wl.angles, wl.obs, w)
+        assert np.array_equal(_bits(w), _bits(exp)), chunks
+    # the per-ray entry points keep their own kernels under this schedule
+    r = np.empty(len(ins) * len(wl.angles), np.float32)
+    g.calc_range_repeat_angles(ins, wl.angles, r)
+    assert np.array_equal(_bits(r), _bits(ref.calc_range_repeat_angles(ins, wl.angles)))
+
+
 def test_fused_many_beams_underflow(rl, oracle_mod):
     """1,081 beams: products reach subnormals and zero; the in-order product stays bit-exact."""
     wl = _pf(n=64, m=1081)
@@ -432,7 +463,7 @@ def test_results_do_not_depend_on_the_schedule(rl):
     g.set_schedule(0, 256, 0, 0)
     g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, base_w)
     g.calc_range_repeat_angles(wl.ins, wl.angles, base_r)
-    for layout in (0, 1, 2):
+    for layout in (0, 1, 2, 3):
         for pf in (0, 1):
             for block in (64, 128, 512):
                 for tile in (0, 1, 7, 32):
