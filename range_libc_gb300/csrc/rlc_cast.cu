@@ -424,68 +424,38 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
 // order (RangeLib.h:533-555, 558-612), in double, exactly as the reference
 // multiplies -- so weights are bit-identical.  A tile holds P particles;
 // its rays store their 16-bit range bin in shared memory (sdi, particle-
-// major) and the beams' observation bins are in sri.  The products then run
-// in two phases: every thread of the block gathers table factors of the
-// tile's rays into shared memory (sdv), so that all the gathers are in
-// flight at once, and then one lane per particle multiplies its factors in
-// beam order -- each double multiply instruction serves up to 32 particles
-// and waits on shared memory only.
+// major), the beams' observation bins are in sri, and the products run one
+// particle per lane: each double multiply instruction then serves up to 32
+// particles instead of one (the FP64 pipe spends the same time on a warp
+// instruction with one active lane as with 32).  Shared memory per block:
+// (P * na + na) * 2 bytes.
 struct TileSmem {
-    double* sdv;     // [P * na] table factors
     uint16_t* sdi;   // [P * na] range bins
     uint16_t* sri;   // [na] observation bins
 };
 
 __host__ __device__ inline size_t tile_smem(int P, int na) {
-    return ((size_t)P * na * (sizeof(double) + sizeof(uint16_t)) + (size_t)na * sizeof(uint16_t) + 15) & ~(size_t)15;
+    return (((size_t)P * na + (size_t)na) * sizeof(uint16_t) + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ TileSmem tile_layout(unsigned char* base, int P, int na) {
     TileSmem t;
-    t.sdv = reinterpret_cast<double*>(base);
-    t.sdi = reinterpret_cast<uint16_t*>(base + (size_t)P * na * sizeof(double));
+    t.sdi = reinterpret_cast<uint16_t*>(base);
     t.sri = t.sdi + (size_t)P * na;
     return t;
 }
 
-// table factor of each of nr rays (ray r: beam r % na, bin sdi[r]) into dst,
-// kBatch independent gathers in flight per thread
-__device__ __forceinline__ void gather_factors(const SensorDev& sm, const uint16_t* sdi, const uint16_t* sri, int na,
-                                               int nr, double* dst) {
-    constexpr int kBatch = 4;
-    for (int r0 = threadIdx.x; r0 < nr; r0 += kBatch * blockDim.x) {
-        double v[kBatch];
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-            const int r = r0 + u * blockDim.x;
-            if (r < nr) v[u] = __ldg(sm.table + (size_t)sri[r % na] * sm.K + sdi[r]);
-        }
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-            const int r = r0 + u * blockDim.x;
-            if (r < nr) dst[r] = v[u];
-        }
-    }
-}
-
-// one lane per particle multiplies its na factors (row-major in sdv) in beam order
-__device__ __forceinline__ void chain_products(const double* sdv, int na, int np, int first,
-                                               double* __restrict__ weights) {
-    for (int li = threadIdx.x; li < np; li += blockDim.x) {
-        const double* row = sdv + (size_t)li * na;
-        double w = 1.0;
-#pragma unroll 8
-        for (int a = 0; a < na; ++a) w = __dmul_rn(w, row[a]);
-        weights[first + li] = w;
-    }
-}
-
 __device__ __forceinline__ void tile_products(const SensorDev& sm, const TileSmem& ts, int na, int P, int first,
                                               int n, double* __restrict__ weights) {
-    const int np = min(P, n - first);
-    if (np > 0) gather_factors(sm, ts.sdi, ts.sri, na, np * na, ts.sdv);
-    __syncthreads();
-    chain_products(ts.sdv, na, np, first, weights);
+    for (int li = threadIdx.x; li < P; li += blockDim.x) {
+        const int i = first + li;
+        if (i >= n) continue;
+        const uint16_t* row = ts.sdi + (size_t)li * na;
+        double w = 1.0;
+#pragma unroll 8
+        for (int a = 0; a < na; ++a) w = __dmul_rn(w, __ldg(sm.table + (size_t)ts.sri[a] * sm.K + row[a]));
+        weights[i] = w;
+    }
 }
 
 __device__ __forceinline__ void tile_obs_bins(const CastParams& p, const SensorDev& sm, const float* __restrict__ obs,
@@ -842,13 +812,13 @@ struct RunAngles {
 
 // particles per tile (P) and threads per block: P = tile if given, else the
 // most particles whose rays fit one ray per thread; P is capped so that the
-// tile's bins and factors fit kTileSmem bytes
+// tile's bins fit kTileSmem bytes
 constexpr size_t kTileSmem = 48 * 1024;
 inline void product_shape(int na, int block, int tile, int& P, int& threads) {
     if (block <= 0) block = 256;
     if (na <= 0) { P = block; threads = block; return; }   // empty product: weight 1.0
     P = tile > 0 ? tile : (na >= block ? 1 : block / na);
-    int cap = (int)((kTileSmem / sizeof(uint16_t) - (size_t)na) / ((size_t)na * (1 + sizeof(double) / sizeof(uint16_t))));
+    int cap = (int)((kTileSmem / sizeof(uint16_t) - (size_t)na) / (size_t)na);
     if (cap < 1) cap = 1;
     if (P > cap) P = cap;
     int nr = P * na;
