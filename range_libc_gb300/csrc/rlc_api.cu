@@ -868,6 +868,7 @@ struct rlc_batch {
     int nf = 0;
     FilterDev* d_filters = nullptr;
     unsigned* d_queue = nullptr;
+    uint16_t* d_bins = nullptr;   // every filter's n x na range bins
     unsigned total_tiles = 0;
     long long rays = 0;
     int grid = 0;
@@ -887,6 +888,7 @@ struct rlc_batch {
         if (cap) cudaStreamDestroy(cap);
         cudaFree(d_filters);
         cudaFree(d_queue);
+        cudaFree(d_bins);
     }
 
     // (re)build the device filter table for the current schedule
@@ -894,7 +896,12 @@ struct rlc_batch {
         drop_graph();
         struct Item { FilterDev f; double cost; };
         std::vector<Item> items;
-        size_t sm_bytes = 0;
+        if (!d_bins) {
+            size_t total = 0;
+            for (const rlc_filter_desc& d : descs) total += (size_t)d.n_particles * d.n_angles;
+            CUDA_OR_FAIL(cudaMalloc(&d_bins, (total ? total : 1) * sizeof(uint16_t)), "batch range bins");
+        }
+        size_t bin_ofs = 0;
         for (const rlc_filter_desc& d : descs) {
             rlc_method* m = d.method;
             Item it{};
@@ -913,10 +920,11 @@ struct rlc_batch {
             it.f.weights = d.weights;
             it.f.n = d.n_particles;
             it.f.na = d.n_angles;
-            it.f.ppb = tile_particles(d.n_angles, block, tile > 0 ? tile : 32);
+            it.f.bins = d_bins + bin_ofs;
+            bin_ofs += (size_t)d.n_particles * d.n_angles;
+            it.f.ppb = tile > 0 ? tile : 32;   // 32 particles: one full lane set of the product warp
             // heavier tiles first: rays per tile x march length
             it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
-            sm_bytes = std::max(sm_bytes, tile_smem_bytes(it.f.ppb, d.n_angles));
             items.push_back(it);
         }
         std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
@@ -931,7 +939,7 @@ struct rlc_batch {
         int dev = 0, sms = 0, per_sm = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = batch_occupancy(block, sm_bytes, rm_only, layout, prefetch, &per_sm);
+        if (e == cudaSuccess) e = batch_occupancy(block, 0, rm_only, layout, prefetch, &per_sm);
         if (e == cudaSuccess && per_sm <= 0) e = cudaErrorInvalidConfiguration;
         if (e == cudaSuccess && !d_filters) e = cudaMalloc(&d_filters, descs.size() * sizeof(FilterDev));
         if (e == cudaSuccess)
@@ -941,7 +949,7 @@ struct rlc_batch {
         if (e != cudaSuccess) return cuda_fail(e, "batch setup");
         nf = (int)hf.size();
         total_tiles = (unsigned)tiles;
-        smem = sm_bytes;
+        smem = 0;
         long long g = (long long)sms * per_sm;
         if (g > (long long)tiles) g = (long long)tiles;
         grid = (int)(g > 0 ? g : 1);

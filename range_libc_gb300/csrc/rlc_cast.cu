@@ -445,6 +445,54 @@ __device__ __forceinline__ TileSmem tile_layout(unsigned char* base, int P, int 
     return t;
 }
 
+// In-order product of the table factors table[sri(a) * K + bin(a)], a = 0 ..
+// na - 1, as a three-stage software pipeline over groups of kGroup beams: in
+// each step the bins of group g + 2 and the factors of group g + 1 are
+// requested while group g is multiplied, so the dependent bin -> factor ->
+// multiply chain of one group no longer waits on memory.  Groups past na
+// multiply by 1.0, which leaves every double (subnormals included) as is.
+// Registers: 2 x kGroup doubles and 2 x kGroup bins.
+template <int kGroup, class SriF, class BinF>
+__device__ __forceinline__ double product_chain(const SensorDev& sm, int na, SriF sri, BinF bin) {
+    unsigned bx[kGroup], by[kGroup];
+    double f0[kGroup], f1[kGroup];
+    auto load_bins = [&](unsigned* b, int g) {
+#pragma unroll
+        for (int u = 0; u < kGroup; ++u) {
+            const int a = g * kGroup + u;
+            b[u] = a < na ? bin(a) : 0u;
+        }
+    };
+    auto load_factors = [&](double* f, const unsigned* b, int g) {
+#pragma unroll
+        for (int u = 0; u < kGroup; ++u) {
+            const int a = g * kGroup + u;
+            f[u] = a < na ? __ldg(sm.table + (size_t)sri(a) * sm.K + b[u]) : 1.0;
+        }
+    };
+    auto multiply = [&](double w, const double* f) {
+#pragma unroll
+        for (int u = 0; u < kGroup; ++u) w = __dmul_rn(w, f[u]);
+        return w;
+    };
+    const int ng = (na + kGroup - 1) / kGroup;
+    double w = 1.0;
+    load_bins(bx, 0);
+    load_factors(f0, bx, 0);
+    load_bins(bx, 1);
+    for (int g = 0; g < ng; g += 2) {
+        load_bins(by, g + 2);
+        load_factors(f1, bx, g + 1);
+        w = multiply(w, f0);
+        if (g + 1 >= ng) break;
+        load_bins(bx, g + 3);
+        load_factors(f0, by, g + 2);
+        w = multiply(w, f1);
+    }
+    return w;
+}
+
+// one lane per particle; a short unrolled gather keeps the fused kernels' registers low
 __device__ __forceinline__ void tile_products(const SensorDev& sm, const TileSmem& ts, int na, int P, int first,
                                               int n, double* __restrict__ weights) {
     for (int li = threadIdx.x; li < P; li += blockDim.x) {
@@ -481,45 +529,44 @@ __global__ void __launch_bounds__(512) k_eval_sensor(CastParams p, SensorDev sm,
     tile_products(sm, ts, na, P, first, n, outs);
 }
 
-// one tile of the fused update: cast P particles x na beams (ranges in
-// pixels, RangeLib.h:558-612) and bin them into ts.sdi
+// range of ray (particle i, beam a) in pixels (RangeLib.h:558-612)
+template <int KIND, int LAYOUT, int PF>
+__device__ __forceinline__ float cast_ray(const CastParams& p, const float* __restrict__ ins,
+                                          const float* __restrict__ angles, int i, int a, int na, int layout, int pf) {
+    float ax, ay, th;
+    world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1), __ldg(ins + 3 * (size_t)i + 2),
+                  ax, ay, th);
+    const long long ray = (long long)i * na + a;
+    const float h = __fsub_rn(th, __ldg(angles + a));
+    if (KIND >= 0) return cast_one<KIND, LAYOUT, PF>(p, ax, ay, h, ray);
+    if (KIND == kRmOnly) return cast_one<K_RM, LAYOUT, PF>(p, ax, ay, h, ray);   // every filter ray-marches
+    // mixed kinds: dispatch at run time
+    if (p.kind == K_RM) {
+        if (layout == DT_U16)
+            return pf ? cast_one<K_RM, DT_U16, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_U16, 0>(p, ax, ay, h, ray);
+        if (layout == DT_TILED)
+            return pf ? cast_one<K_RM, DT_TILED, kPrefetch>(p, ax, ay, h, ray)
+                      : cast_one<K_RM, DT_TILED, 0>(p, ax, ay, h, ray);
+        return pf ? cast_one<K_RM, DT_LINEAR, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_LINEAR, 0>(p, ax, ay, h, ray);
+    }
+    if (p.kind == K_BL) return cast_one<K_BL, DT_LINEAR, 0>(p, ax, ay, h, ray);
+    return cast_one<K_CDDT, DT_LINEAR, 0>(p, ax, ay, h, ray);
+}
+
+// one tile of the fused update: cast P particles x na beams and bin them into ts.sdi
 template <int KIND, int LAYOUT, int PF>
 __device__ __forceinline__ void tile_cast(const CastParams& p, const SensorDev& sm, const float* __restrict__ ins,
                                           const float* __restrict__ angles, const float* __restrict__ obs,
                                           float* __restrict__ ranges, int n, int na, int P, int first,
                                           const TileSmem& ts, int layout, int pf) {
-    uint16_t* sdi = ts.sdi;
     tile_obs_bins(p, sm, obs, na, ts.sri);
     const int nr = P * na;
     for (int r = threadIdx.x; r < nr; r += blockDim.x) {
-        int li = r / na, a = r - li * na, i = first + li;
+        const int li = r / na, a = r - li * na, i = first + li;
         if (i < n) {
-            float ax, ay, th;
-            world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
-                          __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
-            const long long ray = (long long)i * na + a;
-            const float h = __fsub_rn(th, __ldg(angles + a));
-            float d;
-            if (KIND >= 0) {
-                d = cast_one<KIND, LAYOUT, PF>(p, ax, ay, h, ray);
-            } else if (KIND == kRmOnly) {   // persistent kernel, every filter ray-marches
-                d = cast_one<K_RM, LAYOUT, PF>(p, ax, ay, h, ray);
-            } else {   // persistent kernel, mixed kinds: dispatch at run time
-                if (p.kind == K_RM) {
-                    if (layout == DT_U16) d = pf ? cast_one<K_RM, DT_U16, kPrefetch>(p, ax, ay, h, ray)
-                                                 : cast_one<K_RM, DT_U16, 0>(p, ax, ay, h, ray);
-                    else if (layout == DT_TILED) d = pf ? cast_one<K_RM, DT_TILED, kPrefetch>(p, ax, ay, h, ray)
-                                                        : cast_one<K_RM, DT_TILED, 0>(p, ax, ay, h, ray);
-                    else d = pf ? cast_one<K_RM, DT_LINEAR, kPrefetch>(p, ax, ay, h, ray)
-                                : cast_one<K_RM, DT_LINEAR, 0>(p, ax, ay, h, ray);
-                } else if (p.kind == K_BL) {
-                    d = cast_one<K_BL, DT_LINEAR, 0>(p, ax, ay, h, ray);
-                } else {
-                    d = cast_one<K_CDDT, DT_LINEAR, 0>(p, ax, ay, h, ray);
-                }
-            }
-            if (ranges) ranges[ray] = d;
-            sdi[r] = (uint16_t)sensor_bin(d, sm.K, p.err);
+            const float d = cast_ray<KIND, LAYOUT, PF>(p, ins, angles, i, a, na, layout, pf);
+            if (ranges) ranges[(size_t)i * na + a] = d;
+            ts.sdi[r] = (uint16_t)sensor_bin(d, sm.K, p.err);
         }
     }
     __syncthreads();
@@ -546,36 +593,79 @@ __global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const
 }
 
 // ------------------------------------------------- persistent multi-filter
-// Every block loops: take the next tile index from the device queue, cast
-// the tile's rays (P particles of one filter) and multiply each particle's
-// factors in beam order.  Filters are stored in descending per-tile cost, so
-// heavy tiles are handed out first.  There is no waiting on other blocks: a
-// block that finds the queue exhausted exits.
+// Every block loops: take the next tile index from the device queue and
+// cast the tile's rays (P particles of one filter) into the filter's range
+// bins in global memory; warps take the rays 32 at a time from a
+// shared-memory counter.  The products of a tile's particles (in beam order,
+// up to 32 particles per lane set) are run by warp 0 while the other warps
+// cast the block's next tile -- a product chain is as long as the tile's
+// beam count in dependent double multiplies, and would otherwise idle the
+// block -- and warp 0 joins the cast when it is done.  Filters are stored in
+// descending per-tile cost, so heavy tiles are handed out first.  There is
+// no waiting on other blocks: a block that finds the queue exhausted
+// multiplies its last tile and exits.
+__device__ __forceinline__ void batch_products(const FilterDev& F, int first, int np) {
+    const int lane = threadIdx.x & 31;
+    const float* obs = F.obs;
+    const float inv_s = F.p.world.inv_s;
+    const int K = F.sm.K;
+    unsigned* err = F.p.err;
+    for (int li = lane; li < np; li += 32) {
+        const uint16_t* row = F.bins + (size_t)(first + li) * F.na;
+        F.weights[first + li] = product_chain<4>(
+            F.sm, F.na, [&](int a) { return (unsigned)sensor_bin(__fmul_rn(__ldg(obs + a), inv_s), K, err); },
+            [&](int a) { return (unsigned)row[a]; });
+    }
+}
+
 template <int MODE, int LAYOUT, int PF>
-__global__ void __launch_bounds__(512) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
+__global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
                                                unsigned* __restrict__ queue) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ unsigned s_tile;
+    __shared__ unsigned s_tile, s_next;
     __shared__ int s_f;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool mult = threadIdx.x < 32;   // warp 0 multiplies the previous tile
+    int prev_f = -1, prev_first = 0, prev_np = 0;
     for (;;) {
         if (threadIdx.x == 0) {
-            unsigned t = atomicAdd(queue, 1u);
+            const unsigned t = atomicAdd(queue, 1u);
             s_tile = t;
             int lo = 0, hi = nf - 1;   // last filter with tile_begin <= t
             while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
+                const int mid = (lo + hi + 1) >> 1;
                 if (filters[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
             }
             s_f = lo;
+            s_next = 0u;
         }
         __syncthreads();
         const unsigned t = s_tile;
+        const int f = s_f;
+        if (mult && prev_f >= 0) batch_products(filters[prev_f], prev_first, prev_np);
         if (t >= total_tiles) break;
-        const FilterDev& F = filters[s_f];
-        const int P = F.ppb;
-        fused_tile<MODE, LAYOUT, PF>(F.p, F.sm, F.ins, F.angles, F.obs, F.weights, F.ranges, F.n, F.na, P,
-                             (int)(t - F.tile_begin) * P, tile_layout(smem_raw, P, F.na), F.layout, F.prefetch);
-        __syncthreads();   // before the next tile reuses shared memory and s_tile
+        const FilterDev& F = filters[f];
+        const int P = F.ppb, na = F.na, n = F.n;
+        const int first = (int)(t - F.tile_begin) * P;
+        const int nr = min(P, n - first) * na;
+        uint16_t* bins = F.bins + (size_t)first * na;
+        for (;;) {
+            unsigned base = 0u;
+            if (lane == 0) base = atomicAdd(&s_next, 32u);
+            base = __shfl_sync(full, base, 0);
+            if (base >= (unsigned)nr) break;
+            const int r = (int)base + lane;
+            if (r < nr) {
+                const int li = r / na, a = r - li * na;
+                const float d = cast_ray<MODE, LAYOUT, PF>(F.p, F.ins, F.angles, first + li, a, na, F.layout, F.prefetch);
+                if (F.ranges) F.ranges[(size_t)(first + li) * na + a] = d;
+                bins[r] = (uint16_t)sensor_bin(d, F.sm.K, F.p.err);
+            }
+        }
+        __syncthreads();   // the tile's bins are written; s_tile, s_f and s_next may be reused
+        prev_f = f;
+        prev_first = first;
+        prev_np = min(P, n - first);
     }
 }
 
@@ -883,7 +973,6 @@ int tile_particles(int na, int block, int tile) {
     return P;
 }
 
-size_t tile_smem_bytes(int P, int na) { return tile_smem(P, na); }
 
 cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,
                                unsigned long long* total, cudaStream_t s) {

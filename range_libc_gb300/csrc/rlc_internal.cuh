@@ -102,9 +102,8 @@ cudaError_t launch_eval_sensor(const CastParams& p, const SensorDev& sm, const f
 cudaError_t launch_fused(const CastParams& p, int layout, int pf, const SensorDev& sm, const float* ins,
                          const float* angles, const float* obs, double* weights, int n, int na,
                          int block, int tile, cudaStream_t s);
-// particles per tile the fused kernels use, and the shared memory of such a tile
+// particles per tile the fused kernel uses
 int tile_particles(int na, int block, int tile);
-size_t tile_smem_bytes(int P, int na);
 
 // beam-major fused particle update with a staged shared-memory window of the
 // 8-bit distance transform (RM only): bins[a * n + i] receives each ray's
@@ -130,6 +129,7 @@ struct FilterDev {
     const float* obs;
     float* ranges;            // optional pixel ranges
     double* weights;
+    uint16_t* bins;           // n x na range bins (batch scratch)
     int n, na, ppb;           // particles, beams, particles per tile
     unsigned tile_begin;      // first global tile of this filter
 };
