@@ -194,6 +194,15 @@ def run_reference(args):
     return 0
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from one `ncu --set full` capture
+# of the same workload (profiles/k_fused_corridor2048_pf4000x61.md, profiles/k_batch_uneven32.md)
+FUSED_NCU_TRAFFIC = 511_488
+FUSED_NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"
+BATCH6_NCU_TRAFFIC = 559_306_752 + 32_608_512
+BATCH6_NCU_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 filters "
+                     "(--filters 6); the 32-filter launch is not captured")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -207,6 +216,9 @@ def main():
     ap.add_argument("--filters", type=int, default=32, help="batch workload: number of filters")
     ap.add_argument("--no-plain", action="store_true", help="batch workload: skip the per-call comparisons")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--schedule", default=None,
+                    help="fixed schedule instead of the autotuner (for profiling): fused 'layout,block,prefetch,tile', "
+                         "batch 'layout,prefetch,block,tile'")
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -247,9 +259,12 @@ def main():
         method.eval_sensor_model(obs, ranges, weights, na, n)
         return 2
 
-    # autotune the schedule on this workload, then warm up
+    # autotune the schedule on this workload (or take the given one), then warm up
     if args.workload == "fused":
-        method.autotune(ins, angles, obs, weights)
+        if args.schedule:
+            method.set_schedule(*[int(v) for v in args.schedule.split(",")])
+        else:
+            method.autotune(ins, angles, obs, weights)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -321,7 +336,8 @@ def main():
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / kern_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "peak_source": f"hbm_gbs burst ({peak_kind})",
+                "traffic": FUSED_NCU_TRAFFIC, "traffic_source": FUSED_NCU_SOURCE,
+                "peak_source": f"hbm_gbs burst ({peak_kind})",
                 "algorithmic_bytes_per_launch": alg_bytes, "mean_march_steps_per_ray": total_steps / rays_per_step,
                 "kernel": "k_fused (cast + sensor model)"}
 
@@ -409,10 +425,14 @@ def run_batch(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     # per-filter schedules for the per-filter comparison, one batch schedule for the batch
-    for m, ins, ang, obs, w in filters:
-        m.autotune(ins, ang, obs, w)
+    if not args.no_plain:
+        for m, ins, ang, obs, w in filters:
+            m.autotune(ins, ang, obs, w)
     batch = rl.PyFilterBatch(filters)
-    batch.autotune()
+    if args.schedule:
+        batch.set_schedule(*[int(v) for v in args.schedule.split(",")])
+    else:
+        batch.autotune()
 
     def batched():
         batch.run()
@@ -465,6 +485,16 @@ def run_batch(args):
 
     total_b = max_over_ranks(dist, sum(tb))
     value = ws * rays * args.steps / (total_b / 1e3)
+    # roofline of k_batch: per particle pose in + weight out, per ray one table read + a 2-byte
+    # range bin written and read back + 4 B per distance-transform read
+    steps_total = sum(m.count_steps(wl.ins, wl.angles) for (m, *_), wl in zip(filters, host))
+    alg_bytes = particles * (12 + 8) + rays * (8 + 4) + 4 * steps_total
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (total_b / args.steps / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": BATCH6_NCU_TRAFFIC if len(filters) == 6 else None, "traffic_source": BATCH6_NCU_SOURCE,
+                "peak_source": f"hbm_gbs burst ({peak_kind})", "algorithmic_bytes_per_launch": alg_bytes,
+                "mean_march_steps_per_ray": steps_total / rays, "kernel": "k_batch (persistent cast + products)"}
     line = {
         "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_b / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -478,7 +508,7 @@ def run_batch(args):
         "plain_per_call_rays_per_s": rays * plain_steps / tp,
         "batched_over_plain": (rays * args.steps / (sum(tb) / 1e3)) / (rays * plain_steps / tp),
         "weights_equal_per_filter_fused": same, "weights_equal_plain": same_plain,
-        "gpu_launches": launches, "setup_s": setup_s, "clocks": clk,
+        "gpu_launches": launches, "setup_s": setup_s, "roofline": roofline, "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line))
