@@ -11,8 +11,8 @@
 //    printing (the reference prints, throws std::string or invokes UB);
 //  * OMap(std::string[, float]) (PNG loading) is not provided in C++ -- build
 //    the grid from memory; the Python module loads PNGs;
-//  * GiantLUTCast, serializeJson/Yaml, saveTrace and the radial-pair helpers
-//    are outside this library.
+//  * serializeJson/Yaml and saveTrace are outside this library; CDDT tables
+//    are exported/imported as arrays (compressed_lut(), rlc_cddt_table_load).
 #ifndef RANGELIB_GB300_H
 #define RANGELIB_GB300_H
 
@@ -199,6 +199,18 @@ public:
         }
         return lut;
     }
+    // calc_range_pair (RangeLib.h:1521-1615): ranges at heading and heading + pi
+    std::pair<float, float> calc_range_pair(float x, float y, float heading) {
+        float r = 0.0f, ri = 0.0f;
+        check(rlc_cddt_calc_range_pair(h, x, y, heading, &r, &ri));
+        return std::make_pair(r, ri);
+    }
+    // calc_range_many_radial_optimized (RangeLib.h:616-676)
+    void calc_range_many_radial_optimized(float* ins, float* outs, int num_particles, int num_rays, float min_angle,
+                                          float max_angle) {
+        check(rlc_cddt_calc_range_many_radial(h, ins, outs, num_particles, num_rays, min_angle, max_angle, 0,
+                                              nullptr));
+    }
     std::vector<float> lut_translations() {
         std::vector<int> widths(theta_discretization);
         std::vector<float> trans(theta_discretization);
@@ -206,6 +218,21 @@ public:
         return trans;
     }
     unsigned int theta_discretization;
+};
+
+// GiantLUTCast (RangeLib.h:1772-1904): the 16-bit table is built on the GPU
+class GiantLUTCast : public RangeMethod {
+public:
+    GiantLUTCast(OMap m, float mr, int td) : RangeMethod(std::move(m), mr, RLC_GLT, (unsigned)td), theta_discretization(td) {}
+    int lut_size() { return (int)(map.width * map.height * (unsigned)theta_discretization * sizeof(uint16_t)); }
+    int memory() { return lut_size(); }
+    // the table, giant_lut[x][y][i] at [(x * height + y) * td + i]
+    std::vector<uint16_t> lut() {
+        std::vector<uint16_t> t((size_t)map.width * map.height * theta_discretization);
+        check(rlc_glt_table(h, t.data()));
+        return t;
+    }
+    int theta_discretization;
 };
 
 class RayMarchingGPU : public RangeMethod {

@@ -69,7 +69,8 @@ enum rlc_kind {
     RLC_RM = 1,           /* RayMarching,      RangeLib.h:922-969 */
     RLC_CDDT = 2,         /* CDDTCast,         RangeLib.h:971-1770 */
     RLC_PCDDT = 3,        /* CDDTCast + prune(max_range) (PyCDDTCast + prune, RangeLibc.pyx:253-262) */
-    RLC_RMGPU = 4         /* RayMarchingGPU,   RangeLib.h:774-920 (same kernels as RLC_RM) */
+    RLC_RMGPU = 4,        /* RayMarchingGPU,   RangeLib.h:774-920 (same kernels as RLC_RM) */
+    RLC_GLT = 5           /* GiantLUTCast,     RangeLib.h:1772-1904 (16-bit table built on the device) */
 };
 
 enum rlc_flags {
@@ -110,8 +111,10 @@ RLC_API int rlc_map_edge_map(rlc_map* map, uint8_t* edge_out);
 
 /* ---- range methods ----------------------------------------------------- */
 /* BresenhamsLine(OMap, mr) / RayMarching(OMap, mr) / CDDTCast(OMap, mr, td) /
- * RayMarchingGPU(OMap, mr) constructors.  theta_disc is used by CDDT only.
- * The CDDT table is built on the device. */
+ * RayMarchingGPU(OMap, mr) / GiantLUTCast(OMap, mr, td) constructors.  theta_disc is used by
+ * CDDT and GLT only.  The CDDT table and the GLT table (width x height x td uint16: one ray
+ * march from every cell corner at every angle bin, RangeLib.h:1782-1818) are built on the
+ * device. */
 RLC_API int rlc_method_create(rlc_map* map, int kind, float max_range, unsigned theta_disc, rlc_method** out);
 /* CDDT constructor with caller-supplied cosines and sines of the td discrete
  * angles i * (2*pi/td) (as float).  Used to pin a table to another host's libm. */
@@ -130,6 +133,22 @@ RLC_API int rlc_cddt_table_export(rlc_method* m, int* widths, float* trans, int6
 /* Replace the table (same theta_disc and bin counts), e.g. one exported from the reference. */
 RLC_API int rlc_cddt_table_load(rlc_method* m, const float* trans, const int64_t* bin_len, const float* zeros,
                                 int64_t num_zeros);
+
+/* GiantLUTCast table export: lut[(x * height + y) * td + i] as the reference stores it
+ * (giant_lut[x][y][i], RangeLib.h:1782-1818). */
+RLC_API int rlc_glt_table(rlc_method* m, uint16_t* lut_out);
+
+/* CDDTCast::calc_range_pair(x, y, heading) (RangeLib.h:1521-1615): the ranges at heading and
+ * at heading + pi from one bin search, in grid space.  A bin outside the slice gives
+ * (max_range, max_range) where the reference indexes it unchecked. */
+RLC_API int rlc_cddt_calc_range_pair(rlc_method* m, float x, float y, float heading, float* r, float* r_inv);
+/* CDDTCast::calc_range_many_radial_optimized(ins, outs, n, num_rays, min_angle, max_angle)
+ * (RangeLib.h:616-676): world-frame poses, num_rays beams from min_angle to max_angle, the
+ * first num_rays/3 beams cast in pairs with the beam pi further on.  Positions of a row the
+ * reference does not write keep the caller's values; writes the reference sends past a
+ * particle's row are dropped (the next particle overwrites them there). */
+RLC_API int rlc_cddt_calc_range_many_radial(rlc_method* m, const float* ins, float* outs, int n, int num_rays,
+                                            float min_angle, float max_angle, unsigned flags, void* stream);
 
 /* ---- queries ----------------------------------------------------------- */
 /* RangeMethod::calc_range(x, y, heading) (virtual, RangeLib.h:419): one ray in grid space. */

@@ -27,8 +27,8 @@ REF_SO = os.path.join(HERE, "_ref", "librlc_ref.so")
 REF_FAST_SO = os.path.join(HERE, "_ref", "librlc_ref_fast.so")
 REF_SRC = os.environ.get("RLC_REFERENCE_DIR", "/root/reference")
 
-BL, RM, CDDT = 0, 1, 2
-KINDS = {"bl": BL, "rm": RM, "cddt": CDDT, "pcddt": CDDT}
+BL, RM, CDDT, GLT = 0, 1, 2, 3
+KINDS = {"bl": BL, "rm": RM, "cddt": CDDT, "pcddt": CDDT, "glt": GLT}
 
 _f32p = C.POINTER(C.c_float)
 _f64p = C.POINTER(C.c_double)
@@ -59,7 +59,15 @@ class _Method(C.Structure):
         ("kind", C.c_int), ("width", C.c_int), ("height", C.c_int),
         ("occ", _u8p), ("dt", _f32p), ("cddt", C.c_void_p),
         ("max_range", C.c_float), ("world", _World),
-        ("table", _f64p), ("K", C.c_int),
+        ("table", _f64p), ("K", C.c_int), ("glt", C.c_void_p),
+    ]
+
+
+class _Glt(C.Structure):
+    _fields_ = [
+        ("width", C.c_int), ("height", C.c_int), ("td", C.c_uint), ("max_range", C.c_float),
+        ("td_div_2pi", C.c_float), ("twopi_div_td", C.c_float), ("max_div_limits", C.c_float),
+        ("limits_div_max", C.c_float), ("lut", C.POINTER(C.c_uint16)),
     ]
 
 
@@ -112,6 +120,14 @@ def lib():
         L.orc_world_rays.argtypes = [C.POINTER(_World), _f32p, _f32p, C.c_int, C.c_int, _f32p, _f32p]
         L.orc_mean_steps.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int]
         L.orc_mean_steps.restype = C.c_double
+        L.orc_cddt_calc_range_pair.argtypes = [C.POINTER(_Cddt), C.c_float, C.c_float, C.c_float, _f32p, _f32p]
+        L.orc_cddt_radial.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int, C.c_float, C.c_float]
+        L.orc_glt_build.argtypes = [_f32p, C.c_int, C.c_int, C.c_float, C.c_uint, C.c_int]
+        L.orc_glt_build.restype = C.POINTER(_Glt)
+        L.orc_glt_free.argtypes = [C.POINTER(_Glt)]
+        L.orc_glt_calc_range.argtypes = [C.POINTER(_Glt), C.c_float, C.c_float, C.c_float]
+        L.orc_glt_calc_range.restype = C.c_float
+        L.orc_glt_discretize.argtypes = [C.POINTER(_Glt), C.c_float]
         _lib = L
     return _lib
 
@@ -162,17 +178,22 @@ def world_rays(world, ins, angles=None):
 class OracleMethod:
     """One of the reference's range methods, restated on the CPU.
 
-    kind: 'bl', 'rm', 'cddt' or 'pcddt' (pruned at construction).
+    kind: 'bl', 'rm', 'cddt', 'pcddt' (pruned at construction) or 'glt' (GiantLUTCast with td
+    angle bins, built from the distance transform with ``nthreads`` threads).
     """
 
-    def __init__(self, occ, kind: str, max_range: float, td: int = 108, world=None):
+    def __init__(self, occ, kind: str, max_range: float, td: int = 108, world=None, nthreads: int = 1):
         self.occ = _occ(occ)
         self.width, self.height = self.occ.shape
         self.kind_name = kind
         self.kind = KINDS[kind]
         self.max_range = float(max_range)
         self.world = world_tuple() if world is None else tuple(world)
-        self.dt = edt(self.occ) if self.kind == RM else None
+        self.dt = edt(self.occ) if self.kind in (RM, GLT) else None
+        self.glt = None
+        if self.kind == GLT:
+            self.glt = lib().orc_glt_build(_ptr(self.dt, _f32p), self.width, self.height,
+                                           C.c_float(self.max_range), td, nthreads)
         self.cddt = None
         if self.kind == CDDT:
             self.cddt = lib().orc_cddt_build(_ptr(self.occ, _u8p), self.width, self.height,
@@ -194,11 +215,36 @@ class OracleMethod:
         m.world = _World(*self.world)
         m.table = _ptr(self.table, _f64p) if self.table is not None else None
         m.K = 0 if self.table is None else self.table.shape[0]
+        m.glt = C.cast(self.glt, C.c_void_p) if self.glt is not None else None
 
     def __del__(self):
         if getattr(self, "cddt", None) is not None:
             lib().orc_cddt_free(self.cddt)
             self.cddt = None
+        if getattr(self, "glt", None) is not None:
+            lib().orc_glt_free(self.glt)
+            self.glt = None
+
+    # --- GiantLUTCast table ---
+    def glt_table(self):
+        """The uint16 LUT as an array [width, height, td]."""
+        g = self.glt.contents
+        n = g.width * g.height * g.td
+        return np.ctypeslib.as_array(g.lut, (max(n, 1),))[:n].reshape(g.width, g.height, g.td).copy()
+
+    # --- CDDT radial pairs ---
+    def calc_range_pair(self, x, y, heading):
+        r, ri = C.c_float(), C.c_float()
+        lib().orc_cddt_calc_range_pair(self.cddt, x, y, heading, C.byref(r), C.byref(ri))
+        return r.value, ri.value
+
+    def calc_range_many_radial_optimized(self, num_rays, min_angle, max_angle, ins, outs):
+        """Fills outs [n * num_rays] in place (positions the reference does not write keep their values)."""
+        ins = np.ascontiguousarray(ins, np.float32)
+        assert outs.dtype == np.float32 and outs.flags.c_contiguous and outs.size == ins.shape[0] * num_rays
+        lib().orc_cddt_radial(C.byref(self._m), _ptr(ins, _f32p), _ptr(outs, _f32p), ins.shape[0], num_rays,
+                              min_angle, max_angle)
+        return outs
 
     # --- CDDT table ---
     def prune(self, max_range: float | None = None):
@@ -336,6 +382,9 @@ def ref_lib(fast: bool = False):
         L.ref_cddt_num_bins.argtypes = [vp]
         L.ref_cddt_num_bins.restype = C.c_longlong
         L.ref_cddt_export.argtypes = [vp, _i32p, _f32p, _i64p, _f32p]
+        L.ref_cddt_pair.argtypes = [vp, C.c_float, C.c_float, C.c_float, _f32p, _f32p]
+        L.ref_cddt_radial.argtypes = [vp, _f32p, _f32p, C.c_int, C.c_int, C.c_float, C.c_float]
+        L.ref_glt_slice.argtypes = [vp, C.c_float, _f32p]
         _ref[key] = L
     return _ref[key]
 
@@ -393,6 +442,26 @@ class RefMethod:
 
     def calc_range(self, x, y, h):
         return self.L.ref_calc_range(self.h, x, y, h)
+
+    def calc_range_pair(self, x, y, heading):
+        r, ri = C.c_float(), C.c_float()
+        self.L.ref_cddt_pair(self.h, x, y, heading, C.byref(r), C.byref(ri))
+        return r.value, ri.value
+
+    def calc_range_many_radial_optimized(self, num_rays, min_angle, max_angle, ins, outs):
+        ins = np.ascontiguousarray(ins, np.float32)
+        self.L.ref_cddt_radial(self.h, _ptr(ins, _f32p), _ptr(outs, _f32p), ins.shape[0], num_rays,
+                               min_angle, max_angle)
+        return outs
+
+    def glt_table(self):
+        """The LUT as [width, height, td] (the reference's get_slice per angle bin)."""
+        w, h = self.map.occ.shape
+        out = np.empty((self.td, w, h), np.float32)
+        for i in range(self.td):
+            theta = float(np.float32(i) * np.float32(6.28318530718 / np.float32(self.td)))
+            self.L.ref_glt_slice(self.h, theta, _ptr(out[i], _f32p))
+        return np.moveaxis(out, 0, 2).astype(np.uint16)
 
     def calc_range_many(self, ins):
         ins = np.ascontiguousarray(ins, np.float32)

@@ -11,7 +11,9 @@
 //   BresenhamsLine 691-772, RayMarching 922-969, CDDTCast 971-1770 (+ prune),
 //   RangeMethod::numpy_calc_range 439-480, numpy_calc_range_angles 482-520,
 //   set_sensor_model 523-532, eval_sensor_model 533-555,
-//   calc_range_repeat_angles_eval_sensor_model 558-612.
+//   calc_range_repeat_angles_eval_sensor_model 558-612,
+//   CDDTCast::calc_range_pair 1521-1615, calc_range_many_radial_optimized 616-676,
+//   GiantLUTCast 1772-1904 (+ get_slice).
 #include "includes/RangeLib.h"
 
 #include <cstdint>
@@ -21,9 +23,10 @@ using namespace ranges;
 
 namespace {
 struct RefMethod {
-    int kind;  // 0 BL, 1 RM, 2 CDDT
+    int kind;  // 0 BL, 1 RM, 2 CDDT, 3 GLT
     RangeMethod* m;
     CDDTCast* cddt;
+    GiantLUTCast* glt;
 };
 }  // namespace
 
@@ -83,8 +86,10 @@ void* ref_method_create(void* map, int kind, float max_range, unsigned td) {
     RefMethod* r = new RefMethod();
     r->kind = kind;
     r->cddt = nullptr;
+    r->glt = nullptr;
     if (kind == 0) r->m = new BresenhamsLine(*m, max_range);
     else if (kind == 1) r->m = new RayMarching(*m, max_range);
+    else if (kind == 3) { r->glt = new GiantLUTCast(*m, max_range, (int)td); r->m = r->glt; }
     else { r->cddt = new CDDTCast(*m, max_range, td); r->m = r->cddt; }
     return r;
 }
@@ -157,6 +162,24 @@ void ref_cddt_export(void* h, int* widths, float* trans, long long* bin_len, flo
             for (float v : bin) zeros[z++] = v;
         }
     }
+}
+
+void ref_cddt_pair(void* h, float x, float y, float heading, float* r, float* r_inv) {
+    std::pair<float, float> p = static_cast<RefMethod*>(h)->cddt->calc_range_pair(x, y, heading);
+    *r = p.first;
+    *r_inv = p.second;
+}
+
+void ref_cddt_radial(void* h, float* ins, float* outs, int n, int num_rays, float min_angle, float max_angle) {
+    static_cast<RefMethod*>(h)->cddt->calc_range_many_radial_optimized(ins, outs, n, num_rays, min_angle, max_angle);
+}
+
+// the 16-bit LUT entries of angle bin `theta` as floats, out[x * height + y]
+void ref_glt_slice(void* h, float theta, float* out) {
+    DistanceTransform* d = static_cast<RefMethod*>(h)->glt->get_slice(theta);
+    for (unsigned x = 0; x < d->width; ++x)
+        for (unsigned y = 0; y < d->height; ++y) out[(size_t)x * d->height + y] = d->grid[x][y];
+    delete d;
 }
 
 }  // extern "C"

@@ -521,10 +521,107 @@ void orc_cddt_prune(orc_cddt* c, float max_range) {
 /* ------------------------------------------------------------------ */
 /* RangeMethod batched wrappers, RangeLib.h:439-612                      */
 /* ------------------------------------------------------------------ */
+/* calc_range_pair, RangeLib.h:1521-1615.  The reference indexes the bin with an unchecked
+ * (int) lut_space_y; here a bin outside the slice gives (max_range, max_range).  Its forward
+ * branch tests the occupancy without returning (RangeLib.h:1580), which is kept: the search
+ * goes on. */
+void orc_cddt_calc_range_pair(const orc_cddt* c, float x, float y, float heading, float* r, float* r_inv) {
+    const float mr = c->max_range;
+    int a, fl;
+    float dtheta;
+    *r = mr;
+    *r_inv = mr;
+    if (x != x || y != y || heading != heading) return;
+    orc_cddt_discretize(c, (float)(-1.0 * (double)heading), &a, &dtheta, &fl);
+    float ca = cosf(dtheta), sa = sinf(dtheta);
+    float lx = x * ca - y * sa;
+    float ly = (x * sa + y * ca) + c->trans[a];
+    unsigned li = (unsigned)f2i(ly);
+    if (li >= (unsigned)c->widths[a]) return;
+    int64_t b = c->slice_base[a] + li;
+    const float* bin = c->zeros + c->bin_start[b];
+    int n = (int)(c->bin_start[b + 1] - c->bin_start[b]);
+    int high = n - 1;
+    if (high == -1) return;
+    if (fl) {
+        if (bin[0] > lx) { float d = bin[0] - lx; *r_inv = d < mr ? d : mr; return; }
+        if (bin[high] < lx) { *r = lx - bin[high]; return; }
+        if (cddt_occupied(c, x, y)) { *r = 0.0f; *r_inv = 0.0f; return; }
+        int idx = high;                                 /* last zero point <= lx */
+        while (idx > 0 && bin[idx] > lx) --idx;
+        *r = lx - bin[idx];
+        if (idx + 1 != n) *r_inv = bin[idx + 1] - lx;
+    } else {
+        if (bin[high] < lx) { float d = lx - bin[high]; *r_inv = d < mr ? d : mr; return; }
+        int idx = 0;                                    /* first zero point >= lx */
+        while (idx < high && bin[idx] < lx) ++idx;
+        *r = bin[idx] - lx;
+        if (idx - 1 != -1) *r_inv = lx - bin[idx - 1];
+    }
+}
+
+/* ---- GiantLUTCast, RangeLib.h:1772-1904 (cached constants, 16-bit entries) ---- */
+typedef struct { orc_glt* g; const float* dt; } glt_ctx;
+
+static void glt_rows(void* p, int lo, int hi) {
+    glt_ctx* k = (glt_ctx*)p;
+    orc_glt* g = k->g;
+    for (int x = lo; x < hi; ++x)
+        for (int y = 0; y < g->height; ++y)
+            for (unsigned i = 0; i < g->td; ++i) {
+                float angle = (float)i * g->twopi_div_td;
+                float r = orc_rm_calc_range(k->dt, g->width, g->height, g->max_range, (float)x, (float)y, angle, NULL);
+                r = r < g->max_range ? r : g->max_range;                  /* std::min(max_range, r) */
+                g->lut[((size_t)x * g->height + y) * g->td + i] = (uint16_t)(r * g->limits_div_max);
+            }
+}
+
+orc_glt* orc_glt_build(const float* dt, int width, int height, float max_range, unsigned td, int nthreads) {
+    orc_glt* g = (orc_glt*)calloc(1, sizeof(orc_glt));
+    g->width = width;
+    g->height = height;
+    g->td = td;
+    g->max_range = max_range;
+    g->td_div_2pi = (float)((double)td / ORC_M_2PI);
+    g->twopi_div_td = (float)(ORC_M_2PI / (double)(float)td);
+    g->max_div_limits = max_range / 65535;
+    g->limits_div_max = 65535 / max_range;
+    g->lut = (uint16_t*)malloc((size_t)width * height * td * sizeof(uint16_t) + 1);
+    glt_ctx k = {g, dt};
+    orc_parallel(glt_rows, &k, width, nthreads);
+    return g;
+}
+
+void orc_glt_free(orc_glt* g) {
+    if (!g) return;
+    free(g->lut);
+    free(g);
+}
+
+/* discretize_theta, RangeLib.h:1834-1867 (alternate mod, cached constants, roundf) */
+int orc_glt_discretize(const orc_glt* g, float theta) {
+    int it = 0;
+    if (theta < 0.0) {
+        while (theta < 0.0 && it++ < ORC_MAX_WRAP) theta = (float)((double)theta + ORC_M_2PI);
+    } else if (theta > ORC_M_2PI) {
+        while (theta > ORC_M_2PI && it++ < ORC_MAX_WRAP) theta = (float)((double)theta - ORC_M_2PI);
+    }
+    int rounded = f2i(roundf(theta * g->td_div_2pi));
+    return (int)((unsigned)rounded % g->td);
+}
+
+float orc_glt_calc_range(const orc_glt* g, float x, float y, float heading) {
+    if (x != x || y != y || heading != heading) return g->max_range;
+    if (x < 0 || x >= (float)g->width || y < 0 || y >= (float)g->height) return g->max_range;
+    int b = orc_glt_discretize(g, heading);
+    return g->lut[((size_t)f2i(x) * g->height + f2i(y)) * g->td + b] * g->max_div_limits;
+}
+
 float orc_method_calc_range(const orc_method* m, float x, float y, float heading, int* steps) {
     switch (m->kind) {
     case ORC_BL: return orc_bl_calc_range(m->occ, m->width, m->height, m->max_range, x, y, heading, steps);
     case ORC_RM: return orc_rm_calc_range(m->dt, m->width, m->height, m->max_range, x, y, heading, steps);
+    case ORC_GLT: if (steps) *steps = 1; return orc_glt_calc_range(m->glt, x, y, heading);
     default: return orc_cddt_calc_range(m->cddt, x, y, heading, steps);
     }
 }
@@ -569,6 +666,37 @@ static void numpy_range_body(void* p, int lo, int hi) {
 void orc_numpy_calc_range(const orc_method* m, const float* ins, float* outs, int n, int nthreads) {
     batch_ctx b = {m, ins, NULL, NULL, outs, NULL, NULL, 0, make_world(&m->world)};
     orc_parallel(numpy_range_body, &b, n, nthreads);
+}
+
+/* calc_range_many_radial_optimized, RangeLib.h:616-676.  The reference writes in this order
+ * per particle: for a = 0..P (P = num_rays / 3.0): row[a] = r(a), row[a + K] = r_inv(a);
+ * then row[a] = calc_range(a) for a = P+1..K-1, with K = roundf((num_rays - 1) * pi /
+ * (max - min)) and the heading offset accumulated as angle += step.  It is restated
+ * literally, with writes outside the row dropped. */
+void orc_cddt_radial(const orc_method* m, const float* ins, float* outs, int n, int num_rays,
+                     float min_angle, float max_angle) {
+    world_consts k = make_world(&m->world);
+    float step = (max_angle - min_angle) / (float)(num_rays - 1);
+    int max_pair = (int)((double)(float)num_rays / 3.0);
+    float off_f = (float)(((double)num_rays - 1.0) * ORC_M_PI / (double)(max_angle - min_angle));
+    int off = f2i(roundf(off_f));
+    for (int i = 0; i < n; ++i) {
+        float ax, ay, th;
+        world_to_grid(&m->world, &k, ins + 3 * (size_t)i, &ax, &ay, &th);
+        float* row = outs + (size_t)i * num_rays;
+        float angle = min_angle;
+        for (int a = 0; a <= max_pair; ++a) {
+            float r, ri;
+            orc_cddt_calc_range_pair(m->cddt, ax, ay, th - angle, &r, &ri);
+            if (a >= 0 && a < num_rays) row[a] = r * k.s;
+            if (a + off >= 0 && a + off < num_rays) row[a + off] = ri * k.s;
+            angle += step;
+        }
+        for (int a = max_pair + 1; a < off; ++a) {
+            if (a < num_rays) row[a] = orc_cddt_calc_range(m->cddt, ax, ay, th - angle, NULL) * k.s;
+            angle += step;
+        }
+    }
 }
 
 static void raw_range_body(void* p, int lo, int hi) {

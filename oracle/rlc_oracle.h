@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-enum { ORC_BL = 0, ORC_RM = 1, ORC_CDDT = 2 };
+enum { ORC_BL = 0, ORC_RM = 1, ORC_CDDT = 2, ORC_GLT = 3 };
 
 /* World parameters of an OMap (RangeLib.h:134-141). */
 typedef struct orc_world {
@@ -52,6 +52,18 @@ typedef struct orc_cddt {
     int64_t total_bins;
 } orc_cddt;
 
+/* GiantLUTCast (RangeLib.h:1772-1904): lut[(x * height + y) * td + i], uint16. */
+typedef struct orc_glt {
+    int width, height;
+    unsigned td;
+    float max_range;
+    float td_div_2pi;        /* theta_discretization_div_M_2PI (float member) */
+    float twopi_div_td;      /* M_2PI_div_theta_discretization (float member) */
+    float max_div_limits;    /* max_range / 65535 */
+    float limits_div_max;    /* 65535 / max_range */
+    uint16_t* lut;
+} orc_glt;
+
 /* A range method over one map. */
 typedef struct orc_method {
     int kind;                /* ORC_BL, ORC_RM, ORC_CDDT */
@@ -63,6 +75,7 @@ typedef struct orc_method {
     orc_world world;
     const double* table;     /* sensor model, K x K row-major (borrowed) */
     int K;
+    orc_glt* glt;            /* GLT: borrowed table */
 } orc_method;
 
 /* ---- map preprocessing ---- */
@@ -89,6 +102,23 @@ int64_t orc_cddt_num_zeros(const orc_cddt* c);
 /* Replace the table of c by a caller-provided CSR table (same td/widths). */
 int orc_cddt_load(orc_cddt* c, const int* widths, const float* trans,
                   const int64_t* bin_len, const float* zeros, int64_t nzeros);
+
+/* calc_range_pair (RangeLib.h:1521-1615): ranges at heading and heading + pi from one bin search. */
+void orc_cddt_calc_range_pair(const orc_cddt* c, float x, float y, float heading, float* r, float* r_inv);
+/* calc_range_many_radial_optimized (RangeLib.h:616-676), world frame, m->kind == ORC_CDDT.
+ * Positions of a particle's row that the reference does not write are left as they are;
+ * writes that the reference sends past the row (into the next particle's row, which that
+ * particle then overwrites, or past the array) are dropped. */
+void orc_cddt_radial(const orc_method* m, const float* ins, float* outs, int n, int num_rays,
+                     float min_angle, float max_angle);
+
+/* ---- GiantLUTCast ---- */
+/* Build from the distance transform: one RayMarching cast from each cell corner (x, y) at each
+ * of the td angles, clamped to max_range and stored as uint16 (RangeLib.h:1782-1818). */
+orc_glt* orc_glt_build(const float* dt, int width, int height, float max_range, unsigned td, int nthreads);
+void orc_glt_free(orc_glt* g);
+int orc_glt_discretize(const orc_glt* g, float theta);
+float orc_glt_calc_range(const orc_glt* g, float x, float y, float heading);
 
 /* ---- batched RangeMethod API (RangeLib.h:439-612) ---- */
 float orc_method_calc_range(const orc_method* m, float x, float y, float heading, int* steps);

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -42,6 +43,15 @@ int cuda_fail(cudaError_t e, const char* what) {
     } while (0)
 
 constexpr double kM2Pi = 6.28318530718;   // RangeLib.h:61
+constexpr double kMPi = 3.14159265358979323846;   // M_PI
+
+// float -> int with C truncation, saturating, NaN -> 0 (as the device's cvt.rzi.s32.f32)
+inline int host_f2i(float v) {
+    if (v != v) return 0;
+    if (v >= 2147483648.0f) return INT_MAX;
+    if (v <= -2147483904.0f) return INT_MIN;
+    return (int)v;
+}
 constexpr double kEps = 0.00001;          // RangeLib.h:60
 
 }  // namespace
@@ -129,6 +139,9 @@ struct rlc_method {
     float* d_cos = nullptr;
     float* d_sin = nullptr;
     CddtBuild tab;
+    // GiantLUTCast
+    uint16_t* d_lut = nullptr;
+    float max_div_limits = 0.0f, limits_div_max = 0.0f;
     // sensor model
     double* d_table = nullptr;
     int K = 0;
@@ -161,6 +174,7 @@ struct rlc_method {
         cudaFree(d_err);
         cudaFree(d_trig);
         cudaFree(d_bins);
+        cudaFree(d_lut);
         if (map) map->release();
     }
 
@@ -183,6 +197,10 @@ struct rlc_method {
         p.cddt.cosv = d_cos;
         p.cddt.sinv = d_sin;
         p.cddt.slice_base = tab.slice_base;
+        p.glt.lut = d_lut;
+        p.glt.td = td;
+        p.glt.td_div_2pi = td_div_2pi;
+        p.glt.max_div_limits = max_div_limits;
         p.cddt.bin_start = tab.bin_start;
         p.cddt.zeros = tab.zeros;
         p.world = world;
@@ -390,28 +408,56 @@ int rlc_map_edge_map(rlc_map* map, uint8_t* edge_out) {
     return finish_launch(e, "edge map");
 }
 
+// GiantLUTCast constructor (RangeLib.h:1782-1818; cached constants, 16-bit entries): the
+// angles i * M_2PI_div_theta_discretization, their host-libm cosf/sinf, and one ray march
+// per (cell corner, angle) on the device
+static int glt_build(rlc_method* m, const float* cos_tab, const float* sin_tab) {
+    cddt_constants(m, cos_tab, sin_tab);   // td_div_2pi, twopi_div_td and the per-angle cos/sin
+    m->max_div_limits = m->mr / 65535;
+    m->limits_div_max = 65535 / m->mr;
+    const size_t cells = (size_t)m->map->W * m->map->H;
+    int rc = upload((void**)&m->d_cos, m->h_cos.data(), m->td * sizeof(float), "GLT cos");
+    if (!rc) rc = upload((void**)&m->d_sin, m->h_sin.data(), m->td * sizeof(float), "GLT sin");
+    if (rc) return rc;
+    cudaError_t e = cudaMalloc(&m->d_lut, (cells * m->td ? cells * m->td : 1) * sizeof(uint16_t));
+    if (e != cudaSuccess) {
+        m->d_lut = nullptr;
+        return fail(RLC_ERR_NOMEM, "GiantLUTCast table of %zu bytes: %s", cells * m->td * sizeof(uint16_t),
+                    cudaGetErrorString(e));
+    }
+    CastParams p = m->params();
+    p.map.dt = m->map->d_dt;
+    e = launch_glt_build(p.map, m->mr, m->td, m->d_cos, m->d_sin, m->limits_div_max, m->d_lut, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    return e == cudaSuccess ? RLC_OK : cuda_fail(e, "GiantLUTCast construction");
+}
+
 static int method_create(rlc_map* map, int kind, float max_range, unsigned td, const float* cos_tab,
                          const float* sin_tab, rlc_method** out) {
     if (!out) return fail(RLC_ERR_ARG, "null output handle");
     *out = nullptr;
     if (!map) return fail(RLC_ERR_ARG, "null map handle");
-    if (kind < RLC_BL || kind > RLC_RMGPU) return fail(RLC_ERR_ARG, "unknown method kind %d", kind);
+    if (kind < RLC_BL || kind > RLC_GLT) return fail(RLC_ERR_ARG, "unknown method kind %d", kind);
     if (!std::isfinite(max_range)) return fail(RLC_ERR_ARG, "max_range must be finite");
     bool cddt = kind == RLC_CDDT || kind == RLC_PCDDT;
+    const bool glt = kind == RLC_GLT;
     if (cddt && td < 2) return fail(RLC_ERR_ARG, "theta_discretization %u must be >= 2", td);
+    if (glt && td < 1) return fail(RLC_ERR_ARG, "theta_discretization must be >= 1");
+    if (glt && !(max_range > 0.0f)) return fail(RLC_ERR_ARG, "GiantLUTCast needs max_range > 0");
     rlc_method* m = new rlc_method();
     map->retain();
     m->map = map;
     m->kind = kind;
-    m->dkind = kind == RLC_BL ? K_BL : (cddt ? K_CDDT : K_RM);
+    m->dkind = kind == RLC_BL ? K_BL : (cddt ? K_CDDT : (glt ? K_GLT : K_RM));
     m->mr = max_range;
-    m->td = cddt ? td : 0;
+    m->td = (cddt || glt) ? td : 0;
     m->world = world_consts(map->world);
     int rc = RLC_OK;
     cudaError_t e = cudaMalloc(&m->d_err, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(m->d_err, 0, sizeof(unsigned));
     if (e != cudaSuccess) rc = cuda_fail(e, "method state");
-    if (!rc && m->dkind == K_RM) rc = map->ensure_dt();
+    if (!rc && (m->dkind == K_RM || glt)) rc = map->ensure_dt();
+    if (!rc && glt) rc = glt_build(m, cos_tab, sin_tab);
     if (!rc && cddt) {
         cddt_constants(m, cos_tab, sin_tab);
         rc = upload((void**)&m->d_widths, m->h_widths.data(), td * sizeof(int), "cddt widths");
@@ -444,7 +490,8 @@ int rlc_method_create(rlc_map* map, int kind, float max_range, unsigned theta_di
 
 int rlc_method_create_cddt_trig(rlc_map* map, int kind, float max_range, unsigned theta_disc,
                                 const float* cos_tab, const float* sin_tab, rlc_method** out) {
-    if (kind != RLC_CDDT && kind != RLC_PCDDT) return fail(RLC_ERR_ARG, "trig tables apply to CDDT kinds");
+    if (kind != RLC_CDDT && kind != RLC_PCDDT && kind != RLC_GLT)
+        return fail(RLC_ERR_ARG, "trig tables apply to CDDT and GLT kinds");
     if (!cos_tab || !sin_tab) return fail(RLC_ERR_ARG, "null trig table");
     return method_create(map, kind, max_range, theta_disc, cos_tab, sin_tab, out);
 }
@@ -546,6 +593,79 @@ int rlc_method_set_trig_override(rlc_method* m, const float* trig, int64_t count
     if (!trig || count <= 0) return RLC_OK;
     if (int rc = upload((void**)&m->d_trig, trig, (size_t)count * 2 * sizeof(float), "trig override")) return rc;
     m->trig_count = count;
+    return RLC_OK;
+}
+
+int rlc_glt_table(rlc_method* m, uint16_t* lut_out) {
+    if (int rc = check_method(m)) return rc;
+    if (m->dkind != K_GLT) return fail(RLC_ERR_STATE, "not a GiantLUTCast method");
+    if (!lut_out) return fail(RLC_ERR_ARG, "null output");
+    const size_t n = (size_t)m->map->W * m->map->H * m->td;
+    if (n) CUDA_OR_FAIL(cudaMemcpy(lut_out, m->d_lut, n * sizeof(uint16_t), cudaMemcpyDeviceToHost), "GLT export");
+    return RLC_OK;
+}
+
+int rlc_cddt_calc_range_pair(rlc_method* m, float x, float y, float heading, float* r, float* r_inv) {
+    if (int rc = check_method(m)) return rc;
+    if (m->dkind != K_CDDT) return fail(RLC_ERR_STATE, "calc_range_pair applies to CDDT methods");
+    if (!r || !r_inv) return fail(RLC_ERR_ARG, "null output");
+    void* st;
+    if (int rc = m->stage(2 * sizeof(float), &st)) return rc;
+    CastParams p = m->params();
+    CUDA_OR_FAIL(launch_cddt_pair(p, x, y, heading, (float*)st, 0), "calc_range_pair");
+    float h[2];
+    CUDA_OR_FAIL(cudaMemcpy(h, st, sizeof(h), cudaMemcpyDeviceToHost), "calc_range_pair");
+    *r = h[0];
+    *r_inv = h[1];
+    return RLC_OK;
+}
+
+// the loop constants of calc_range_many_radial_optimized (RangeLib.h:636-646) and the
+// heading offset of each loop index, accumulated as the reference does (angle += step)
+static void radial_plan(int num_rays, float min_angle, float max_angle, int* mp, int* off, std::vector<float>* ang) {
+    const float step = (max_angle - min_angle) / (float)(num_rays - 1);
+    *mp = (int)((double)(float)num_rays / 3.0);
+    const float off_f = (float)(((double)num_rays - 1.0) * kMPi / (double)(max_angle - min_angle));
+    *off = host_f2i(std::round(off_f));
+    const int A = std::max(*mp + 1, *off);
+    ang->resize(A > 0 ? A : 1);
+    float angle = min_angle;
+    for (int a = 0; a < A; ++a) {
+        (*ang)[a] = angle;
+        angle += step;
+    }
+}
+
+int rlc_cddt_calc_range_many_radial(rlc_method* m, const float* ins, float* outs, int n, int num_rays,
+                                    float min_angle, float max_angle, unsigned flags, void* stream) {
+    if (int rc = check_method(m)) return rc;
+    if (m->dkind != K_CDDT) return fail(RLC_ERR_STATE, "calc_range_many_radial_optimized applies to CDDT methods");
+    if (n < 0 || num_rays < 0) return fail(RLC_ERR_ARG, "negative size");
+    if ((long long)n * num_rays == 0) return RLC_OK;
+    if (!ins || !outs) return fail(RLC_ERR_ARG, "null array");
+    int mp = 0, off = 0;
+    std::vector<float> ang;
+    radial_plan(num_rays, min_angle, max_angle, &mp, &off, &ang);
+    if ((long long)ang.size() > (1ll << 24)) return fail(RLC_ERR_ARG, "beam offset %d out of range", off);
+    cudaStream_t s = (cudaStream_t)stream;
+    CastParams p = m->params();
+    const size_t b_ang = align256(ang.size() * sizeof(float));
+    const size_t b_in = (flags & RLC_DEVICE_PTRS) ? 0 : align256((size_t)n * 3 * sizeof(float));
+    const size_t b_out = (flags & RLC_DEVICE_PTRS) ? 0 : (size_t)n * num_rays * sizeof(float);
+    void* st;
+    if (int rc = m->stage(b_ang + b_in + b_out, &st)) return rc;
+    float* d_ang = (float*)st;
+    CUDA_OR_FAIL(cudaMemcpyAsync(d_ang, ang.data(), ang.size() * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    if (flags & RLC_DEVICE_PTRS)
+        return finish_launch(launch_cddt_radial(p, ins, d_ang, outs, n, num_rays, mp, off, s), "radial");
+    float* d_in = (float*)((char*)st + b_ang);
+    float* d_out = (float*)((char*)st + b_ang + b_in);
+    CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
+    // positions the reference does not write keep the caller's values
+    CUDA_OR_FAIL(cudaMemcpyAsync(d_out, outs, b_out, cudaMemcpyHostToDevice, s), "H2D");
+    CUDA_OR_FAIL(launch_cddt_radial(p, d_in, d_ang, d_out, n, num_rays, mp, off, s), "radial");
+    CUDA_OR_FAIL(cudaMemcpyAsync(outs, d_out, b_out, cudaMemcpyDeviceToHost, s), "D2H");
+    CUDA_OR_FAIL(cudaStreamSynchronize(s), "radial");
     return RLC_OK;
 }
 
@@ -717,7 +837,7 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
                     int64_t* total_steps) {
     if (int rc = check_method(m)) return rc;
     if (!total_steps) return fail(RLC_ERR_ARG, "null output");
-    if (m->dkind == K_CDDT) return fail(RLC_ERR_STATE, "step counts apply to RM and BL");
+    if (m->dkind == K_CDDT || m->dkind == K_GLT) return fail(RLC_ERR_STATE, "step counts apply to RM and BL");
     if (n < 0 || na < 0) return fail(RLC_ERR_ARG, "negative size");
     *total_steps = 0;
     if ((long long)n * na == 0) return RLC_OK;

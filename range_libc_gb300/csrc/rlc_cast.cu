@@ -322,10 +322,103 @@ __device__ __forceinline__ float cddt_cast_warp(const CastParams& p, bool active
     return r;
 }
 
+// ------------------------------------------------------- GiantLUTCast
+// discretize_theta, RangeLib.h:1834-1867 (alternate mod, cached constants, roundf)
+__device__ __forceinline__ int glt_discretize(const GltDev& g, float theta, unsigned* err) {
+    int it = 0;
+    if (theta < 0.0f) {
+        while (theta < 0.0f) {
+            if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
+            theta = __double2float_rn(__dadd_rn((double)theta, kM2Pi));
+        }
+    } else if ((double)theta > kM2Pi) {
+        while ((double)theta > kM2Pi) {
+            if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
+            theta = __double2float_rn(__dsub_rn((double)theta, kM2Pi));
+        }
+    }
+    const int rounded = __float2int_rz(roundf(__fmul_rn(theta, g.td_div_2pi)));
+    return (int)((unsigned)rounded % g.td);
+}
+
+// GiantLUTCast::calc_range, RangeLib.h:1869-1881; NaN arguments give max_range
+__device__ __forceinline__ float glt_cast(const CastParams& p, float x, float y, float heading) {
+    if (isnan(x) || isnan(y) || isnan(heading)) return p.mr;
+    if (x < 0.0f || x >= __int2float_rn(p.map.W) || y < 0.0f || y >= __int2float_rn(p.map.H)) return p.mr;
+    const GltDev& g = p.glt;
+    const int b = glt_discretize(g, heading, p.err);
+    const size_t cell = (size_t)__float2int_rz(x) * p.map.H + __float2int_rz(y);
+    return __fmul_rn(__int2float_rn(__ldg(g.lut + cell * g.td + b)), g.max_div_limits);
+}
+
+// one ray per (cell corner, angle bin), angle bins fastest: lut[(x * H + y) * td + i]
+__global__ void __launch_bounds__(256) k_glt_build(MapDev m, float mr, unsigned td, const float* __restrict__ cosv,
+                                                   const float* __restrict__ sinv, float limits_div_max,
+                                                   uint16_t* __restrict__ lut, long long total) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long cell = idx / td;
+    const int i = (int)(idx - cell * td);
+    const int x = (int)(cell / m.H), y = (int)(cell - (long long)x * m.H);
+    float r = rm_cast<DT_LINEAR, 0>(m, mr, __int2float_rn(x), __int2float_rn(y), __ldg(cosv + i), __ldg(sinv + i));
+    r = r < mr ? r : mr;   // std::min(max_range, r)
+    lut[idx] = (uint16_t)__float2uint_rz(__fmul_rn(r, limits_div_max));
+}
+
+// -------------------------------------------- CDDT radial pairs
+// calc_range_pair, RangeLib.h:1521-1615: the ranges at heading and at
+// heading + pi from one bin search.  A bin outside the slice gives
+// (max_range, max_range) (the reference indexes it unchecked); the forward
+// branch's occupancy test has no effect in the reference and is omitted.
+__device__ void cddt_pair(const CastParams& p, float x, float y, float heading, float& r, float& ri) {
+    const CddtDev& c = p.cddt;
+    const float mr = p.mr;
+    r = mr;
+    ri = mr;
+    if (isnan(x) || isnan(y) || isnan(heading)) return;
+    int a;
+    bool fl;
+    cddt_discretize(c, -heading, a, fl, p.err);
+    const float ca = __ldg(c.cosv + a), sa = __ldg(c.sinv + a);
+    const float lx = __fsub_rn(__fmul_rn(x, ca), __fmul_rn(y, sa));
+    const float ly = __fadd_rn(__fadd_rn(__fmul_rn(x, sa), __fmul_rn(y, ca)), __ldg(c.trans + a));
+    const unsigned li = (unsigned)__float2int_rz(ly);
+    if (li >= (unsigned)__ldg(c.widths + a)) return;
+    const unsigned b = __ldg(c.slice_base + a) + li;
+    const unsigned lo = __ldg(c.bin_start + b);
+    const int n = (int)(__ldg(c.bin_start + b + 1) - lo);
+    const float* bin = c.zeros + lo;
+    const int high = n - 1;
+    if (high == -1) return;
+    const float first = __ldg(bin), last = __ldg(bin + high);
+    if (fl) {
+        if (first > lx) { ri = ref_minf(mr, __fsub_rn(first, lx)); return; }
+        if (last < lx) { r = __fsub_rn(lx, last); return; }
+        const bool occ = (x > -1.0f) && (y > -1.0f) && occ_at(p.map, __float2int_rz(x), __float2int_rz(y));
+        if (occ) { r = 0.0f; ri = 0.0f; return; }
+        const int idx = bound_g(bin, n, lx, true) - 1;   // last zero point <= lx
+        r = __fsub_rn(lx, __ldg(bin + idx));
+        if (idx + 1 != n) ri = __fsub_rn(__ldg(bin + idx + 1), lx);
+    } else {
+        if (last < lx) { ri = ref_minf(mr, __fsub_rn(lx, last)); return; }
+        const int idx = bound_g(bin, n, lx, false);        // first zero point >= lx
+        r = __fsub_rn(__ldg(bin + idx), lx);
+        if (idx != 0) ri = __fsub_rn(lx, __ldg(bin + idx - 1));
+    }
+}
+
+__global__ void k_cddt_pair(CastParams p, float x, float y, float heading, float* out) {
+    float r, ri;
+    cddt_pair(p, x, y, heading, r, ri);
+    out[0] = r;
+    out[1] = ri;
+}
+
 // ------------------------------------------------------------- dispatch
 template <int KIND, int LAYOUT, int PF = 0>
 __device__ __forceinline__ float cast_one(const CastParams& p, float x, float y, float h, long long ray) {
     if (KIND == K_CDDT) return cddt_cast(p, x, y, h);
+    if (KIND == K_GLT) return glt_cast(p, x, y, h);
     float c, s;
     if (p.trig) {
         c = p.trig[2 * ray];
@@ -356,6 +449,43 @@ __device__ __forceinline__ int sensor_bin(float v, int K, unsigned* err) {
     v = ref_minf(ref_maxf(v, 0.0f), hi);
     if (isnan(v)) { atomicOr(err, F_NAN_INDEX); return 0; }
     return __float2int_rz(v);
+}
+
+// Which write of calc_range_many_radial_optimized's loops stays at row
+// position q: the single-cast loop (P < q < K) writes last; otherwise the
+// later of pair iteration q's forward write and pair iteration q - K's
+// inverse write (each pair iteration writes forward, then inverse).
+// Returns 2a for the forward write of iteration a, 2a + 1 for the inverse.
+__device__ __forceinline__ int radial_last_write(int q, int mp, int off) {
+    int key = -1;
+    if (q >= 0 && q <= mp) key = 2 * q;
+    const int ai = q - off;
+    if (ai >= 0 && ai <= mp && 2 * ai + 1 > key) key = 2 * ai + 1;
+    return key;
+}
+
+// one thread per (particle i, loop index a), a < max(mp + 1, off)
+__global__ void __launch_bounds__(256) k_cddt_radial(CastParams p, const float* __restrict__ ins,
+                                                     const float* __restrict__ angles, float* __restrict__ outs,
+                                                     int n, int nr, int mp, int off, int A) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)n * A) return;
+    const int i = (int)(g / A), a = (int)(g - (long long)i * A);
+    float ax, ay, th;
+    world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1), __ldg(ins + 3 * (size_t)i + 2),
+                  ax, ay, th);
+    const float h = __fsub_rn(th, __ldg(angles + a));
+    float* row = outs + (size_t)i * nr;
+    if (a <= mp) {
+        float r, ri;
+        cddt_pair(p, ax, ay, h, r, ri);
+        if (a < nr && radial_last_write(a, mp, off) == 2 * a) row[a] = __fmul_rn(r, p.world.s);
+        const int q = a + off;
+        if (q >= 0 && q < nr && !(q > mp && q < off) && radial_last_write(q, mp, off) == 2 * a + 1)
+            row[q] = __fmul_rn(ri, p.world.s);
+    } else if (a < off && a < nr) {
+        row[a] = __fmul_rn(cddt_cast(p, ax, ay, h), p.world.s);
+    }
 }
 
 // ---------------------------------------------------------------- kernels
@@ -550,6 +680,7 @@ __device__ __forceinline__ float cast_ray(const CastParams& p, const float* __re
         return pf ? cast_one<K_RM, DT_LINEAR, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_LINEAR, 0>(p, ax, ay, h, ray);
     }
     if (p.kind == K_BL) return cast_one<K_BL, DT_LINEAR, 0>(p, ax, ay, h, ray);
+    if (p.kind == K_GLT) return cast_one<K_GLT, DT_LINEAR, 0>(p, ax, ay, h, ray);
     return cast_one<K_CDDT, DT_LINEAR, 0>(p, ax, ay, h, ray);
 }
 
@@ -875,6 +1006,7 @@ cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
         return F<K_RM, DT_LINEAR, 0>::run(args...);
     }
     if (kind == K_BL) return F<K_BL, DT_LINEAR, 0>::run(args...);
+    if (kind == K_GLT) return F<K_GLT, DT_LINEAR, 0>::run(args...);
     if (pf) return F<K_CDDT, DT_LINEAR, 1>::run(args...);   // warp-cooperative bin search
     return F<K_CDDT, DT_LINEAR, 0>::run(args...);
 }
@@ -1026,6 +1158,28 @@ cudaError_t launch_fused_staged(const CastParams& p, const SensorDev& sm, const 
     e = set_smem(k_bm_weights, wsmem);
     if (e != cudaSuccess) return e;
     k_bm_weights<<<blocks_for(n, PB), 128, wsmem, s>>>(p, sm, obs, bins, n, na, PB, weights);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_glt_build(const MapDev& map, float mr, unsigned td, const float* cosv, const float* sinv,
+                             float limits_div_max, uint16_t* lut, cudaStream_t s) {
+    const long long total = (long long)map.W * map.H * td;
+    if (total <= 0) return cudaSuccess;
+    k_glt_build<<<blocks_for(total, 256), 256, 0, s>>>(map, mr, td, cosv, sinv, limits_div_max, lut, total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cddt_pair(const CastParams& p, float x, float y, float heading, float* out, cudaStream_t s) {
+    k_cddt_pair<<<1, 1, 0, s>>>(p, x, y, heading, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cddt_radial(const CastParams& p, const float* ins, const float* angles, float* outs, int n,
+                               int num_rays, int mp, int off, cudaStream_t s) {
+    const int A = mp + 1 > off ? mp + 1 : off;
+    const long long total = (long long)n * A;
+    if (total <= 0 || num_rays <= 0) return cudaSuccess;
+    k_cddt_radial<<<blocks_for(total, 256), 256, 0, s>>>(p, ins, angles, outs, n, num_rays, mp, off, A);
     return cudaGetLastError();
 }
 

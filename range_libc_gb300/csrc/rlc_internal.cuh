@@ -22,7 +22,7 @@ struct rlc_method;
 
 namespace rlc {
 
-enum Kind : int { K_BL = 0, K_RM = 1, K_CDDT = 2 };
+enum Kind : int { K_BL = 0, K_RM = 1, K_CDDT = 2, K_GLT = 3 };
 
 // error flags a kernel can raise (ORed into a per-method device word)
 enum DevFlag : unsigned {
@@ -56,6 +56,14 @@ struct CddtDev {
     const float* zeros;
 };
 
+// GiantLUTCast table (RangeLib.h:1772-1904): lut[(x * H + y) * td + i]
+struct GltDev {
+    const uint16_t* lut;
+    unsigned td;
+    float td_div_2pi;         // theta_discretization / M_2PI, as float
+    float max_div_limits;     // max_range / 65535
+};
+
 struct WorldDev {
     float inv_s, s, rc, ox, oy, sa, ca;
 };
@@ -65,6 +73,7 @@ struct CastParams {
     float mr;
     MapDev map;
     CddtDev cddt;
+    GltDev glt;
     WorldDev world;
     const float* trig;        // optional per-ray (cos, sin) override (parity mode)
     unsigned* err;            // device error word
@@ -113,6 +122,18 @@ int tile_particles(int na, int block, int tile);
 cudaError_t launch_fused_staged(const CastParams& p, const SensorDev& sm, const float* ins, const float* angles,
                                 const float* obs, double* weights, int n, int na, int chunks,
                                 uint16_t* bins, cudaStream_t s);
+
+// GiantLUTCast construction: one ray march (linear DT, the given per-angle
+// cos/sin) from every cell corner at every angle bin, clamped to max_range
+// and stored as uint16 (RangeLib.h:1782-1818)
+cudaError_t launch_glt_build(const MapDev& map, float mr, unsigned td, const float* cosv, const float* sinv,
+                             float limits_div_max, uint16_t* lut, cudaStream_t s);
+// CDDT calc_range_pair of one grid-frame query (RangeLib.h:1521-1615): out[0] = r, out[1] = r_inv
+cudaError_t launch_cddt_pair(const CastParams& p, float x, float y, float heading, float* out, cudaStream_t s);
+// calc_range_many_radial_optimized (RangeLib.h:616-676) for world-frame poses:
+// beam a < max(mp + 1, off) at heading offset angles[a]; see k_cddt_radial
+cudaError_t launch_cddt_radial(const CastParams& p, const float* ins, const float* angles, float* outs, int n,
+                               int num_rays, int mp, int off, cudaStream_t s);
 
 // march steps of world-frame repeat-angle rays (RM and BL), summed into *total
 cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,

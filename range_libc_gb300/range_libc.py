@@ -485,8 +485,41 @@ class PyCDDTCast(_RangeMethod):
         call("rlc_cddt_table_load", self._h, trans.ctypes.data_as(_lib._f32p), bin_len.ctypes.data_as(_lib._i64p),
              zeros.ctypes.data_as(_lib._f32p), len(zeros))
 
-    def calc_range_many_radial_optimized(self, num_rays, min_angle, max_angle, ins, outs):
-        raise NotImplementedError("calc_range_many_radial_optimized is not part of the GPU path")
+    def calc_range_pair(self, x: float, y: float, heading: float):
+        """CDDTCast::calc_range_pair (RangeLib.h:1521-1615): (range at heading, range at heading + pi)."""
+        r, ri = C.c_float(), C.c_float()
+        call("rlc_cddt_calc_range_pair", self._h, float(x), float(y), float(heading), C.byref(r), C.byref(ri))
+        return r.value, ri.value
+
+    def calc_range_many_radial_optimized(self, num_rays: int, min_angle: float, max_angle: float, ins, outs) -> None:
+        """CDDTCast::calc_range_many_radial_optimized (RangeLib.h:616-676; RangeLibc.pyx:275-277):
+        world-frame poses ins[n, 3], outs[n * num_rays]; the first num_rays / 3 beams are cast in
+        pairs with the beam pi further on.  Positions the reference leaves unwritten keep their values."""
+        pi, di = _arg(ins, np.float32, 2, "ins")
+        po, do = _arg(outs, np.float32, 1, "outs")
+        flags, stream = _flags_stream([di, do], ins)
+        n = ins.shape[0]
+        if outs.shape[0] != n * int(num_rays):
+            raise ValueError("outs must hold len(ins) * num_rays ranges")
+        call("rlc_cddt_calc_range_many_radial", self._h, pi, po, n, int(num_rays), float(min_angle), float(max_angle),
+             flags, stream)
+
+
+class PyGiantLUTCast(_RangeMethod):
+    """GiantLUTCast (RangeLib.h:1772-1904; RangeLibc.pyx:288-312): a width x height x td table of
+    16-bit ranges, built on the GPU by one ray march from every cell corner at every angle bin;
+    each query is one table read."""
+    _kind = _lib.RLC_GLT
+
+    def __init__(self, Map: PyOMap, max_range: float, theta_disc: int, *, trig=None):
+        super().__init__(Map, max_range, theta_disc, _trig=trig)
+
+    def lut(self) -> np.ndarray:
+        """The table as uint16 [width, height, td] (giant_lut[x][y][i])."""
+        w, h = self.map.width(), self.map.height()
+        out = np.empty((w, h, self.theta_disc), np.uint16)
+        call("rlc_glt_table", self._h, out.ctypes.data_as(C.POINTER(C.c_uint16)))
+        return out
 
 
 class PyRayMarchingGPU(_RangeMethod):
@@ -667,7 +700,7 @@ def library_path() -> str:
 
 
 __all__ = [
-    "PyOMap", "PyBresenhamsLine", "PyRayMarching", "PyCDDTCast", "PyRayMarchingGPU", "PyNull",
+    "PyOMap", "PyBresenhamsLine", "PyRayMarching", "PyCDDTCast", "PyGiantLUTCast", "PyRayMarchingGPU", "PyNull",
     "PyFilterBatch", "USE_CACHED_TRIG", "USE_ALTERNATE_MOD", "USE_CACHED_CONSTANTS", "USE_FAST_ROUND",
     "NO_INLINE", "USE_LRU_CACHE", "LRU_CACHE_SIZE", "SHOULD_USE_CUDA",
 ]

@@ -12,7 +12,10 @@ sensor tables, what the reference's own classes return:
     BresenhamsLine, RayMarching, CDDTCast and pruned CDDTCast;
   * numpy_calc_range_angles, eval_sensor_model and
     calc_range_repeat_angles_eval_sensor_model on a particle-filter step;
-  * CDDT tables (compressed_lut, lut_translations), unpruned and pruned.
+  * CDDT tables (compressed_lut, lut_translations), unpruned and pruned;
+  * CDDTCast::calc_range_pair and calc_range_many_radial_optimized on the
+    particle-filter map and poses;
+  * a GiantLUTCast table (giant_lut) and its calc_range queries.
 
 Alongside, it stores the per-ray cosf/sinf of every BL/RM heading and the
 cosf/sinf of every CDDT slice angle as this host's libm computes them, so a
@@ -149,6 +152,36 @@ def case_particle_filter(out):
         out[f"pf/{kind}/fused"] = m.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs)
 
 
+def case_pairs_radial_glt(out):
+    wl = W.particle_filter_step(side=256, n_particles=200, n_beams=31, max_range_px=100.0, seed=9,
+                                origin=(-1.5, -0.75))
+    world = tuple(float(np.float32(v)) for v in wl.world)
+    rmap = O.RefMap(wl.occ, world=world)
+    rng = np.random.default_rng(404)
+    q = np.stack([rng.uniform(0, 255.99, 3000), rng.uniform(0, 255.99, 3000), rng.uniform(-9, 9, 3000)], 1)
+    q = q.astype(np.float32)
+    q[:300, :2] = np.floor(q[:300, :2]) + 0.5
+    out["pair/ins"] = q
+    for kind in ("cddt", "pcddt"):
+        m = O.RefMethod(rmap, kind, wl.max_range, 108)
+        out[f"pair/{kind}"] = np.array([m.calc_range_pair(*v) for v in q], np.float32)
+        for nr, span in ((31, 1.5), (100, 2.0), (7, 2.0)):
+            lo, hi = np.float32(-span * np.pi / 2), np.float32(span * np.pi / 2)
+            o = np.full(len(wl.ins) * nr + 4 * nr, -7.0, np.float32)
+            m.calc_range_many_radial_optimized(nr, lo, hi, wl.ins, o)
+            out[f"radial/{kind}/{nr}"] = o[: len(wl.ins) * nr]
+            out[f"radial/{kind}/{nr}/span"] = np.array([lo, hi], np.float32)
+    occ = np.ascontiguousarray(W.rect_disk_map(96, 101)[:64, :48])
+    g = O.RefMethod(O.RefMap(occ), "glt", 40.0, 24)
+    out["glt/occ"] = occ
+    out["glt/slice_trig_24"] = slice_trig(24)
+    out["glt/lut"] = g.glt_table()
+    qg = np.stack([rng.uniform(-2, 66, 2000), rng.uniform(-2, 50, 2000), rng.uniform(-20, 20, 2000)], 1)
+    qg = qg.astype(np.float32)
+    out["glt/ins"] = qg
+    out["glt/ranges"] = np.array([g.calc_range(*v) for v in qg], np.float32)
+
+
 def main():
     O.build(reference=True)
     out = {}
@@ -166,6 +199,7 @@ def main():
     for name, occ in maps.items():
         case_map(name, occ, out, mr=60.0, td=108, worlds=worlds)
     case_particle_filter(out)
+    case_pairs_radial_glt(out)
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path}: {len(out)} arrays, {os.path.getsize(path) / 1e6:.2f} MB")

@@ -30,7 +30,8 @@ def test_header_declares_entry_points():
     for must in ("rlc_map_create", "rlc_method_create", "rlc_calc_range_many", "rlc_calc_range_repeat_angles",
                  "rlc_set_sensor_model", "rlc_eval_sensor_model",
                  "rlc_calc_range_repeat_angles_eval_sensor_model", "rlc_cddt_prune", "rlc_batch_run",
-                 "rlc_distance_transform_noalloc"):
+                 "rlc_distance_transform_noalloc", "rlc_glt_table", "rlc_cddt_calc_range_pair",
+                 "rlc_cddt_calc_range_many_radial"):
         assert must in names
 
 

@@ -21,7 +21,8 @@ def gold():
 
 
 def _names(gold):
-    return sorted({k.split("/")[0] for k in gold if k.endswith("/occ") and k.count("/") == 1 and k != "pf/occ"})
+    return sorted({k.split("/")[0] for k in gold
+                   if k.endswith("/occ") and k.count("/") == 1 and k not in ("pf/occ", "glt/occ")})
 
 
 def _bits(a):
@@ -120,3 +121,31 @@ def test_particle_filter_step(rl, gold, kind):
     assert np.array_equal(_bits(w), _bits(gold[f"pf/{kind}/eval"]))
     g.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs, w)
     assert np.array_equal(_bits(w), _bits(gold[f"pf/{kind}/fused"]))
+
+
+@pytest.mark.parametrize("kind", ["cddt", "pcddt"])
+def test_pairs_and_radial(rl, gold, kind):
+    """CDDTCast::calc_range_pair and calc_range_many_radial_optimized against the reference's vectors."""
+    trig = gold["pf/slice_trig_108"]
+    g = rl.PyCDDTCast(_map(rl, gold["pf/occ"], gold["pf/world"]), 100.0, 108, trig=(trig[:, 0], trig[:, 1]))
+    if kind == "pcddt":
+        g.prune()
+    got = np.array([g.calc_range_pair(*v) for v in gold["pair/ins"]], np.float32)
+    assert np.array_equal(_bits(got), _bits(gold[f"pair/{kind}"]))
+    ins = gold["pf/ins"]
+    for nr in (31, 100, 7):
+        lo, hi = gold[f"radial/{kind}/{nr}/span"]
+        out = np.full(len(ins) * nr, -7.0, np.float32)
+        g.calc_range_many_radial_optimized(nr, float(lo), float(hi), ins, out)
+        assert np.array_equal(_bits(out), _bits(gold[f"radial/{kind}/{nr}"])), nr
+
+
+def test_giant_lut(rl, gold):
+    """GiantLUTCast: the GPU-built table and its queries against the reference's."""
+    t = gold["glt/slice_trig_24"]
+    g = rl.PyGiantLUTCast(_map(rl, gold["glt/occ"]), 40.0, 24, trig=(t[:, 0], t[:, 1]))
+    assert np.array_equal(g.lut(), gold["glt/lut"])
+    q = np.ascontiguousarray(gold["glt/ins"])
+    out = np.empty(len(q), np.float32)
+    rl._lib.call("rlc_calc_range_many", g.handle, q.ctypes.data, out.ctypes.data, len(q), rl._lib.RLC_NO_WORLD, None)
+    assert np.array_equal(_bits(out), _bits(gold["glt/ranges"]))

@@ -6,6 +6,8 @@ oracle's (parity mode).  With the device's own sincosf, ranges may differ
 where a last-bit difference of cos/sin moves a ray across a cell corner;
 that is bounded below.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -284,6 +286,65 @@ def test_staged_update_parity(rl, oracle_mod, side, n, mr):
     assert np.array_equal(_bits(r), _bits(ref.calc_range_repeat_angles(ins, wl.angles)))
 
 
+@pytest.mark.parametrize("td", [1, 72, 101])
+def test_giant_lut_parity(rl, oracle_mod, td):
+    """GiantLUTCast: the GPU-built table equals the oracle's; every entry point (world-frame
+    queries with off-map and NaN poses, repeat angles, sensor model, fused) equals the oracle's."""
+    wl = _pf(side=160, n=200, m=31, mr=80.0)
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyGiantLUTCast(m, wl.max_range, td)
+    ref = oracle_mod.OracleMethod(wl.occ, "glt", wl.max_range, td=td, world=m.world, nthreads=os.cpu_count() or 1)
+    assert np.array_equal(g.lut(), ref.glt_table())
+    q = wl.ins.copy()
+    q[:3] = [[np.nan, 0.0, 0.0], [1e6, -1e6, 1.0], [0.0, 0.0, np.nan]]
+    out = np.empty(len(q), np.float32)
+    g.calc_range_many(q, out)
+    assert np.array_equal(_bits(out), _bits(ref.calc_range_many(q)))
+    r = np.empty(len(q) * len(wl.angles), np.float32)
+    g.calc_range_repeat_angles(q, wl.angles, r)
+    assert np.array_equal(_bits(r), _bits(ref.calc_range_repeat_angles(q, wl.angles)))
+    g.set_sensor_model(wl.table)
+    ref.set_sensor_model(wl.table)
+    w = np.empty(len(q), np.float64)
+    g.calc_range_repeat_angles_eval_sensor_model(q, wl.angles, wl.obs, w)
+    assert np.array_equal(_bits(w), _bits(ref.calc_range_repeat_angles_eval_sensor_model(q, wl.angles, wl.obs)))
+
+
+@pytest.mark.parametrize("kind", ["cddt", "pcddt"])
+def test_cddt_pairs_and_radial_parity(rl, oracle_mod, kind):
+    """calc_range_pair and calc_range_many_radial_optimized against the oracle on a larger map,
+    host and device buffers, beam counts whose loops overlap or leave positions unwritten."""
+    torch = pytest.importorskip("torch")
+    wl = _pf(side=512, n=700, m=61, mr=200.0)
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyCDDTCast(m, wl.max_range, 108)
+    ref = oracle_mod.OracleMethod(wl.occ, "cddt", wl.max_range, td=108, world=m.world)
+    if kind == "pcddt":
+        g.prune()
+        ref.prune()
+    q = _queries(wl.occ, 4000, 71, spread=4.0)
+    got = np.array([g.calc_range_pair(*v) for v in q[:1500]], np.float32)
+    exp = np.array([ref.calc_range_pair(*v) for v in q[:1500]], np.float32)
+    assert np.array_equal(_bits(got), _bits(exp))
+    ins = wl.ins.copy()
+    ins[:2] = [[np.nan, 0.0, 0.0], [0.0, 0.0, np.nan]]
+    for nr, span in ((61, 1.5), (1081, 1.5), (100, 2.0), (8, 1.0), (2, 0.5)):
+        lo, hi = float(np.float32(-span * np.pi / 2)), float(np.float32(span * np.pi / 2))
+        out = np.full(len(ins) * nr, -7.0, np.float32)
+        g.calc_range_many_radial_optimized(nr, lo, hi, ins, out)
+        exp = np.full(len(ins) * nr, -7.0, np.float32)
+        ref.calc_range_many_radial_optimized(nr, lo, hi, ins, exp)
+        assert np.array_equal(_bits(out), _bits(exp)), nr
+    dev = torch.device("cuda:0")
+    d_out = torch.full((len(ins) * 61,), -7.0, dtype=torch.float32, device=dev)
+    g.calc_range_many_radial_optimized(61, float(np.float32(-0.75 * np.pi)), float(np.float32(0.75 * np.pi)),
+                                       torch.from_numpy(ins).to(dev), d_out)
+    torch.cuda.synchronize()
+    exp = np.full(len(ins) * 61, -7.0, np.float32)
+    ref.calc_range_many_radial_optimized(61, float(np.float32(-0.75 * np.pi)), float(np.float32(0.75 * np.pi)), ins, exp)
+    assert np.array_equal(_bits(d_out.cpu().numpy()), _bits(exp))
+
+
 def test_fused_many_beams_underflow(rl, oracle_mod):
     """1,081 beams: products reach subnormals and zero; the in-order product stays bit-exact."""
     wl = _pf(n=64, m=1081)
@@ -382,14 +443,17 @@ def test_batch_matches_per_filter_calls(rl, oracle_mod):
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda:0")
     specs = [W.FilterSpec(256, 300, 45, 120.0, 51), W.FilterSpec(512, 40, 700, 250.0, 52),
-             W.FilterSpec(128, 1000, 30, 60.0, 53), W.FilterSpec(256, 7, 300, 90.0, 54)]
-    kinds = ["rm", "bl", "cddt", "rm"]
+             W.FilterSpec(128, 1000, 30, 60.0, 53), W.FilterSpec(256, 7, 300, 90.0, 54),
+             W.FilterSpec(128, 150, 61, 80.0, 55)]
+    kinds = ["rm", "bl", "cddt", "rm", "glt"]
     filters, expect, keep = [], [], []
     for spec, kind in zip(specs, kinds):
         wl = W.batch_filter(spec)
         m = _pymap(rl, wl.occ)
         if kind == "cddt":
             g = rl.PyCDDTCast(m, wl.max_range, 108)
+        elif kind == "glt":
+            g = rl.PyGiantLUTCast(m, wl.max_range, 72)
         else:
             g = (rl.PyBresenhamsLine if kind == "bl" else rl.PyRayMarching)(m, wl.max_range)
         g.set_sensor_model(wl.table)

@@ -20,7 +20,8 @@ def gold():
 
 
 def _names(gold):
-    return sorted({k.split("/")[0] for k in gold if k.endswith("/occ") and k.count("/") == 1 and k != "pf/occ"})
+    return sorted({k.split("/")[0] for k in gold
+                   if k.endswith("/occ") and k.count("/") == 1 and k not in ("pf/occ", "glt/occ")})
 
 
 def _bits(a):
@@ -110,3 +111,30 @@ def test_particle_filter_step(gold, oracle_mod, kind):
     assert np.array_equal(_bits(m.eval_sensor_model(obs, r, na, n)), _bits(gold[f"pf/{kind}/eval"]))
     assert np.array_equal(_bits(m.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs)),
                           _bits(gold[f"pf/{kind}/fused"]))
+
+
+@pytest.mark.parametrize("kind", ["cddt", "pcddt"])
+def test_pairs_and_radial(gold, oracle_mod, kind):
+    """calc_range_pair and calc_range_many_radial_optimized (RangeLib.h:1521-1615, 616-676)."""
+    if not np.array_equal(_host_slice_trig(108), gold["pf/slice_trig_108"]):
+        pytest.skip("this host's cosf/sinf of the slice angles differ from the recorded ones")
+    world = tuple(float(v) for v in gold["pf/world"])
+    m = oracle_mod.OracleMethod(gold["pf/occ"], kind, 100.0, td=108, world=world)
+    got = np.array([m.calc_range_pair(*v) for v in gold["pair/ins"]], np.float32)
+    assert np.array_equal(_bits(got), _bits(gold[f"pair/{kind}"]))
+    ins = gold["pf/ins"]
+    for nr in (31, 100, 7):
+        lo, hi = gold[f"radial/{kind}/{nr}/span"]
+        out = np.full(len(ins) * nr, -7.0, np.float32)
+        m.calc_range_many_radial_optimized(nr, lo, hi, ins, out)
+        assert np.array_equal(_bits(out), _bits(gold[f"radial/{kind}/{nr}"])), nr
+
+
+def test_giant_lut(gold, oracle_mod):
+    """GiantLUTCast table and queries (RangeLib.h:1772-1904)."""
+    if not np.array_equal(_host_slice_trig(24), gold["glt/slice_trig_24"]):
+        pytest.skip("this host's cosf/sinf of the angle bins differ from the recorded ones")
+    m = oracle_mod.OracleMethod(gold["glt/occ"], "glt", 40.0, td=24, nthreads=4)
+    assert np.array_equal(m.glt_table(), gold["glt/lut"])
+    got = np.array([m.calc_range(*v) for v in gold["glt/ins"]], np.float32)
+    assert np.array_equal(_bits(got), _bits(gold["glt/ranges"]))

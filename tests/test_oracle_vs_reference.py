@@ -100,3 +100,51 @@ def test_multithreaded_oracle_equals_single(O):
     a = orc.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=1)
     b = orc.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=7)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("td", [36, 101])
+def test_giant_lut(O, td):
+    """GiantLUTCast: the 16-bit table and its queries (RangeLib.h:1772-1904)."""
+    occ = np.ascontiguousarray(W.rect_disk_map(128, 21)[:128, :96])
+    orc = O.OracleMethod(occ, "glt", 60.0, td=td, nthreads=4)
+    ref = O.RefMethod(O.RefMap(occ), "glt", 60.0, td)
+    assert np.array_equal(orc.glt_table(), ref.glt_table())
+    rng = np.random.default_rng(td)
+    q = np.stack([rng.uniform(-3, 131, 4000), rng.uniform(-3, 99, 4000), rng.uniform(-30, 30, 4000)], 1)
+    q = q.astype(np.float32)
+    q[:5] = [[np.nan, 1, 1], [1, np.nan, 1], [1, 1, np.nan], [127.99, 95.99, 0], [128, 0, 0]]
+    got = np.array([orc.calc_range(*v) for v in q[5:]], np.float32)
+    exp = np.array([ref.calc_range(*v) for v in q[5:]], np.float32)
+    assert np.array_equal(_bits(got), _bits(exp))
+
+
+def test_cddt_calc_range_pair(O):
+    """calc_range_pair (RangeLib.h:1521-1615) on free, occupied and on-zero-point queries."""
+    occ = MAPS["rect_512"]()
+    for kind in ("cddt", "pcddt"):
+        orc = O.OracleMethod(occ, kind, 300.0, td=108)
+        ref = O.RefMethod(O.RefMap(occ), kind, 300.0, 108)
+        rng = np.random.default_rng(3)
+        q = np.stack([rng.uniform(0, 511.99, 20000), rng.uniform(0, 511.99, 20000),
+                      rng.uniform(-12, 12, 20000)], 1).astype(np.float32)
+        q[:2000, :2] = np.floor(q[:2000, :2]) + 0.5      # cell centres, some occupied
+        got = np.array([orc.calc_range_pair(*v) for v in q], np.float32)
+        exp = np.array([ref.calc_range_pair(*v) for v in q], np.float32)
+        assert np.array_equal(_bits(got), _bits(exp)), kind
+
+
+@pytest.mark.parametrize("num_rays,span", [(61, 1.5), (1081, 1.5), (100, 2.0), (10, 1.0), (7, 2.0), (3, 0.6), (2, 1.0)])
+def test_cddt_radial(O, num_rays, span):
+    """calc_range_many_radial_optimized (RangeLib.h:616-676) on the particle-filter workload's poses,
+    including beam counts whose pairs overlap the single casts or leave positions unwritten."""
+    wl = W.particle_filter_step(side=512, n_particles=300, n_beams=61, max_range_px=200.0, origin=(-1.25, -2.5))
+    w = O.world_tuple(*wl.world[:4])
+    orc = O.OracleMethod(wl.occ, "cddt", wl.max_range, td=108, world=w)
+    ref = O.RefMethod(O.RefMap(wl.occ, world=w), "cddt", wl.max_range, 108)
+    lo, hi = np.float32(-span * np.pi / 2), np.float32(span * np.pi / 2)
+    n = len(wl.ins)
+    o_ref = np.full(n * num_rays + 4 * num_rays, -7.0, np.float32)   # room for the reference's row overrun
+    o_orc = np.full(n * num_rays, -7.0, np.float32)
+    ref.calc_range_many_radial_optimized(num_rays, lo, hi, wl.ins, o_ref)
+    orc.calc_range_many_radial_optimized(num_rays, lo, hi, wl.ins, o_orc)
+    assert np.array_equal(_bits(o_orc), _bits(o_ref[: n * num_rays]))
