@@ -209,7 +209,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="fused", choices=["fused", "plain", "batch", "cddt", "learned"])
+    ap.add_argument("--workload", default="fused", choices=["fused", "plain", "batch", "cddt", "learned", "glt", "radial"])
     ap.add_argument("--train-rays", type=int, default=64_000_000, help="learned workload: training rays")
     ap.add_argument("--td", type=int, default=108, help="cddt workload: theta discretization")
     ap.add_argument("--prune", action="store_true", help="cddt workload: pruned table (PCDDT)")
@@ -231,6 +231,10 @@ def main():
         return run_cddt(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "glt":
+        return run_glt(args)
+    if args.workload == "radial":
+        return run_radial(args)
 
     import torch
     import range_libc_gb300.range_libc as rl
@@ -584,6 +588,129 @@ def run_cddt(args):
         "host_equals_device": same, "gpu_launches": launches, "clocks": clk,
         "search": {"per_thread_rays_per_s": n * args.steps / (per_mode[0] / 1e3),
                    "warp_cooperative_rays_per_s": n * args.steps / (per_mode[1] / 1e3), "chosen": int(best)},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(json.dumps(line) + "\n")
+    return 0
+
+
+def run_glt(args):
+    """GiantLUTCast on the 2048^2 rectangles-and-disks map: GPU table build (one ray march per
+    cell corner and angle bin) and 1M-query throughput."""
+    import torch
+    import range_libc_gb300.range_libc as rl
+    from range_libc_gb300 import workloads as W
+
+    rank, ws, dist = dist_init()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    wl = W.cddt_queries(td=args.td)
+    omap = rl.PyOMap(np.ascontiguousarray(wl.occ.T))
+    rl.PyRayMarching(omap, wl.max_range)   # distance transform outside the build timing
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m = rl.PyGiantLUTCast(omap, wl.max_range, args.td)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    w, h = wl.occ.shape
+    build_rays = w * h * args.td
+    ins = torch.from_numpy(wl.ins).to(dev)
+    outs = torch.empty(len(wl.ins), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        m.calc_range_many(ins, outs)
+        return 1
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t, launches = _event_steps(torch, stream, args.steps, flush, step)
+    clk = clocks.stop()
+    total = max_over_ranks(dist, sum(t))
+    n = len(wl.ins)
+    value = ws * n * args.steps / (total / 1e3)
+    peak, peak_kind = load_peaks()
+    # per query: 12 B pose in, 4 B range out, one 2-byte table entry (a 32-B sector in practice)
+    alg = n * (12 + 4 + 2)
+    achieved = alg / (total / args.steps / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u16 table / f32 ranges", "data": "synthetic",
+        "config": {"workload": f"GiantLUTCast td {args.td}, 2048^2 rect/disk map, {n} free-cell queries",
+                   "l2": "flushed before every step (256 MiB write); table > L2"},
+        "table": {"build_s": build_s, "build_rays": build_rays, "build_rays_per_s": build_rays / build_s,
+                  "bytes": build_rays * 2},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": f"hbm_gbs burst ({peak_kind})",
+                     "algorithmic_bytes_per_launch": alg, "kernel": "k_calc_range_many<GLT>"},
+        "gpu_launches": launches, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(json.dumps(line) + "\n")
+    return 0
+
+
+def run_radial(args):
+    """CDDT calc_range_many_radial_optimized on the particle-filter step's map and poses (4,000
+    particles x 61 beams over 270 degrees) against calc_range_repeat_angles of the same beams."""
+    import torch
+    import range_libc_gb300.range_libc as rl
+    from range_libc_gb300 import workloads as W
+
+    rank, ws, dist = dist_init()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    wl = W.particle_filter_step()
+    omap = rl.PyOMap(np.ascontiguousarray(wl.occ.T))
+    omap.set_world(*wl.world[:4])
+    m = rl.PyCDDTCast(omap, wl.max_range, args.td)
+    if args.prune:
+        m.prune()
+    n, na = len(wl.ins), len(wl.angles)
+    lo, hi = float(wl.angles[0]), float(wl.angles[-1])
+    ins = torch.from_numpy(wl.ins).to(dev)
+    ang = torch.from_numpy(wl.angles).to(dev)
+    out_r = torch.empty(n * na, dtype=torch.float32, device=dev)
+    out_a = torch.empty(n * na, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def radial():
+        m.calc_range_many_radial_optimized(na, lo, hi, ins, out_r)
+        return 1
+
+    def angles():
+        m.calc_range_repeat_angles(ins, ang, out_a)
+        return 1
+
+    for _ in range(args.warmup):
+        radial()
+        angles()
+    ta, _ = _event_steps(torch, stream, args.steps, flush, angles)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t, launches = _event_steps(torch, stream, args.steps, flush, radial)
+    clk = clocks.stop()
+    total = max_over_ranks(dist, sum(t))
+    value = ws * n * na * args.steps / (total / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{'PCDDT' if args.prune else 'CDDT'} td {args.td} radial pairs, corridor 2048^2 "
+                               f"@0.05 m/px, {n} particles x {na} beams over 270 deg",
+                   "l2": "flushed before every step (256 MiB write)"},
+        "repeat_angles_rays_per_s": n * na * args.steps / (sum(ta) / 1e3),
+        "radial_over_repeat_angles": sum(ta) / sum(t),
+        "gpu_launches": launches, "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line))
