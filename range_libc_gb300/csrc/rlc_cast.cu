@@ -22,6 +22,17 @@ constexpr double kM2Pi = 6.28318530718;           // RangeLib.h:61 M_2PI
 constexpr double kMPi = 3.14159265358979323846;   // <cmath> M_PI
 constexpr int kBinarySearchThreshold = 64;         // RangeLib.h:62
 constexpr int kMaxWrap = 100000;                   // bound on discretize_theta's loops
+// For a float t, (double)t > M_2PI <=> t > kM2PiDownF (the largest float below
+// M_2PI) and (double)t >= M_PI <=> t >= kMPiUpF (the smallest float above
+// M_PI): the range tests of discretize_theta stay off the FP64 pipe.
+constexpr float kM2PiDownF = 0x1.921fb4p+2f;
+constexpr float kMPiUpF = 0x1.921fb6p+1f;
+// (float)((double)t - M_PI) for every float t in [kMPiUpF, kM2PiDownF] equals
+// (t - kMPiHiF) - kMPiLoF in float arithmetic: the first difference is exact
+// (Sterbenz) and the second rounds like the double expression -- checked for
+// all 8,388,608 floats of the interval (tests/test_float_identities.py).
+constexpr float kMPiHiF = 0x1.921fb6p+1f;     // (float)M_PI
+constexpr float kMPiLoF = -0x1.777a5cp-24f;   // (float)(M_PI - kMPiHiF)
 constexpr int kPrefetch = 8;                        // RM prefetch distance (px) of the prefetching schedule
 constexpr int kAnyKind = -1;                        // fused_tile: kind, layout and prefetch chosen per filter
 constexpr int kRmOnly = -2;                         // fused_tile: every filter ray-marches (LAYOUT, PF given)
@@ -174,16 +185,17 @@ __device__ __forceinline__ void cddt_discretize(const CddtDev& c, float theta, i
             if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
             theta = __double2float_rn(__dadd_rn((double)theta, kM2Pi));
         }
-    } else if ((double)theta > kM2Pi) {
-        while ((double)theta > kM2Pi) {
+    } else if (theta > kM2PiDownF) {
+        while (theta > kM2PiDownF) {
             if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
             theta = __double2float_rn(__dsub_rn((double)theta, kM2Pi));
         }
     }
     bool fl = false;
-    if ((double)theta >= kMPi) {
+    if (theta >= kMPiUpF) {
         fl = true;
-        theta = __double2float_rn(__dsub_rn((double)theta, kMPi));
+        theta = theta <= kM2PiDownF ? __fsub_rn(__fsub_rn(theta, kMPiHiF), kMPiLoF)
+                                    : __double2float_rn(__dsub_rn((double)theta, kMPi));   // after a bounded wrap
     }
     int rounded = __float2int_rz(roundf(__fmul_rn(theta, c.td_div_2pi)));
     if ((unsigned)rounded == (c.td >> 1)) {
@@ -331,8 +343,8 @@ __device__ __forceinline__ int glt_discretize(const GltDev& g, float theta, unsi
             if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
             theta = __double2float_rn(__dadd_rn((double)theta, kM2Pi));
         }
-    } else if ((double)theta > kM2Pi) {
-        while ((double)theta > kM2Pi) {
+    } else if (theta > kM2PiDownF) {
+        while (theta > kM2PiDownF) {
             if (++it > kMaxWrap) { atomicOr(err, F_WRAP_BOUND); break; }
             theta = __double2float_rn(__dsub_rn((double)theta, kM2Pi));
         }
