@@ -9,12 +9,16 @@ cast + sensor-model call (calc_range_repeat_angles_eval_sensor_model).
   value  rays/s with inputs resident in HBM, CUDA-event time of the fused
          kernel per step, L2 flushed (a 256 MiB write) before every step.
   e2e    the same call through the public Python API with host (pinned)
-         numpy buffers: H2D of poses, angles and observations, the kernel
-         and the D2H of the weights inside the timed region.
+         numpy buffers, host<->device transfers inside the timed region: on
+         Grace + Blackwell the kernel reads the poses, angles and
+         observations from host memory and writes the weights back over
+         NVLink-C2C (coherent host access); elsewhere they are copied.
 
 Other workloads (--workload): plain (cast to ranges, then the separate
 sensor model), batch (32 uneven filters in one persistent launch),
-cddt (1M queries, td 108, 2048^2 map), rect_disk (10k BL/RM queries, 512^2).
+cddt (1M queries, td 108/216, 2048^2 map, --prune for PCDDT), glt
+(GiantLUTCast build + 1M queries), radial (CDDT radial pairs), learned
+(the MLP surrogate).
 
 --impl reference times the reference algorithm on the host cores instead
 (the C restatement in oracle/, all threads).  Multi-GPU: every rank runs

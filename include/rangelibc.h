@@ -150,6 +150,15 @@ RLC_API int rlc_cddt_calc_range_pair(rlc_method* m, float x, float y, float head
 RLC_API int rlc_cddt_calc_range_many_radial(rlc_method* m, const float* ins, float* outs, int n, int num_rays,
                                             float min_angle, float max_angle, unsigned flags, void* stream);
 
+/* Host buffers of calls without RLC_DEVICE_PTRS.  RLC_HOST_AUTO (default): where the GPU reads
+ * and writes pageable host memory coherently (Grace + Blackwell over NVLink-C2C,
+ * cudaDevAttrPageableMemoryAccess) the kernels work on the caller's buffers in place; elsewhere
+ * the buffers are staged through device memory.  RLC_HOST_STAGED: always stage.  Process-wide. */
+enum rlc_host_path_mode { RLC_HOST_AUTO = 0, RLC_HOST_STAGED = 1 };
+RLC_API int rlc_set_host_path(int mode);
+/* 1 if host-pointer calls on the current device run in place, 0 if they are staged. */
+RLC_API int rlc_host_path(int* direct);
+
 /* ---- queries ----------------------------------------------------------- */
 /* RangeMethod::calc_range(x, y, heading) (virtual, RangeLib.h:419): one ray in grid space. */
 RLC_API int rlc_calc_range(rlc_method* m, float x, float y, float heading, float* out);

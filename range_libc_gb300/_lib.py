@@ -15,6 +15,7 @@ from .build import LIB_PATH as _LIB_PATH, build as _build_library
 RLC_OK, RLC_ERR_ARG, RLC_ERR_CUDA, RLC_ERR_STATE, RLC_ERR_NOMEM = range(5)
 RLC_BL, RLC_RM, RLC_CDDT, RLC_PCDDT, RLC_RMGPU, RLC_GLT = range(6)
 RLC_DEVICE_PTRS = 1
+RLC_HOST_AUTO, RLC_HOST_STAGED = 0, 1
 RLC_NO_WORLD = 2
 ABI_VERSION = 1
 
@@ -64,6 +65,8 @@ SIGNATURES = {
     "rlc_cddt_table_export": (C.c_int, [_vp, _i32p, _f32p, _i64p, _f32p]),
     "rlc_cddt_table_load": (C.c_int, [_vp, _f32p, _i64p, _f32p, C.c_int64]),
     "rlc_glt_table": (C.c_int, [_vp, C.POINTER(C.c_uint16)]),
+    "rlc_set_host_path": (C.c_int, [C.c_int]),
+    "rlc_host_path": (C.c_int, [_i32p]),
     "rlc_cddt_calc_range_pair": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, _f32p, _f32p]),
     "rlc_cddt_calc_range_many_radial": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_float, C.c_float,
                                                   C.c_uint, _vp]),

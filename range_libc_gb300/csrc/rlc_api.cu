@@ -293,6 +293,28 @@ int check_method(const rlc_method* m) {
     return RLC_OK;
 }
 
+// Host buffers of the host-pointer entry points.  Where the GPU can read and
+// write pageable host memory coherently (Grace + Blackwell over NVLink-C2C:
+// cudaDevAttrPageableMemoryAccess), the kernels run on the caller's buffers
+// in place -- no staging copies; elsewhere the buffers are staged through
+// device memory with one copy each way.
+std::atomic<int> g_host_path{RLC_HOST_AUTO};
+
+bool host_direct() {
+    if (g_host_path.load() == RLC_HOST_STAGED) return false;
+    static std::atomic<int> cached[64];   // per device: 0 unknown, 1 no, 2 yes
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    int c = cached[dev].load();
+    if (c == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) v = 0;
+        c = v ? 2 : 1;
+        cached[dev].store(c);
+    }
+    return c == 2;
+}
+
 int finish_launch(cudaError_t e, const char* what) {
     if (e != cudaSuccess) return cuda_fail(e, what);
     return RLC_OK;
@@ -596,6 +618,18 @@ int rlc_method_set_trig_override(rlc_method* m, const float* trig, int64_t count
     return RLC_OK;
 }
 
+int rlc_set_host_path(int mode) {
+    if (mode != RLC_HOST_AUTO && mode != RLC_HOST_STAGED) return fail(RLC_ERR_ARG, "host path mode %d", mode);
+    g_host_path.store(mode);
+    return RLC_OK;
+}
+
+int rlc_host_path(int* direct) {
+    if (!direct) return fail(RLC_ERR_ARG, "null output");
+    *direct = host_direct() ? 1 : 0;
+    return RLC_OK;
+}
+
 int rlc_glt_table(rlc_method* m, uint16_t* lut_out) {
     if (int rc = check_method(m)) return rc;
     if (m->dkind != K_GLT) return fail(RLC_ERR_STATE, "not a GiantLUTCast method");
@@ -658,6 +692,11 @@ int rlc_cddt_calc_range_many_radial(rlc_method* m, const float* ins, float* outs
     CUDA_OR_FAIL(cudaMemcpyAsync(d_ang, ang.data(), ang.size() * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
     if (flags & RLC_DEVICE_PTRS)
         return finish_launch(launch_cddt_radial(p, ins, d_ang, outs, n, num_rays, mp, off, s), "radial");
+    if (host_direct()) {
+        CUDA_OR_FAIL(launch_cddt_radial(p, ins, d_ang, outs, n, num_rays, mp, off, s), "radial");
+        CUDA_OR_FAIL(cudaStreamSynchronize(s), "radial");
+        return RLC_OK;
+    }
     float* d_in = (float*)((char*)st + b_ang);
     float* d_out = (float*)((char*)st + b_ang + b_in);
     CUDA_OR_FAIL(cudaMemcpyAsync(d_in, ins, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
@@ -687,6 +726,11 @@ int rlc_calc_range_many(rlc_method* m, const float* ins, float* outs, int n, uns
     bool world = !(flags & RLC_NO_WORLD);
     if (flags & RLC_DEVICE_PTRS)
         return finish_launch(launch_calc_range_many(p, cast_layout(m), m->prefetch, world, ins, outs, n, s), "calc_range_many");
+    if (host_direct()) {
+        CUDA_OR_FAIL(launch_calc_range_many(p, cast_layout(m), m->prefetch, world, ins, outs, n, s), "calc_range_many");
+        CUDA_OR_FAIL(cudaStreamSynchronize(s), "calc_range_many");
+        return RLC_OK;
+    }
     size_t bin = align256((size_t)n * 3 * sizeof(float));
     void* st;
     if (int rc = m->stage(bin + (size_t)n * sizeof(float), &st)) return rc;
@@ -711,6 +755,11 @@ int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* a
     CastParams p = m->params();
     if (flags & RLC_DEVICE_PTRS)
         return finish_launch(launch_repeat_angles(p, cast_layout(m), m->prefetch, ins, angles, outs, n, na, s), "repeat_angles");
+    if (host_direct()) {
+        CUDA_OR_FAIL(launch_repeat_angles(p, cast_layout(m), m->prefetch, ins, angles, outs, n, na, s), "repeat_angles");
+        CUDA_OR_FAIL(cudaStreamSynchronize(s), "repeat_angles");
+        return RLC_OK;
+    }
     size_t b0 = align256((size_t)n * 3 * sizeof(float));
     size_t b1 = align256((size_t)na * sizeof(float));
     void* st;
@@ -751,6 +800,11 @@ int rlc_eval_sensor_model(rlc_method* m, const float* obs, const float* ranges, 
     SensorDev sm{m->d_table, m->K};
     if (flags & RLC_DEVICE_PTRS)
         return finish_launch(launch_eval_sensor(p, sm, obs, ranges, outs, na, n, s), "eval_sensor_model");
+    if (host_direct()) {
+        CUDA_OR_FAIL(launch_eval_sensor(p, sm, obs, ranges, outs, na, n, s), "eval_sensor_model");
+        CUDA_OR_FAIL(cudaStreamSynchronize(s), "eval_sensor_model");
+        return RLC_OK;
+    }
     size_t b0 = align256((size_t)na * sizeof(float));
     size_t b1 = align256((size_t)n * na * sizeof(float));
     void* st;
@@ -784,6 +838,11 @@ int rlc_calc_range_repeat_angles_eval_sensor_model(rlc_method* m, const float* i
     if (int rc = check_trig(m, (long long)n * na)) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (flags & RLC_DEVICE_PTRS) return fused_device(m, ins, angles, obs, weights, n, na, s);
+    if (host_direct()) {
+        if (int rc = fused_device(m, ins, angles, obs, weights, n, na, s)) return rc;
+        CUDA_OR_FAIL(cudaStreamSynchronize(s), "fused sensor model");
+        return RLC_OK;
+    }
     size_t b0 = align256((size_t)n * 3 * sizeof(float));
     size_t b1 = align256((size_t)na * sizeof(float));
     size_t b2 = align256((size_t)na * sizeof(float));

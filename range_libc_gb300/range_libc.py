@@ -546,6 +546,21 @@ class PyNull:
         return a, b, c
 
 
+# ---------------------------------------------------------------- host buffers
+def set_host_path(mode: str = "auto") -> None:
+    """'auto': host (numpy) buffers are read and written in place by the kernels where the GPU
+    accesses host memory coherently (Grace + Blackwell, NVLink-C2C), else staged; 'staged':
+    always staged through device memory.  Process-wide."""
+    call("rlc_set_host_path", {"auto": _lib.RLC_HOST_AUTO, "staged": _lib.RLC_HOST_STAGED}[mode])
+
+
+def host_path_direct() -> bool:
+    """True if host-buffer calls on the current device run in place."""
+    v = C.c_int()
+    call("rlc_host_path", C.byref(v))
+    return bool(v.value)
+
+
 # ---------------------------------------------------------------- batch
 class PyFilterBatch:
     """Many particle filters updated by one persistent launch, replayed as a CUDA graph.
@@ -701,7 +716,7 @@ def library_path() -> str:
 
 __all__ = [
     "PyOMap", "PyBresenhamsLine", "PyRayMarching", "PyCDDTCast", "PyGiantLUTCast", "PyRayMarchingGPU", "PyNull",
-    "PyFilterBatch", "USE_CACHED_TRIG", "USE_ALTERNATE_MOD", "USE_CACHED_CONSTANTS", "USE_FAST_ROUND",
+    "PyFilterBatch", "set_host_path", "host_path_direct", "USE_CACHED_TRIG", "USE_ALTERNATE_MOD", "USE_CACHED_CONSTANTS", "USE_FAST_ROUND",
     "NO_INLINE", "USE_LRU_CACHE", "LRU_CACHE_SIZE", "SHOULD_USE_CUDA",
 ]
 

@@ -31,7 +31,7 @@ def test_header_declares_entry_points():
                  "rlc_set_sensor_model", "rlc_eval_sensor_model",
                  "rlc_calc_range_repeat_angles_eval_sensor_model", "rlc_cddt_prune", "rlc_batch_run",
                  "rlc_distance_transform_noalloc", "rlc_glt_table", "rlc_cddt_calc_range_pair",
-                 "rlc_cddt_calc_range_many_radial"):
+                 "rlc_cddt_calc_range_many_radial", "rlc_set_host_path", "rlc_host_path"):
         assert must in names
 
 

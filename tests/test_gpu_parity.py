@@ -544,3 +544,35 @@ def test_results_do_not_depend_on_the_schedule(rl):
     g.calc_range_repeat_angles_eval_sensor_model(ins, ang, obs, w)
     torch.cuda.synchronize()
     assert np.array_equal(w.cpu().numpy(), base_w)
+
+
+def test_host_buffers_in_place_and_staged(rl, oracle_mod):
+    """Host-buffer calls give the same results whether the kernels work on the host buffers in
+    place (coherent host memory access) or on staged device copies; unwritten radial positions
+    keep the caller's values in both."""
+    wl = _pf(n=300, m=61)
+    m = _pymap(rl, wl.occ, wl.world)
+    results = {}
+    for mode in ("auto", "staged"):
+        rl.set_host_path(mode)
+        try:
+            g = rl.PyRayMarching(m, wl.max_range)
+            g.set_sensor_model(wl.table)
+            c = rl.PyCDDTCast(m, wl.max_range, 108)
+            r1 = np.empty(len(wl.ins), np.float32)
+            g.calc_range_many(wl.ins, r1)
+            r2 = np.empty(len(wl.ins) * len(wl.angles), np.float32)
+            g.calc_range_repeat_angles(wl.ins, wl.angles, r2)
+            w1 = np.empty(len(wl.ins), np.float64)
+            g.eval_sensor_model(wl.obs, r2, w1, len(wl.angles), len(wl.ins))
+            w2 = np.empty(len(wl.ins), np.float64)
+            g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, w2)
+            r3 = np.full(len(wl.ins) * 100, -7.0, np.float32)
+            c.calc_range_many_radial_optimized(100, -3.1, 3.1, wl.ins, r3)
+            results[mode] = (r1, r2, w1, w2, r3, g.calc_range(200.5, 100.5, 0.3))
+        finally:
+            rl.set_host_path("auto")
+    for a, b in zip(results["auto"], results["staged"]):
+        assert np.array_equal(np.asarray(a), np.asarray(b))
+    assert (results["auto"][4] == -7.0).any()
+    assert isinstance(rl.host_path_direct(), bool)
