@@ -271,7 +271,10 @@ RLC_API int rlc_learned_sample_rays(rlc_learned* l, long long first_id, unsigned
                                     float* d_t, float* d_range, void* stream);
 RLC_API int rlc_learned_train(rlc_learned* l, int steps, int batch, float lr, unsigned seed, float* final_loss,
                               void* stream);
+/* t of n grid-frame rays by the fused forward kernel (the whole network per 128-ray tile on one SM) */
 RLC_API int rlc_learned_predict(rlc_learned* l, const float* d_xyt, int n, float* d_pred, void* stream);
+/* the same through the layer-by-layer GEMMs of the training path (bit-identical; test reference) */
+RLC_API int rlc_learned_predict_layered(rlc_learned* l, const float* d_xyt, int n, float* d_pred, void* stream);
 RLC_API int rlc_learned_calc_range_repeat_angles(rlc_learned* l, const float* d_ins, const float* d_angles,
                                                  float* d_outs, int n, int num_angles, uint8_t* d_accepted,
                                                  int64_t* n_recast, void* stream);

@@ -91,6 +91,7 @@ SIGNATURES = {
     "rlc_learned_sample_rays": (C.c_int, [_vp, C.c_longlong, C.c_uint, C.c_int, _vp, _vp, _vp, _vp]),
     "rlc_learned_train": (C.c_int, [_vp, C.c_int, C.c_int, C.c_float, C.c_uint, _f32p, _vp]),
     "rlc_learned_predict": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "rlc_learned_predict_layered": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
     "rlc_learned_calc_range_repeat_angles": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp, _i64p, _vp]),
     "rlc_learned_features": (C.c_int, [_vp, _vp, C.c_int, _vp]),
     "rlc_learned_gradients": (C.c_int, [_vp, _vp, _vp, C.c_int, _f32p, _f32p]),

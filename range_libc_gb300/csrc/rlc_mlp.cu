@@ -66,15 +66,24 @@ struct GemmArgs {
     unsigned* err;
 };
 
+// GELU (tanh form).  tanh is the SFU's single-instruction approximation
+// (PTX tanh.approx.f32, relative error about 2^-11, below the BF16 rounding
+// of the activations); training and inference use the same function.
+__device__ __forceinline__ float tanh_sfu(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ float gelu(float z) {
     const float k0 = 0.7978845608028654f, k1 = 0.044715f;
-    return 0.5f * z * (1.0f + tanhf(k0 * (z + k1 * z * z * z)));
+    return 0.5f * z * (1.0f + tanh_sfu(k0 * (z + k1 * z * z * z)));
 }
 
 __device__ __forceinline__ float gelu_grad(float z) {
     const float k0 = 0.7978845608028654f, k1 = 0.044715f;
     float u = k0 * (z + k1 * z * z * z);
-    float th = tanhf(u);
+    float th = tanh_sfu(u);
     return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * k0 * (1.0f + 3.0f * k1 * z * z);
 }
 
@@ -249,6 +258,178 @@ __global__ void k_features(FeatParams fp, const float* __restrict__ xyt, int n, 
         return;
     }
     ray_features(fp, xyt[3 * (size_t)r], xyt[3 * (size_t)r + 1], xyt[3 * (size_t)r + 2], out);
+}
+
+// ------------------------------------------------------ fused forward pass
+// Inference of the whole network for 128 rays per CTA without leaving the SM:
+// the features of one 64-wide K chunk are computed straight into the A
+// operand (shared memory, core-matrix layout), each layer accumulates its
+// 128 x 256 output in TMEM, and the epilogue (bias, BF16 rounding, GELU)
+// writes the next layer's A operand back into shared memory; the output
+// layer is a per-row dot product in the last epilogue.  Only the rays' poses
+// come in and one float per ray goes out (the layer-by-layer path moves
+// ~3.1 KB per ray through HBM).  Weights stream from L2 in 32 KB K chunks.
+// Every MMA operand, rounding point and summation order matches the
+// layer-by-layer path, so the predictions are bit-identical to it.
+// 112 KB of shared memory and 256 TMEM columns per CTA: two CTAs per SM, so
+// one CTA's epilogue or operand loads overlap the other's MMAs.
+constexpr int kFwdThreads = 128;
+constexpr size_t kFwdSmem = 16384 + 32768 + 65536;
+
+// features [64c, 64c + 64) of a ray with inputs u (input d = c / 2,
+// frequencies (c % 2) * 32 ..), as 8 rows of 16 bytes for the core layout
+__device__ __forceinline__ void feature_chunk(const FeatParams& fp, const float* u, int c, uint4* out) {
+    const int d = c >> 1, k0 = (c & 1) * 32;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {   // 4 frequencies (8 values) per 16-byte vector
+        __nv_bfloat162 h[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float sn, cs;
+            sincospif(fp.freq[k0 + 4 * v + q] * u[d], &sn, &cs);
+            h[q] = __floats2bfloat162_rn(sn, cs);
+        }
+        out[v] = *reinterpret_cast<const uint4*>(h);
+    }
+}
+
+__device__ __forceinline__ bool fwd_mma_chunk(uint32_t tmem, uint32_t idesc, uint32_t a0, uint32_t b0, bool first,
+                                              uint32_t mbar, uint32_t& phase) {
+    tc::fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+#pragma unroll
+        for (int ks = 0; ks < tc::kKChunk / 16; ++ks) {
+            const uint64_t ad = tc::make_desc(a0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
+            const uint64_t bd = tc::make_desc(b0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
+            tc::mma_bf16(tmem, ad, bd, idesc, (!first || ks > 0) ? 1u : 0u);
+        }
+        tc::mma_commit(mbar);
+    }
+    const bool w = tc::mbar_wait(mbar, phase);
+    phase ^= 1u;
+    const bool ok = __syncthreads_and(w) != 0;
+    tc::fence_after_sync();
+    return ok;
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, const float* __restrict__ xyt, int n,
+                                                                 const bf16* __restrict__ wbf,
+                                                                 const float* __restrict__ params,
+                                                                 float* __restrict__ y, unsigned* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sA = smem;                  // layer 0: 128 rows x 64 features
+    uint8_t* sB = smem + 16384;          // 256 weight rows x 64
+    uint8_t* sH = smem + 16384 + 32768;  // activations: 4 K chunks of 128 x 64
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = threadIdx.x;         // TMEM lane = ray of the tile
+    if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_addr(&mbar), 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_base, mb = tc::smem_addr(&mbar);
+    const uint32_t idesc = tc::make_idesc(kBM, kBN);
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const int r = blockIdx.x * kBM + row;
+    float u[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const bool live = r < n;
+    if (live) {
+        float sn, cs;
+        sincosf(__ldg(xyt + 3 * (size_t)r + 2), &sn, &cs);
+        u[0] = __ldg(xyt + 3 * (size_t)r) * fp.inv_w;
+        u[1] = __ldg(xyt + 3 * (size_t)r + 1) * fp.inv_h;
+        u[2] = cs;
+        u[3] = sn;
+    }
+    // layer 0: features chunk by chunk
+    for (int c = 0; c < kFeat / tc::kKChunk && ok; ++c) {
+        uint4 f[8];
+        if (live) {
+            feature_chunk(fp, u, c, f);
+        } else {
+#pragma unroll
+            for (int v = 0; v < 8; ++v) f[v] = make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int v = 0; v < 8; ++v) *reinterpret_cast<uint4*>(sA + tc::core_offset(row, v * 8)) = f[v];
+        load_tile(sB, wbf + w_offset(0), kFeat, 0, 0, kBN, c * tc::kKChunk);
+        ok = fwd_mma_chunk(tmem, idesc, tc::smem_addr(sA), tc::smem_addr(sB), c == 0, mb, phase);
+    }
+    float out = 0.0f;
+    for (int l = 0; l < kLayers && ok; ++l) {
+        if (l > 0) {   // hidden layer l: A = activations in sH
+            for (int c = 0; c < kHidden / tc::kKChunk && ok; ++c) {
+                load_tile(sB, wbf + w_offset(l), kHidden, 0, 0, kBN, c * tc::kKChunk);
+                ok = fwd_mma_chunk(tmem, idesc, tc::smem_addr(sH + c * 16384), tc::smem_addr(sB), c == 0, mb, phase);
+            }
+            if (!ok) break;
+        }
+        // epilogue of layer l: z = acc + b, rounded to bf16; h = bf16(GELU(z))
+        const float* bias = params + b_offset(l);
+        const bool last = l == kLayers - 1;
+        float part[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) part[i] = 0.0f;
+        const float* wout = params + kOutW;
+        for (int cb = 0; cb < kHidden; cb += 32) {
+            float v[32];
+            tc::tmem_ld32(lane_addr + cb, v);
+#pragma unroll
+            for (int i = 0; i < 32; i += 2) {
+                const float z0 = v[i] + __ldg(bias + cb + i), z1 = v[i + 1] + __ldg(bias + cb + i + 1);
+                const float2 zf = __bfloat1622float2(__floats2bfloat162_rn(z0, z1));
+                const __nv_bfloat162 hb = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
+                if (last) {   // the output layer's dot product, in k_out_layer's order
+                    const float2 hf = __bfloat1622float2(hb);
+                    part[i] = __fadd_rn(part[i], __fmul_rn(hf.x, __ldg(wout + cb + i)));
+                    part[i + 1] = __fadd_rn(part[i + 1], __fmul_rn(hf.y, __ldg(wout + cb + i + 1)));
+                } else {
+                    const int k = cb + i;
+                    *reinterpret_cast<__nv_bfloat162*>(sH + (k >> 6) * 16384 + tc::core_offset(row, k & 63)) = hb;
+                }
+            }
+        }
+        if (last) {
+#pragma unroll
+            for (int o = 16; o; o >>= 1)
+#pragma unroll
+                for (int i = 0; i < o; ++i) part[i] = __fadd_rn(part[i], part[i + o]);
+            out = __fadd_rn(part[0], __ldg(wout + kHidden));
+        }
+        tc::fence_before_sync();   // TMEM reads done before the next layer's MMAs overwrite it
+    }
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(err, 16u);
+    } else if (live) {
+        y[r] = out;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    (void)lane;
+}
+
+cudaError_t mlp_forward(const FeatParams& fp, const float* xyt, int n, const bf16* wbf, const float* params, float* y,
+                        unsigned* err, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_mlp_forward<<<(n + kBM - 1) / kBM, kFwdThreads, kFwdSmem, s>>>(fp, xyt, n, wbf, params, y, err);
+    return cudaGetLastError();
 }
 
 // output layer: y = H . w + b (fp32)
@@ -767,6 +948,14 @@ int rlc_learned_sample_rays(rlc_learned* L, long long first_id, unsigned seed, i
 
 // Forward only: predicted t for n grid-frame rays (device buffers).
 int rlc_learned_predict(rlc_learned* L, const float* d_xyt, int n, float* d_pred, void* stream) {
+    if (!L || n < 0 || (n > 0 && (!d_xyt || !d_pred))) return lfail(RLC_ERR_ARG, "bad argument");
+    LearnedModel& M = L->m;
+    LTRY(mlp_forward(M.fp, d_xyt, n, M.wbf, M.params, d_pred, M.err, (cudaStream_t)stream), "fused forward");
+    return RLC_OK;
+}
+
+// The same predictions through the training path's layer-by-layer GEMMs (test reference).
+int rlc_learned_predict_layered(rlc_learned* L, const float* d_xyt, int n, float* d_pred, void* stream) {
     if (!L || n < 0 || (n > 0 && (!d_xyt || !d_pred))) return lfail(RLC_ERR_ARG, "bad argument");
     LearnedModel& M = L->m;
     cudaStream_t s = (cudaStream_t)stream;

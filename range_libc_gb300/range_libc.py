@@ -659,10 +659,13 @@ class PyLearnedRM:
              r.data_ptr(), _stream_of(xyt))
         return xyt, t, r
 
-    def predict(self, xyt):
+    def predict(self, xyt, layered: bool = False):
+        """Predicted hit parameter t of grid-frame rays xyt [n, 3] (CUDA): the fused forward kernel,
+        or with layered=True the training path's layer-by-layer GEMMs (bit-identical)."""
         import torch
         out = torch.empty(xyt.shape[0], dtype=torch.float32, device=xyt.device)
-        call("rlc_learned_predict", self._h, xyt.data_ptr(), int(xyt.shape[0]), out.data_ptr(), _stream_of(xyt))
+        call("rlc_learned_predict_layered" if layered else "rlc_learned_predict", self._h, xyt.data_ptr(),
+             int(xyt.shape[0]), out.data_ptr(), _stream_of(xyt))
         return out
 
     def features(self, xyt):

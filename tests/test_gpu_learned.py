@@ -187,3 +187,16 @@ def test_learned_query_recasts_are_exact(rl, learned_setup):
     assert np.array_equal(o[~a], ex[~a])           # recast rays are the exact ranges
     # a hit cell reached at t < max_range can have its corner up to sqrt(2) farther (as in the reference)
     assert np.all(np.isfinite(o)) and np.all(o <= 100.0 + 1.5)
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 5000])
+def test_fused_forward_matches_layered(rl, learned_setup, n):
+    """The fused forward kernel (whole network per 128-ray tile on one SM) gives the layer-by-layer
+    GEMM path's predictions bit for bit, for a trained and a ragged number of rays."""
+    occ, m, rm = learned_setup
+    L = rl.PyLearnedRM(rm, seed=8)
+    L.train(steps=50, batch=4096, lr=2e-3, seed=23)
+    xyt, _, _ = L.sample_rays(n, first_id=77_000_000, seed=5)
+    a = L.predict(xyt).cpu().numpy()
+    b = L.predict(xyt, layered=True).cpu().numpy()
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
