@@ -273,23 +273,23 @@ __global__ void k_features(FeatParams fp, const float* __restrict__ xyt, int n, 
 // layer-by-layer path, so the predictions are bit-identical to it.
 // 112 KB of shared memory and 256 TMEM columns per CTA: two CTAs per SM, so
 // one CTA's epilogue or operand loads overlap the other's MMAs.
-constexpr int kFwdThreads = 128;
+constexpr int kFwdThreads = 256;   // two threads per TMEM lane (row): column halves
 constexpr size_t kFwdSmem = 16384 + 32768 + 65536;
 
-// features [64c, 64c + 64) of a ray with inputs u (input d = c / 2,
-// frequencies (c % 2) * 32 ..), as 8 rows of 16 bytes for the core layout
-__device__ __forceinline__ void feature_chunk(const FeatParams& fp, const float* u, int c, uint4* out) {
-    const int d = c >> 1, k0 = (c & 1) * 32;
+// features [64c + 32h, 64c + 32h + 32) of a ray with inputs u (input d = c / 2,
+// 16 frequencies from (c % 2) * 32 + 16h), as 4 rows of 16 bytes for the core layout
+__device__ __forceinline__ void feature_half_chunk(const FeatParams& fp, const float* u, int c, int h, uint4* out) {
+    const int d = c >> 1, k0 = (c & 1) * 32 + 16 * h;
 #pragma unroll
-    for (int v = 0; v < 8; ++v) {   // 4 frequencies (8 values) per 16-byte vector
-        __nv_bfloat162 h[4];
+    for (int v = 0; v < 4; ++v) {   // 4 frequencies (8 values) per 16-byte vector
+        __nv_bfloat162 hb[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             float sn, cs;
             sincospif(fp.freq[k0 + 4 * v + q] * u[d], &sn, &cs);
-            h[q] = __floats2bfloat162_rn(sn, cs);
+            hb[q] = __floats2bfloat162_rn(sn, cs);
         }
-        out[v] = *reinterpret_cast<const uint4*>(h);
+        out[v] = *reinterpret_cast<const uint4*>(hb);
     }
 }
 
@@ -314,6 +314,11 @@ __device__ __forceinline__ bool fwd_mma_chunk(uint32_t tmem, uint32_t idesc, uin
     return ok;
 }
 
+// bf16 element k (< 256) of row `row` of the activation buffer (4 K chunks in core layout)
+__device__ __forceinline__ uint32_t act_offset(int row, int k) {
+    return (uint32_t)(k >> 6) * 16384u + tc::core_offset(row, k & 63);
+}
+
 __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, const float* __restrict__ xyt, int n,
                                                                  const bf16* __restrict__ wbf,
                                                                  const float* __restrict__ params,
@@ -324,8 +329,9 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
     uint8_t* sA = smem;                  // layer 0: 128 rows x 64 features
     uint8_t* sB = smem + 16384;          // 256 weight rows x 64
     uint8_t* sH = smem + 16384 + 32768;  // activations: 4 K chunks of 128 x 64
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = threadIdx.x;         // TMEM lane = ray of the tile
+    const int warp = threadIdx.x >> 5;
+    const int row = threadIdx.x & 127;   // TMEM lane = ray of the tile (warp % 4 owns lanes 32 (warp % 4) ..)
+    const int half = threadIdx.x >> 7;   // columns [128 half, 128 half + 128) of every layer
     if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
     if (threadIdx.x == 0) {
         tc::mbar_init(tc::smem_addr(&mbar), 1);
@@ -336,7 +342,7 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base, mb = tc::smem_addr(&mbar);
     const uint32_t idesc = tc::make_idesc(kBM, kBN);
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     uint32_t phase = 0;
     bool ok = true;
 
@@ -353,19 +359,18 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
     }
     // layer 0: features chunk by chunk
     for (int c = 0; c < kFeat / tc::kKChunk && ok; ++c) {
-        uint4 f[8];
+        uint4 f[4];
         if (live) {
-            feature_chunk(fp, u, c, f);
+            feature_half_chunk(fp, u, c, half, f);
         } else {
 #pragma unroll
-            for (int v = 0; v < 8; ++v) f[v] = make_uint4(0, 0, 0, 0);
+            for (int v = 0; v < 4; ++v) f[v] = make_uint4(0, 0, 0, 0);
         }
 #pragma unroll
-        for (int v = 0; v < 8; ++v) *reinterpret_cast<uint4*>(sA + tc::core_offset(row, v * 8)) = f[v];
+        for (int v = 0; v < 4; ++v) *reinterpret_cast<uint4*>(sA + tc::core_offset(row, 32 * half + v * 8)) = f[v];
         load_tile(sB, wbf + w_offset(0), kFeat, 0, 0, kBN, c * tc::kKChunk);
         ok = fwd_mma_chunk(tmem, idesc, tc::smem_addr(sA), tc::smem_addr(sB), c == 0, mb, phase);
     }
-    float out = 0.0f;
     for (int l = 0; l < kLayers && ok; ++l) {
         if (l > 0) {   // hidden layer l: A = activations in sH
             for (int c = 0; c < kHidden / tc::kKChunk && ok; ++c) {
@@ -374,49 +379,56 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
             }
             if (!ok) break;
         }
-        // epilogue of layer l: z = acc + b, rounded to bf16; h = bf16(GELU(z))
+        // epilogue of layer l: z = acc + b, rounded to bf16; h = bf16(GELU(z)) into sH
         const float* bias = params + b_offset(l);
-        const bool last = l == kLayers - 1;
-        float part[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) part[i] = 0.0f;
-        const float* wout = params + kOutW;
-        for (int cb = 0; cb < kHidden; cb += 32) {
+        for (int cb = 128 * half; cb < 128 * half + 128; cb += 32) {
             float v[32];
             tc::tmem_ld32(lane_addr + cb, v);
 #pragma unroll
             for (int i = 0; i < 32; i += 2) {
                 const float z0 = v[i] + __ldg(bias + cb + i), z1 = v[i + 1] + __ldg(bias + cb + i + 1);
                 const float2 zf = __bfloat1622float2(__floats2bfloat162_rn(z0, z1));
-                const __nv_bfloat162 hb = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
-                if (last) {   // the output layer's dot product, in k_out_layer's order
-                    const float2 hf = __bfloat1622float2(hb);
-                    part[i] = __fadd_rn(part[i], __fmul_rn(hf.x, __ldg(wout + cb + i)));
-                    part[i + 1] = __fadd_rn(part[i + 1], __fmul_rn(hf.y, __ldg(wout + cb + i + 1)));
-                } else {
-                    const int k = cb + i;
-                    *reinterpret_cast<__nv_bfloat162*>(sH + (k >> 6) * 16384 + tc::core_offset(row, k & 63)) = hb;
-                }
+                *reinterpret_cast<__nv_bfloat162*>(sH + act_offset(row, cb + i)) =
+                    __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
             }
         }
-        if (last) {
+        tc::fence_before_sync();   // TMEM reads done before the next layer's MMAs overwrite it
+    }
+    if (ok) {
+        // output layer on the last activations, in k_out_layer's summation order: partial
+        // sums over j = i (mod 32) in increasing j, then the xor butterfly
+        __syncthreads();
+        if (half == 0 && live) {
+            const float* wout = params + kOutW;
+            float part[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) part[i] = 0.0f;
+            for (int cb = 0; cb < kHidden; cb += 32) {
+#pragma unroll
+                for (int i = 0; i < 32; i += 8) {
+                    const uint4 q = *reinterpret_cast<const uint4*>(sH + act_offset(row, cb + i));
+                    const __nv_bfloat162* hb = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const float2 hf = __bfloat1622float2(hb[e]);
+                        part[i + 2 * e] = __fadd_rn(part[i + 2 * e], __fmul_rn(hf.x, __ldg(wout + cb + i + 2 * e)));
+                        part[i + 2 * e + 1] =
+                            __fadd_rn(part[i + 2 * e + 1], __fmul_rn(hf.y, __ldg(wout + cb + i + 2 * e + 1)));
+                    }
+                }
+            }
 #pragma unroll
             for (int o = 16; o; o >>= 1)
 #pragma unroll
                 for (int i = 0; i < o; ++i) part[i] = __fadd_rn(part[i], part[i + o]);
-            out = __fadd_rn(part[0], __ldg(wout + kHidden));
+            y[r] = __fadd_rn(part[0], __ldg(wout + kHidden));
         }
-        tc::fence_before_sync();   // TMEM reads done before the next layer's MMAs overwrite it
-    }
-    if (!ok) {
-        if (threadIdx.x == 0) atomicOr(err, 16u);
-    } else if (live) {
-        y[r] = out;
+    } else if (threadIdx.x == 0) {
+        atomicOr(err, 16u);
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 256);
-    (void)lane;
 }
 
 cudaError_t mlp_forward(const FeatParams& fp, const float* xyt, int n, const bf16* wbf, const float* params, float* y,
