@@ -509,7 +509,8 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
         "config": {"workload": "32 uneven filters (maps 512-4096 px, RM), one persistent launch as a CUDA graph",
                    "filters": len(filters), "rays_per_step": rays, "particles_per_step": particles,
-                   "schedule": dict(zip(("dt_layout", "prefetch", "block", "tile"), batch.schedule())),
+                   "schedule": dict(zip(("dt_layout", "prefetch", "block", "tile"), batch.schedule()),
+                                    products=batch.product_mode()),
                    "l2": "flushed before every step (256 MiB write); maps total > L2"},
         "particle_updates_per_s": ws * particles * args.steps / (total_b / 1e3),
         "per_filter_fused_rays_per_s": rays * args.steps / (sum(tf) / 1e3),

@@ -248,6 +248,13 @@ RLC_API int rlc_batch_run(rlc_batch* b, void* stream);
  * (0 = 32).  Results are identical under every schedule. */
 RLC_API int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile);
 RLC_API int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, int* block, int* tile);
+/* Where the per-particle products run: RLC_PRODUCTS_OVERLAPPED -- inside the persistent kernel,
+ * warp 0 of a block multiplying its previous tile while the other warps cast the next one;
+ * RLC_PRODUCTS_SEPARATE -- in a second launch over all particles after the cast (both in the
+ * graph).  Weights are identical; rlc_batch_autotune picks the faster. */
+enum rlc_product_mode { RLC_PRODUCTS_OVERLAPPED = 0, RLC_PRODUCTS_SEPARATE = 1 };
+RLC_API int rlc_batch_set_product_mode(rlc_batch* b, int mode);
+RLC_API int rlc_batch_get_product_mode(const rlc_batch* b, int* mode);
 /* Run the batch under each schedule candidate on `stream` and keep the fastest. */
 RLC_API int rlc_batch_autotune(rlc_batch* b, void* stream);
 RLC_API int rlc_batch_destroy(rlc_batch* b);

@@ -99,6 +99,8 @@ SIGNATURES = {
     "rlc_batch_create": (C.c_int, [C.POINTER(FilterDesc), C.c_int, C.c_int, C.POINTER(_vp)]),
     "rlc_batch_run": (C.c_int, [_vp, _vp]),
     "rlc_batch_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "rlc_batch_set_product_mode": (C.c_int, [_vp, C.c_int]),
+    "rlc_batch_get_product_mode": (C.c_int, [_vp, _i32p]),
     "rlc_batch_get_schedule": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p]),
     "rlc_batch_autotune": (C.c_int, [_vp, _vp]),
     "rlc_batch_destroy": (C.c_int, [_vp]),

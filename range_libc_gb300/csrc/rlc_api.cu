@@ -1043,12 +1043,14 @@ struct rlc_batch {
     bool rm_only = true;
     // schedule
     int layout = DT_LINEAR, prefetch = 0, block = 256, tile = 0;
+    bool separate = false;    // products in a second launch instead of inside the persistent kernel
     // built state
     int nf = 0;
     FilterDev* d_filters = nullptr;
     unsigned* d_queue = nullptr;
     uint16_t* d_bins = nullptr;   // every filter's n x na range bins
     unsigned total_tiles = 0;
+    unsigned total_particles = 0;
     long long rays = 0;
     int grid = 0;
     size_t smem = 0;
@@ -1107,9 +1109,12 @@ struct rlc_batch {
             items.push_back(it);
         }
         std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
-        unsigned long long tiles = 0;
+        unsigned long long tiles = 0, parts = 0;
         std::vector<FilterDev> hf;
         for (auto& it : items) {
+            it.f.part_begin = (unsigned)parts;
+            parts += (unsigned long long)it.f.n;
+            if (parts >= 0xffffffffull) return fail(RLC_ERR_ARG, "too many particles in one batch");
             it.f.tile_begin = (unsigned)tiles;
             tiles += (unsigned long long)((it.f.n + it.f.ppb - 1) / it.f.ppb);
             if (tiles >= 0xffffffffull) return fail(RLC_ERR_ARG, "too many tiles in one batch");
@@ -1118,7 +1123,7 @@ struct rlc_batch {
         int dev = 0, sms = 0, per_sm = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = batch_occupancy(block, 0, rm_only, layout, prefetch, &per_sm);
+        if (e == cudaSuccess) e = batch_occupancy(block, 0, rm_only, layout, prefetch, separate, &per_sm);
         if (e == cudaSuccess && per_sm <= 0) e = cudaErrorInvalidConfiguration;
         if (e == cudaSuccess && !d_filters) e = cudaMalloc(&d_filters, descs.size() * sizeof(FilterDev));
         if (e == cudaSuccess)
@@ -1128,6 +1133,7 @@ struct rlc_batch {
         if (e != cudaSuccess) return cuda_fail(e, "batch setup");
         nf = (int)hf.size();
         total_tiles = (unsigned)tiles;
+        total_particles = (unsigned)parts;
         smem = 0;
         long long g = (long long)sms * per_sm;
         if (g > (long long)tiles) g = (long long)tiles;
@@ -1143,7 +1149,7 @@ struct rlc_batch {
             cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned), cap);
             if (e == cudaSuccess)
                 e = launch_batch(d_filters, nf, total_tiles, d_queue, grid, block, smem, rm_only, layout, prefetch,
-                                 cap);
+                                 separate, total_particles, cap);
             cudaGraph_t g = nullptr;
             cudaError_t e2 = cudaStreamEndCapture(cap, &g);
             if (e == cudaSuccess) e = e2;
@@ -1211,6 +1217,19 @@ int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block,
     return b->build();
 }
 
+int rlc_batch_set_product_mode(rlc_batch* b, int mode) {
+    if (!b) return fail(RLC_ERR_ARG, "null batch handle");
+    if (mode != RLC_PRODUCTS_OVERLAPPED && mode != RLC_PRODUCTS_SEPARATE) return fail(RLC_ERR_ARG, "product mode %d", mode);
+    b->separate = mode == RLC_PRODUCTS_SEPARATE;
+    return b->build();
+}
+
+int rlc_batch_get_product_mode(const rlc_batch* b, int* mode) {
+    if (!b || !mode) return fail(RLC_ERR_ARG, "null argument");
+    *mode = b->separate ? RLC_PRODUCTS_SEPARATE : RLC_PRODUCTS_OVERLAPPED;
+    return RLC_OK;
+}
+
 int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, int* block, int* tile) {
     if (!b) return fail(RLC_ERR_ARG, "null batch handle");
     if (dt_layout) *dt_layout = b->layout;
@@ -1232,12 +1251,15 @@ int rlc_batch_autotune(rlc_batch* b, void* stream) {
     const int tiles[3] = {8, 16, 32};
     float best = 1e30f;
     int bl = b->layout, bp = b->prefetch, bb = b->block, bt = b->tile;
+    bool bs = b->separate;
     int rc = RLC_OK;
+    for (int sp = 0; sp < 2 && !rc; ++sp)
     for (int li = 0; li < 3 && !rc; ++li)
         for (int pf = 0; pf < 2 && !rc; ++pf)
             for (int bi = 0; bi < 2 && !rc; ++bi)
                 for (int ti = 0; ti < 3 && !rc; ++ti) {
                     if (!b->rm_only && (li != 0 || pf != 0)) continue;
+                    b->separate = sp != 0;
                     b->layout = li;
                     b->prefetch = pf;
                     b->block = blocks[bi];
@@ -1253,6 +1275,7 @@ int rlc_batch_autotune(rlc_batch* b, void* stream) {
                     if (e != cudaSuccess) rc = cuda_fail(e, "batch autotune");
                     if (!rc && ms < best) {
                         best = ms;
+                        bs = sp != 0;
                         bl = li;
                         bp = pf;
                         bb = blocks[bi];
@@ -1261,6 +1284,7 @@ int rlc_batch_autotune(rlc_batch* b, void* stream) {
                 }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    b->separate = bs;
     b->layout = bl;
     b->prefetch = bp;
     b->block = bb;

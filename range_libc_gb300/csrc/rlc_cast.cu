@@ -761,7 +761,7 @@ __device__ __forceinline__ void batch_products(const FilterDev& F, int first, in
     }
 }
 
-template <int MODE, int LAYOUT, int PF>
+template <int MODE, int LAYOUT, int PF, bool SEPARATE>
 __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
                                                unsigned* __restrict__ queue) {
     __shared__ unsigned s_tile, s_next;
@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ 
         __syncthreads();
         const unsigned t = s_tile;
         const int f = s_f;
-        if (mult && prev_f >= 0) batch_products(filters[prev_f], prev_first, prev_np);
+        if (!SEPARATE && mult && prev_f >= 0) batch_products(filters[prev_f], prev_first, prev_np);
         if (t >= total_tiles) break;
         const FilterDev& F = filters[f];
         const int P = F.ppb, na = F.na, n = F.n;
@@ -810,6 +810,31 @@ __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ 
         prev_first = first;
         prev_np = min(P, n - first);
     }
+}
+
+
+// Products of every particle of the batch in one launch after the cast (the
+// alternative to k_batch's overlapped products): one thread per particle,
+// 32 particles per warp, the bins read back from global memory.
+__global__ void __launch_bounds__(256) k_batch_products(const FilterDev* __restrict__ filters, int nf,
+                                                        unsigned total_particles) {
+    const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total_particles) return;
+    int lo = 0, hi = nf - 1;   // last filter with part_begin <= g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (filters[mid].part_begin <= g) lo = mid; else hi = mid - 1;
+    }
+    const FilterDev& F = filters[lo];
+    const int i = (int)(g - F.part_begin);
+    const float* obs = F.obs;
+    const float inv_s = F.p.world.inv_s;
+    const int K = F.sm.K;
+    unsigned* err = F.p.err;
+    const uint16_t* row = F.bins + (size_t)i * F.na;
+    F.weights[i] = product_chain<8>(
+        F.sm, F.na, [&](int a) { return (unsigned)sensor_bin(__fmul_rn(__ldg(obs + a), inv_s), K, err); },
+        [&](int a) { return (unsigned)row[a]; });
 }
 
 
@@ -1128,18 +1153,22 @@ cudaError_t launch_count_steps(const CastParams& p, const float* ins, const floa
     return cudaGetLastError();
 }
 
-// batch kernel variant for (rm_only, layout, pf)
+// batch kernel variant for (rm_only, layout, pf, separate products)
 typedef void (*BatchKernel)(const FilterDev*, int, unsigned, unsigned*);
-static BatchKernel batch_kernel(bool rm_only, int layout, int pf) {
-    if (!rm_only) return k_batch<kAnyKind, 0, 0>;
+template <bool SEP>
+static BatchKernel batch_kernel_t(bool rm_only, int layout, int pf) {
+    if (!rm_only) return k_batch<kAnyKind, 0, 0, SEP>;
     if (pf) {
-        if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, kPrefetch>;
-        if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, kPrefetch>;
-        return k_batch<kRmOnly, DT_LINEAR, kPrefetch>;
+        if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, kPrefetch, SEP>;
+        if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, kPrefetch, SEP>;
+        return k_batch<kRmOnly, DT_LINEAR, kPrefetch, SEP>;
     }
-    if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, 0>;
-    if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, 0>;
-    return k_batch<kRmOnly, DT_LINEAR, 0>;
+    if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, 0, SEP>;
+    if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, 0, SEP>;
+    return k_batch<kRmOnly, DT_LINEAR, 0, SEP>;
+}
+static BatchKernel batch_kernel(bool rm_only, int layout, int pf, bool separate) {
+    return separate ? batch_kernel_t<true>(rm_only, layout, pf) : batch_kernel_t<false>(rm_only, layout, pf);
 }
 
 cudaError_t launch_fused_staged(const CastParams& p, const SensorDev& sm, const float* ins, const float* angles,
@@ -1195,20 +1224,25 @@ cudaError_t launch_cddt_radial(const CastParams& p, const float* ins, const floa
     return cudaGetLastError();
 }
 
-cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, int* blocks_per_sm) {
-    BatchKernel k = batch_kernel(rm_only, layout, pf);
+cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, bool separate,
+                            int* blocks_per_sm) {
+    BatchKernel k = batch_kernel(rm_only, layout, pf, separate);
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, block, smem);
 }
 
 cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tiles, unsigned* queue, int grid,
-                         int block, size_t smem, bool rm_only, int layout, int pf, cudaStream_t s) {
+                         int block, size_t smem, bool rm_only, int layout, int pf, bool separate,
+                         unsigned total_particles, cudaStream_t s) {
     if (total_tiles == 0 || nf == 0) return cudaSuccess;
-    BatchKernel k = batch_kernel(rm_only, layout, pf);
+    BatchKernel k = batch_kernel(rm_only, layout, pf, separate);
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
     k<<<grid, block, smem, s>>>(d_filters, nf, total_tiles, queue);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || !separate || total_particles == 0) return e;
+    k_batch_products<<<blocks_for(total_particles, 256), 256, 0, s>>>(d_filters, nf, total_particles);
     return cudaGetLastError();
 }
 

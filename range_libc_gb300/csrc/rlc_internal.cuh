@@ -153,15 +153,20 @@ struct FilterDev {
     uint16_t* bins;           // n x na range bins (batch scratch)
     int n, na, ppb;           // particles, beams, particles per tile
     unsigned tile_begin;      // first global tile of this filter
+    unsigned part_begin;      // first global particle of this filter
 };
 // Persistent launch: `grid` blocks of `block` threads draw tiles from *queue
 // (which must be zero) until all `total_tiles` are done.  rm_only selects the
 // kernel specialised for batches whose filters all ray-march, with the
 // distance-transform layout and prefetch given; otherwise every filter's own
-// kind, layout and prefetch are dispatched at run time.
+// kind, layout and prefetch are dispatched at run time.  The per-particle
+// products run overlapped inside the persistent kernel, or (separate) in a
+// second launch over all `total_particles` after the cast.
 cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tiles, unsigned* queue, int grid,
-                         int block, size_t smem, bool rm_only, int layout, int pf, cudaStream_t s);
-cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, int* blocks_per_sm);
+                         int block, size_t smem, bool rm_only, int layout, int pf, bool separate,
+                         unsigned total_particles, cudaStream_t s);
+cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, bool separate,
+                            int* blocks_per_sm);
 
 // ---- CDDT table (rlc_cddt.cu) ----
 struct CddtBuild {

@@ -597,6 +597,15 @@ class PyFilterBatch:
     def set_schedule(self, dt_layout: int = 0, prefetch: int = 0, block: int = 0, tile: int = 0) -> None:
         call("rlc_batch_set_schedule", self._h, int(dt_layout), int(prefetch), int(block), int(tile))
 
+    def set_product_mode(self, separate: bool) -> None:
+        """Per-particle products inside the persistent kernel (False) or in a second launch (True)."""
+        call("rlc_batch_set_product_mode", self._h, 1 if separate else 0)
+
+    def product_mode(self) -> str:
+        v = C.c_int()
+        call("rlc_batch_get_product_mode", self._h, C.byref(v))
+        return "separate" if v.value else "overlapped"
+
     def schedule(self):
         """(dt_layout, prefetch, block, tile)"""
         v = [C.c_int() for _ in range(4)]

@@ -470,8 +470,12 @@ def test_batch_matches_per_filter_calls(rl, oracle_mod):
     batch = rl.PyFilterBatch(filters)
     rays, tiles = batch.info()
     assert rays == sum(len(f[1]) * len(f[2]) for f in filters) and tiles > 0
-    for sched in ((0, 0, 256, 0), (1, 1, 128, 8), (2, 1, 512, 32), (2, 0, 256, 3)):
-        batch.set_schedule(*sched)
+    for sched in ((0, 0, 256, 0), (1, 1, 128, 8), (2, 1, 512, 32), (2, 0, 256, 3), "separate"):
+        if sched == "separate":
+            batch.set_product_mode(True)
+            assert batch.product_mode() == "separate"
+        else:
+            batch.set_schedule(*sched)
         for _ in range(2):   # graph replays
             for f in filters:
                 f[4].zero_()
