@@ -5,7 +5,8 @@
 //   in.bin : int32 W, H; uint8 occ[W*H] (grid[x][y] at x*H+y); float world[6];
 //            int32 n, na, K; float ins[n*3]; float angles[na]; float obs[na]; double table[K*K]
 //   out.bin: float bl[n], rm[n], cddt[n], pcddt[n]; float ranges[n*na];
-//            double eval[n], fused[n]; float dt[W*H]; float rmgpu_raw[n]
+//            double eval[n], fused[n]; float dt[W*H]; float rmgpu_raw[n];
+//            float glt[n]; uint16 lut[W*H*36]; float pair[n][2]; float radial[n*61]
 #include "RangeLib.h"
 
 #include <cstdio>
@@ -71,6 +72,18 @@ int main(int argc, char** argv) {
     if (g.calc_range(1.0f, 1.0f, 0.0f) != -1.0f) return 3;
     if (c.compressed_lut().size() != 108) return 4;
 
+    GiantLUTCast glt(map, 150.0f, 36);
+    std::vector<float> gl(n), pr((size_t)n * 2), rad((size_t)n * 61, -7.0f);
+    glt.numpy_calc_range(ins.data(), gl.data(), n);
+    std::vector<uint16_t> lut = glt.lut();
+    if (glt.lut_size() != (int)(lut.size() * sizeof(uint16_t))) return 6;
+    for (int i = 0; i < n; ++i) {
+        std::pair<float, float> q = c.calc_range_pair(ins[3 * i], ins[3 * i + 1], ins[3 * i + 2]);
+        pr[2 * i] = q.first;
+        pr[2 * i + 1] = q.second;
+    }
+    c.calc_range_many_radial_optimized(ins.data(), rad.data(), n, 61, -2.35619449f, 2.35619449f);
+
     FILE* o = fopen(argv[2], "wb");
     wr(o, bl.data(), n);
     wr(o, rm.data(), n);
@@ -81,6 +94,10 @@ int main(int argc, char** argv) {
     wr(o, fu.data(), n);
     for (int x = 0; x < W; ++x) wr(o, dt.grid[x].data(), H);
     wr(o, raw.data(), n);
+    wr(o, gl.data(), n);
+    wr(o, lut.data(), lut.size());
+    wr(o, pr.data(), pr.size());
+    wr(o, rad.data(), rad.size());
     fclose(o);
     // a bad call surfaces as an exception, not a crash
     try {

@@ -47,7 +47,20 @@ def test_cpp_caller(rl, oracle_mod, tmp_path):
     ev, fu = take(np.float64, n), take(np.float64, n)
     dt = take(np.float32, Wd * Hd).reshape(Wd, Hd)
     raw = take(np.float32, n)
+    glt = take(np.float32, n)
+    lut = take(np.uint16, Wd * Hd * 36).reshape(Wd, Hd, 36)
+    pair = take(np.float32, n * 2).reshape(n, 2)
+    radial = take(np.float32, n * 61)
     O = oracle_mod
+    og = O.OracleMethod(wl.occ, "glt", 150.0, td=36, world=world, nthreads=os.cpu_count() or 1)
+    assert np.array_equal(lut, og.glt_table())
+    assert np.array_equal(glt, og.calc_range_many(wl.ins))
+    oc = O.OracleMethod(wl.occ, "cddt", 150.0, td=108, world=world)
+    exp_pair = np.array([oc.calc_range_pair(*v) for v in wl.ins], np.float32)
+    assert np.array_equal(pair, exp_pair)
+    exp_rad = np.full(n * 61, -7.0, np.float32)
+    oc.calc_range_many_radial_optimized(61, np.float32(-2.35619449), np.float32(2.35619449), wl.ins, exp_rad)
+    assert np.array_equal(radial, exp_rad)
     assert np.array_equal(dt, O.edt(wl.occ))
     for got, kind in ((bl, "bl"), (rm, "rm")):
         exp = O.OracleMethod(wl.occ, kind, 150.0, world=world).calc_range_many(wl.ins)
