@@ -274,14 +274,26 @@ __global__ void k_features(FeatParams fp, const float* __restrict__ xyt, int n, 
 // 112 KB of shared memory and 256 TMEM columns per CTA: two CTAs per SM, so
 // one CTA's epilogue or operand loads overlap the other's MMAs.
 constexpr int kFwdThreads = 256;   // two threads per TMEM lane (row): column halves
-constexpr size_t kFwdSmem = 16384 + 32768 + 65536;
+constexpr int kFK = 32;            // K elements per pipeline stage
+constexpr uint32_t kFStage = 512;  // bytes between 8-row groups of a 32-wide K tile (4 core matrices)
+constexpr size_t kFwdSmem = 2 * 16384 + 65536;   // two 256 x 32 weight stages + activations
 
-// features [64c + 32h, 64c + 32h + 32) of a ray with inputs u (input d = c / 2,
-// 16 frequencies from (c % 2) * 32 + 16h), as 4 rows of 16 bytes for the core layout
-__device__ __forceinline__ void feature_half_chunk(const FeatParams& fp, const float* u, int c, int h, uint4* out) {
-    const int d = c >> 1, k0 = (c & 1) * 32 + 16 * h;
+// byte offset of element (row, k) (k < 32) in a 32-wide K tile of core matrices
+__device__ __forceinline__ uint32_t core32(int row, int k) {
+    return (uint32_t)((row >> 3) * kFStage + (k >> 3) * tc::kCoreBytes + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// bf16 element k (< 256) of row `row` of the activation buffer (4 K chunks of 64 in core layout)
+__device__ __forceinline__ uint32_t act_offset(int row, int k) {
+    return (uint32_t)(k >> 6) * 16384u + tc::core_offset(row, k & 63);
+}
+
+// 16 features [32c + 16h, 32c + 16h + 16) of a ray with inputs u: input d = c / 4,
+// frequencies (c % 4) * 16 + 8h .. + 8, as 2 rows of 16 bytes of the core layout
+__device__ __forceinline__ void feature_quarter(const FeatParams& fp, const float* u, int c, int h, uint4* out) {
+    const int d = c >> 2, k0 = (c & 3) * 16 + 8 * h;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {   // 4 frequencies (8 values) per 16-byte vector
+    for (int v = 0; v < 2; ++v) {
         __nv_bfloat162 hb[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -293,30 +305,89 @@ __device__ __forceinline__ void feature_half_chunk(const FeatParams& fp, const f
     }
 }
 
-__device__ __forceinline__ bool fwd_mma_chunk(uint32_t tmem, uint32_t idesc, uint32_t a0, uint32_t b0, bool first,
-                                              uint32_t mbar, uint32_t& phase) {
-    tc::fence_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        tc::fence_after_sync();
-#pragma unroll
-        for (int ks = 0; ks < tc::kKChunk / 16; ++ks) {
-            const uint64_t ad = tc::make_desc(a0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
-            const uint64_t bd = tc::make_desc(b0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
-            tc::mma_bf16(tmem, ad, bd, idesc, (!first || ks > 0) ? 1u : 0u);
-        }
-        tc::mma_commit(mbar);
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// weight rows [0, 256) x K [k0, k0 + 32) of a layer (row-major [256][ld]) into a stage, asynchronously
+__device__ __forceinline__ void load_weights32(uint32_t dst, const bf16* __restrict__ w, int ld, int k0) {
+    for (int v = threadIdx.x; v < kBN * (kFK / 8); v += blockDim.x) {
+        const int row = v >> 2, kv = v & 3;
+        cp_async16(dst + (uint32_t)((row >> 3) * kFStage + kv * tc::kCoreBytes + (row & 7) * 16),
+                   w + (size_t)row * ld + k0 + kv * 8);
     }
-    const bool w = tc::mbar_wait(mbar, phase);
-    phase ^= 1u;
-    const bool ok = __syncthreads_and(w) != 0;
-    tc::fence_after_sync();
-    return ok;
 }
 
-// bf16 element k (< 256) of row `row` of the activation buffer (4 K chunks in core layout)
-__device__ __forceinline__ uint32_t act_offset(int row, int k) {
-    return (uint32_t)(k >> 6) * 16384u + tc::core_offset(row, k & 63);
+// One layer's MMA chunks, pipelined: the weights of chunk c + 1 are copied into
+// the other stage while the MMAs of chunk c run; a stage is refilled only after
+// the MMAs that read it have completed (one mbarrier per stage).  Layer 0
+// computes its A operand (features) per chunk into sA[c % 2] inside the
+// activation buffer; hidden layers read A from the activations.
+struct FwdPipe {
+    uint32_t sB[2], mbar[2], par[2];
+    uint32_t tmem, idesc;
+};
+
+template <bool FEATURES>
+__device__ __forceinline__ bool fwd_layer(FwdPipe& P, const bf16* __restrict__ w, int K, uint32_t sH, uint8_t* sA_gen,
+                                          const FeatParams& fp, const float* u, bool live, int row, int half) {
+    const int C = K / kFK;
+    bool ok = true;
+    load_weights32(P.sB[0], w, K, 0);
+    cp_async_commit();
+    for (int c = 0; c < C; ++c) {
+        const int st = c & 1;
+        if (c + 1 < C) {
+            if (c >= 1) {   // stage st ^ 1 was read by the MMAs of chunk c - 1
+                const bool wt = tc::mbar_wait(P.mbar[st ^ 1], P.par[st ^ 1]);
+                P.par[st ^ 1] ^= 1u;
+                if (!__syncthreads_and(wt)) return false;
+            }
+            load_weights32(P.sB[st ^ 1], w, K, (c + 1) * kFK);
+            cp_async_commit();
+        }
+        uint32_t a0;
+        if (FEATURES) {   // A stage st (inside the activation buffer) was read by chunk c - 2, complete by now
+            uint4 f[2];
+            if (live) {
+                feature_quarter(fp, u, c, half, f);
+            } else {
+                f[0] = f[1] = make_uint4(0, 0, 0, 0);
+            }
+            uint8_t* sa = sA_gen + st * 8192;
+            *reinterpret_cast<uint4*>(sa + core32(row, 16 * half)) = f[0];
+            *reinterpret_cast<uint4*>(sa + core32(row, 16 * half + 8)) = f[1];
+            a0 = tc::smem_addr(sa);
+        } else {
+            a0 = sH + (uint32_t)(c >> 1) * 16384u + (uint32_t)(c & 1) * 4u * tc::kCoreBytes;
+        }
+        if (c + 1 < C) cp_async_wait<1>(); else cp_async_wait<0>();
+        tc::fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tc::fence_after_sync();
+            const uint32_t sbo_a = FEATURES ? kFStage : tc::kRowBlockBytes;
+#pragma unroll
+            for (int ks = 0; ks < kFK / 16; ++ks) {
+                const uint64_t ad = tc::make_desc(a0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, sbo_a);
+                const uint64_t bd = tc::make_desc(P.sB[st] + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, kFStage);
+                tc::mma_bf16(P.tmem, ad, bd, P.idesc, (c > 0 || ks > 0) ? 1u : 0u);
+            }
+            tc::mma_commit(P.mbar[st]);
+        }
+    }
+    // the loop waited for the MMAs of chunks 0 .. C - 3; wait for the last two
+    for (int q = C >= 2 ? C - 2 : 0; q < C; ++q) {
+        const int st = q & 1;
+        const bool wt = tc::mbar_wait(P.mbar[st], P.par[st]);
+        P.par[st] ^= 1u;
+        ok = (__syncthreads_and(wt) != 0) && ok;
+    }
+    tc::fence_after_sync();
+    return ok;
 }
 
 __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, const float* __restrict__ xyt, int n,
@@ -324,27 +395,32 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
                                                                  const float* __restrict__ params,
                                                                  float* __restrict__ y, unsigned* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
-    uint8_t* sA = smem;                  // layer 0: 128 rows x 64 features
-    uint8_t* sB = smem + 16384;          // 256 weight rows x 64
-    uint8_t* sH = smem + 16384 + 32768;  // activations: 4 K chunks of 128 x 64
+    uint8_t* sB0 = smem;                 // weight stages: 2 x (256 rows x 32)
+    uint8_t* sH = smem + 2 * 16384;      // activations: 4 K chunks of 128 x 64 (layer 0: feature stages)
     const int warp = threadIdx.x >> 5;
     const int row = threadIdx.x & 127;   // TMEM lane = ray of the tile (warp % 4 owns lanes 32 (warp % 4) ..)
     const int half = threadIdx.x >> 7;   // columns [128 half, 128 half + 128) of every layer
     if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
     if (threadIdx.x == 0) {
-        tc::mbar_init(tc::smem_addr(&mbar), 1);
+        tc::mbar_init(tc::smem_addr(&mbar[0]), 1);
+        tc::mbar_init(tc::smem_addr(&mbar[1]), 1);
         tc::fence_mbar_init();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = tmem_base, mb = tc::smem_addr(&mbar);
-    const uint32_t idesc = tc::make_idesc(kBM, kBN);
-    const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    uint32_t phase = 0;
-    bool ok = true;
+    FwdPipe P;
+    P.sB[0] = tc::smem_addr(sB0);
+    P.sB[1] = tc::smem_addr(sB0 + 16384);
+    P.mbar[0] = tc::smem_addr(&mbar[0]);
+    P.mbar[1] = tc::smem_addr(&mbar[1]);
+    P.par[0] = P.par[1] = 0u;
+    P.tmem = tmem_base;
+    P.idesc = tc::make_idesc(kBM, kBN);
+    const uint32_t lane_addr = tmem_base + ((uint32_t)((warp & 3) * 32) << 16);
+    const uint32_t sHa = tc::smem_addr(sH);
 
     const int r = blockIdx.x * kBM + row;
     float u[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -357,28 +433,10 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
         u[2] = cs;
         u[3] = sn;
     }
-    // layer 0: features chunk by chunk
-    for (int c = 0; c < kFeat / tc::kKChunk && ok; ++c) {
-        uint4 f[4];
-        if (live) {
-            feature_half_chunk(fp, u, c, half, f);
-        } else {
-#pragma unroll
-            for (int v = 0; v < 4; ++v) f[v] = make_uint4(0, 0, 0, 0);
-        }
-#pragma unroll
-        for (int v = 0; v < 4; ++v) *reinterpret_cast<uint4*>(sA + tc::core_offset(row, 32 * half + v * 8)) = f[v];
-        load_tile(sB, wbf + w_offset(0), kFeat, 0, 0, kBN, c * tc::kKChunk);
-        ok = fwd_mma_chunk(tmem, idesc, tc::smem_addr(sA), tc::smem_addr(sB), c == 0, mb, phase);
-    }
+    bool ok = fwd_layer<true>(P, wbf + w_offset(0), kFeat, sHa, sH, fp, u, live, row, half);
     for (int l = 0; l < kLayers && ok; ++l) {
-        if (l > 0) {   // hidden layer l: A = activations in sH
-            for (int c = 0; c < kHidden / tc::kKChunk && ok; ++c) {
-                load_tile(sB, wbf + w_offset(l), kHidden, 0, 0, kBN, c * tc::kKChunk);
-                ok = fwd_mma_chunk(tmem, idesc, tc::smem_addr(sH + c * 16384), tc::smem_addr(sB), c == 0, mb, phase);
-            }
-            if (!ok) break;
-        }
+        if (l > 0) ok = fwd_layer<false>(P, wbf + w_offset(l), kHidden, sHa, sH, fp, u, live, row, half);
+        if (!ok) break;
         // epilogue of layer l: z = acc + b, rounded to bf16; h = bf16(GELU(z)) into sH
         const float* bias = params + b_offset(l);
         for (int cb = 128 * half; cb < 128 * half + 128; cb += 32) {
@@ -426,9 +484,10 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
     } else if (threadIdx.x == 0) {
         atomicOr(err, 16u);
     }
+    cp_async_wait<0>();
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    if (warp == 0) tc::tmem_dealloc(P.tmem, 256);
 }
 
 cudaError_t mlp_forward(const FeatParams& fp, const float* xyt, int n, const bf16* wbf, const float* params, float* y,
