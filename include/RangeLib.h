@@ -11,16 +11,20 @@
 //    printing (the reference prints, throws std::string or invokes UB);
 //  * OMap(std::string[, float]) (PNG loading) is not provided in C++ -- build
 //    the grid from memory; the Python module loads PNGs;
-//  * serializeJson/Yaml and saveTrace are outside this library; CDDT tables
-//    are exported/imported as arrays (compressed_lut(), rlc_cddt_table_load).
+//  * CDDTCast::serializeJson prints 9 significant digits by default (the
+//    reference prints 7, which does not restore every float) and loadJson
+//    reads the document back; serializeYaml and saveTrace are not provided.
 #ifndef RANGELIB_GB300_H
 #define RANGELIB_GB300_H
 
 #include "rangelibc.h"
 
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 #include <iostream>
 #include <memory>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -216,6 +220,107 @@ public:
         std::vector<float> trans(theta_discretization);
         check(rlc_cddt_table_export(h, widths.data(), trans.data(), nullptr, nullptr));
         return trans;
+    }
+
+    // serializeJson (RangeLib.h:1690-1735): the reference's document -- keys, nesting, line
+    // breaks, the comma after the map's data array -- with `precision` significant digits.  The
+    // reference prints 7, which does not restore every float; 9 (the default) does, so loadJson
+    // gives the table back bit for bit.  precision 7 reproduces the reference's text exactly.
+    void serializeJson(std::stringstream* ss, int precision = 9) {
+        const std::vector<std::vector<std::vector<float> > > lut = compressed_lut();
+        const std::vector<float> trans = lut_translations();
+        const std::streamsize old = ss->precision(precision);
+        auto floats = [ss](const std::vector<float>& v) {
+            (*ss) << "[";
+            for (size_t i = 0; i < v.size(); ++i) (*ss) << (i ? "," : "") << v[i];
+            (*ss) << "]";
+        };
+        (*ss) << "{\"cddt\": {\n  \"theta_discretization\": " << theta_discretization << ",\n";
+        (*ss) << "  \"lut_translations\": ";
+        floats(trans);
+        (*ss) << ",\n  \"max_range\":" << max_range << ",\n  \"map\": {\n";
+        (*ss) << "    \"path\": \"" << map.fn << "\",\n    \"width\": " << map.width << ",\n    \"height\": "
+              << map.height << ",\n    \"data\": [";
+        for (unsigned x = 0; x < map.width; ++x) {
+            (*ss) << (x ? ",[" : "[");
+            for (unsigned y = 0; y < map.height; ++y) (*ss) << (y ? "," : "") << (map.grid[x][y] ? '1' : '0');
+            (*ss) << "]";
+        }
+        (*ss) << "],\n  },\n  \"compressed_lut\": [\n";
+        const float step = (float)(6.28318530718 / (double)(float)theta_discretization);
+        for (unsigned a = 0; a < theta_discretization; ++a) {
+            const float theta = (float)a * step;
+            (*ss) << "    {\n      \"theta\": " << theta << ",\n      \"zeros\": [";
+            for (size_t i = 0; i < lut[a].size(); ++i) {
+                if (i) (*ss) << ",";
+                floats(lut[a][i]);
+            }
+            (*ss) << "]\n    }" << (a + 1 == theta_discretization ? "\n" : ",\n");
+        }
+        (*ss) << "  ]\n}}\n";
+        ss->precision(old);
+    }
+
+    // loadJson: replace the table by the one in a serializeJson document (this library's or the
+    // reference's) written for a map of the same size and the same theta_discretization
+    void loadJson(const std::string& doc) {
+        const char* s = doc.c_str();
+        auto after = [&](const char* from, const char* key) {
+            const char* p = std::strstr(from, key);
+            if (!p) throw RangeLibError(RLC_ERR_ARG, std::string("loadJson: missing ") + key);
+            return p + std::strlen(key);
+        };
+        auto skip = [](const char* p) {
+            while (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t' || *p == ':' || *p == ',') ++p;
+            return p;
+        };
+        auto floats = [&](const char*& p, std::vector<float>& out) {   // "[v, ...]"
+            p = skip(p);
+            if (*p != '[') throw RangeLibError(RLC_ERR_ARG, "loadJson: expected '['");
+            p = skip(p + 1);
+            while (*p != ']') {
+                char* end = nullptr;
+                out.push_back(std::strtof(p, &end));
+                if (end == p) throw RangeLibError(RLC_ERR_ARG, "loadJson: bad number");
+                p = skip(end);
+            }
+            ++p;
+        };
+        const char* p = after(s, "\"theta_discretization\"");
+        if (std::strtoul(skip(p), nullptr, 10) != theta_discretization)
+            throw RangeLibError(RLC_ERR_ARG, "loadJson: another theta_discretization");
+        p = after(s, "\"width\"");
+        const unsigned long w = std::strtoul(skip(p), nullptr, 10);
+        p = after(s, "\"height\"");
+        if (w != map.width || std::strtoul(skip(p), nullptr, 10) != map.height)
+            throw RangeLibError(RLC_ERR_ARG, "loadJson: table of a map of another size");
+        std::vector<float> trans, zeros;
+        p = after(s, "\"lut_translations\"");
+        floats(p, trans);
+        if (trans.size() != theta_discretization) throw RangeLibError(RLC_ERR_ARG, "loadJson: lut_translations");
+        int64_t nb = 0, nz = 0;
+        check(rlc_cddt_table_size(h, &nb, &nz));
+        std::vector<int> widths(theta_discretization);
+        std::vector<float> cur(theta_discretization);
+        check(rlc_cddt_table_export(h, widths.data(), cur.data(), nullptr, nullptr));
+        std::vector<int64_t> len;
+        p = after(s, "\"compressed_lut\"");
+        for (unsigned a = 0; a < theta_discretization; ++a) {
+            p = skip(after(p, "\"zeros\""));
+            if (*p != '[') throw RangeLibError(RLC_ERR_ARG, "loadJson: expected '['");
+            p = skip(p + 1);
+            int bins = 0;
+            while (*p != ']') {
+                const size_t before = zeros.size();
+                floats(p, zeros);
+                len.push_back((int64_t)(zeros.size() - before));
+                ++bins;
+                p = skip(p);
+            }
+            ++p;
+            if (bins != widths[a]) throw RangeLibError(RLC_ERR_ARG, "loadJson: slice widths differ from this map's");
+        }
+        check(rlc_cddt_table_load(h, trans.data(), len.data(), zeros.data(), (int64_t)zeros.size()));
     }
     unsigned int theta_discretization;
 };

@@ -385,6 +385,8 @@ def ref_lib(fast: bool = False):
         L.ref_cddt_pair.argtypes = [vp, C.c_float, C.c_float, C.c_float, _f32p, _f32p]
         L.ref_cddt_radial.argtypes = [vp, _f32p, _f32p, C.c_int, C.c_int, C.c_float, C.c_float]
         L.ref_glt_slice.argtypes = [vp, C.c_float, _f32p]
+        L.ref_cddt_json.argtypes = [vp, C.c_char_p, C.c_longlong]
+        L.ref_cddt_json.restype = C.c_longlong
         _ref[key] = L
     return _ref[key]
 
@@ -514,3 +516,10 @@ class RefMethod:
         self.L.ref_cddt_export(self.h, _ptr(widths, _i32p), _ptr(trans, _f32p), _ptr(bin_len, _i64p),
                                _ptr(zeros, _f32p))
         return widths, trans, bin_len[:nb].copy(), zeros[:nz].copy()
+
+    def cddt_json(self) -> str:
+        """The reference's CDDTCast::serializeJson document."""
+        n = int(self.L.ref_cddt_json(self.h, None, 0))
+        buf = C.create_string_buffer(n)
+        self.L.ref_cddt_json(self.h, buf, n)
+        return buf.raw[:n].decode()

@@ -13,11 +13,14 @@
 //   set_sensor_model 523-532, eval_sensor_model 533-555,
 //   calc_range_repeat_angles_eval_sensor_model 558-612,
 //   CDDTCast::calc_range_pair 1521-1615, calc_range_many_radial_optimized 616-676,
-//   GiantLUTCast 1772-1904 (+ get_slice).
+//   GiantLUTCast 1772-1904 (+ get_slice), CDDTCast::serializeJson 1690-1735.
 #include "includes/RangeLib.h"
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <sstream>
+#include <string>
 
 using namespace ranges;
 
@@ -180,6 +183,16 @@ void ref_glt_slice(void* h, float theta, float* out) {
     for (unsigned x = 0; x < d->width; ++x)
         for (unsigned y = 0; y < d->height; ++y) out[(size_t)x * d->height + y] = d->grid[x][y];
     delete d;
+}
+
+// CDDTCast::serializeJson: copies up to `cap` bytes of the document into buf and
+// returns its full length (call with cap 0 to size the buffer)
+long long ref_cddt_json(void* h, char* buf, long long cap) {
+    std::stringstream ss;
+    static_cast<RefMethod*>(h)->cddt->serializeJson(&ss);
+    const std::string doc = ss.str();
+    if (buf && cap > 0) std::memcpy(buf, doc.data(), std::min((size_t)cap, doc.size()));
+    return (long long)doc.size();
 }
 
 }  // extern "C"

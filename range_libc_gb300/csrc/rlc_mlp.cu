@@ -262,16 +262,18 @@ __global__ void k_features(FeatParams fp, const float* __restrict__ xyt, int n, 
 
 // ------------------------------------------------------ fused forward pass
 // Inference of the whole network for 128 rays per CTA without leaving the SM:
-// the features of one 64-wide K chunk are computed straight into the A
+// the features of one 32-wide K stage are computed straight into the A
 // operand (shared memory, core-matrix layout), each layer accumulates its
 // 128 x 256 output in TMEM, and the epilogue (bias, BF16 rounding, GELU)
 // writes the next layer's A operand back into shared memory; the output
 // layer is a per-row dot product in the last epilogue.  Only the rays' poses
 // come in and one float per ray goes out (the layer-by-layer path moves
-// ~3.1 KB per ray through HBM).  Weights stream from L2 in 32 KB K chunks.
-// Every MMA operand, rounding point and summation order matches the
+// ~3.1 KB per ray through HBM).  Weights stream from L2 with cp.async into two
+// 16 KB stages of 256 x 32: stage c+1 is copied while the MMAs of stage c run.
+// Two threads share each TMEM lane (row) and split its features and epilogue
+// columns.  Every MMA operand, rounding point and summation order matches the
 // layer-by-layer path, so the predictions are bit-identical to it.
-// 112 KB of shared memory and 256 TMEM columns per CTA: two CTAs per SM, so
+// 96 KB of shared memory and 256 TMEM columns per CTA: two CTAs per SM, so
 // one CTA's epilogue or operand loads overlap the other's MMAs.
 constexpr int kFwdThreads = 256;   // two threads per TMEM lane (row): column halves
 constexpr int kFK = 32;            // K elements per pipeline stage

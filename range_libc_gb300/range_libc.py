@@ -202,6 +202,86 @@ def png_occupancy(path: str, threshold: float = 128.0) -> np.ndarray:
     return np.ascontiguousarray((gray < np.float32(threshold)).T, dtype=np.uint8)
 
 
+# ---------------------------------------------------------------- CDDT table JSON
+def _fmt_floats(vals, precision: int) -> str:
+    f = "%%.%dg" % precision
+    return "[" + ",".join(f % v for v in np.asarray(vals, np.float32).astype(np.float64).tolist()) + "]"
+
+
+def cddt_json_dumps(theta_disc: int, max_range: float, trans, widths, bin_len, zeros, occ, path: str = "",
+                    precision: int = 9) -> str:
+    """A CDDT table as the document CDDTCast::serializeJson writes (RangeLib.h:1690-1735).
+
+    Same keys, nesting, line breaks and indentation; ``map.data[x]`` is grid[x] (one 0/1 per y),
+    ``compressed_lut[a]`` holds slice a's ``theta`` (a * float(2pi / td), in float like the
+    reference) and its bins' zero points.  The reference prints 7 significant digits, which does
+    not restore every float32; the default here is 9, which does (``cddt_json_loads`` gives the
+    table back bit for bit).  With ``precision=7`` the text is the reference's, byte for byte --
+    including the comma after the map's ``data`` array, which strict JSON parsers reject and
+    ``cddt_json_loads`` accepts.
+    """
+    td = int(theta_disc)
+    widths = np.asarray(widths, np.int64)
+    bin_len = np.asarray(bin_len, np.int64)
+    zeros = np.asarray(zeros, np.float32)
+    occ = np.asarray(occ)
+    if widths.shape != (td,) or int(widths.sum()) != len(bin_len) or int(bin_len.sum()) != len(zeros):
+        raise ValueError("table arrays do not describe theta_disc slices")
+    f = "%%.%dg" % precision
+    W, H = occ.shape
+    rows = np.full((W, max(2 * H - 1, 0)), ord(","), np.uint8)
+    rows[:, 0::2] = (occ != 0).astype(np.uint8) + ord("0")
+    data = ",".join("[" + r.tobytes().decode() + "]" if H else "[]" for r in rows)
+    step = np.float32(6.28318530718 / float(np.float32(td)))
+    out = ['{"cddt": {\n',
+           '  "theta_discretization": %d,\n' % td,
+           '  "lut_translations": %s,\n' % _fmt_floats(trans, precision),
+           '  "max_range":%s,\n' % (f % float(np.float32(max_range))),
+           '  "map": {\n',
+           '    "path": "%s",\n' % path,
+           '    "width": %d,\n' % W,
+           '    "height": %d,\n' % H,
+           '    "data": [%s],\n' % data,
+           '  },\n',
+           '  "compressed_lut": [\n']
+    b = z = 0
+    for a in range(td):
+        theta = float(np.float32(a) * step)
+        bins = []
+        for _ in range(int(widths[a])):
+            n = int(bin_len[b])
+            bins.append(_fmt_floats(zeros[z:z + n], precision))
+            b += 1
+            z += n
+        out.append('    {\n      "theta": %s,\n      "zeros": [%s]\n    }%s\n'
+                   % (f % theta, ",".join(bins), "" if a == td - 1 else ","))
+    out.append("  ]\n}}\n")
+    return "".join(out)
+
+
+def cddt_json_loads(text: str) -> dict:
+    """Parse a document written by ``cddt_json_dumps`` or the reference's serializeJson into
+    ``theta_disc, max_range, trans, widths, bin_len, zeros`` (the CSR table), ``occ`` (grid[x][y],
+    uint8) and ``path``."""
+    import json
+    import re
+    doc = json.loads(re.sub(r",(\s*[}\]])", r"\1", text))["cddt"]
+    td = int(doc["theta_discretization"])
+    lut = doc["compressed_lut"]
+    if len(lut) != td or len(doc["lut_translations"]) != td:
+        raise ValueError("compressed_lut / lut_translations do not hold theta_discretization slices")
+    widths = np.array([len(s["zeros"]) for s in lut], np.int32)
+    bins = [b for s in lut for b in s["zeros"]]
+    bin_len = np.array([len(b) for b in bins], np.int64)
+    zeros = np.array([v for b in bins for v in b], np.float64).astype(np.float32)
+    m = doc["map"]
+    W, H = int(m["width"]), int(m["height"])
+    occ = np.array(m["data"], np.uint8).reshape(W, H) if W and H else np.zeros((W, H), np.uint8)
+    return {"theta_disc": td, "max_range": float(np.float32(doc["max_range"])),
+            "trans": np.array(doc["lut_translations"], np.float64).astype(np.float32),
+            "widths": widths, "bin_len": bin_len, "zeros": zeros, "occ": occ, "path": m.get("path", "")}
+
+
 def _quaternion_yaw(q) -> float:
     x, y, z, w = q.x, q.y, q.z, q.w
     return float(np.arctan2(2.0 * (w * z + x * y), 1.0 - 2.0 * (y * y + z * z)))
@@ -221,10 +301,12 @@ class PyOMap:
 
     def __init__(self, arg1, arg2=None):
         self._error = False
+        self.fn = ""   # the PNG's path, as OMap::fn
         world = (1.0, 0.0, 0.0, 0.0, 0.0, 1.0)
         if arg1 is not None and arg2 is not None and isinstance(arg1, (int, np.integer)):
             occ = np.zeros((int(arg1), int(arg2)), np.uint8)
         elif arg1 is not None and arg2 is not None:
+            self.fn = str(arg1)
             occ = self._from_png(str(arg1), float(arg2))
         elif isinstance(arg1, np.ndarray):
             occ = np.ascontiguousarray((arg1 != 0).T, dtype=np.uint8)
@@ -237,6 +319,7 @@ class PyOMap:
             world = (float(info.resolution), angle, float(info.origin.position.x), float(info.origin.position.y),
                      float(np.sin(angle)), float(np.cos(angle)))
         elif isinstance(arg1, str):
+            self.fn = arg1
             occ = self._from_png(arg1, 128.0)
         else:
             print("Failed to construct PyOMap, check argument types.")
@@ -484,6 +567,34 @@ class PyCDDTCast(_RangeMethod):
         zeros = np.ascontiguousarray(zeros, np.float32)
         call("rlc_cddt_table_load", self._h, trans.ctypes.data_as(_lib._f32p), bin_len.ctypes.data_as(_lib._i64p),
              zeros.ctypes.data_as(_lib._f32p), len(zeros))
+
+    def serialize_json(self, precision: int = 9) -> str:
+        """The table as CDDTCast::serializeJson writes it (RangeLib.h:1690-1735); 9 significant
+        digits by default so that load_json restores it exactly (7 gives the reference's text)."""
+        widths, trans, bin_len, zeros = self.table()
+        return cddt_json_dumps(self.theta_disc, self.max_range, trans, widths, bin_len, zeros,
+                               self.map.occupancy, self.map.fn, precision)
+
+    def load_json(self, text: str) -> None:
+        """Replace the table by one serialised for the same map and theta_disc (by serialize_json
+        or the reference's serializeJson)."""
+        d = cddt_json_loads(text)
+        widths = self.table()[0]
+        if d["theta_disc"] != self.theta_disc or not np.array_equal(d["widths"], widths):
+            raise ValueError("the serialised table has another theta_discretization or other slice widths")
+        if d["occ"].shape != self.map.occupancy.shape:
+            raise ValueError("the serialised table was built for a map of another size")
+        self.load_table(d["trans"], d["bin_len"], d["zeros"])
+
+    @classmethod
+    def from_json(cls, text: str, *, trig=None) -> "PyCDDTCast":
+        """A CDDTCast over the document's own map and max_range, with the document's table."""
+        d = cddt_json_loads(text)
+        omap = PyOMap(np.ascontiguousarray(d["occ"].T))
+        omap.fn = d["path"]
+        m = cls(omap, d["max_range"], d["theta_disc"], trig=trig)
+        m.load_table(d["trans"], d["bin_len"], d["zeros"])
+        return m
 
     def calc_range_pair(self, x: float, y: float, heading: float):
         """CDDTCast::calc_range_pair (RangeLib.h:1521-1615): (range at heading, range at heading + pi)."""

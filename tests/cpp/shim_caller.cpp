@@ -6,10 +6,15 @@
 //            int32 n, na, K; float ins[n*3]; float angles[na]; float obs[na]; double table[K*K]
 //   out.bin: float bl[n], rm[n], cddt[n], pcddt[n]; float ranges[n*na];
 //            double eval[n], fused[n]; float dt[W*H]; float rmgpu_raw[n];
-//            float glt[n]; uint16 lut[W*H*36]; float pair[n][2]; float radial[n*61]
+//            float glt[n]; uint16 lut[W*H*36]; float pair[n][2]; float radial[n*61];
+//            float pcddt_from_json[n]
+//   <out.bin>.json / <out.bin>.json7: the pruned table's serializeJson at 9 / 7 digits
 #include "RangeLib.h"
 
 #include <cstdio>
+#include <fstream>
+#include <sstream>
+#include <string>
 #include <vector>
 
 using namespace ranges;
@@ -84,6 +89,17 @@ int main(int argc, char** argv) {
     }
     c.calc_range_many_radial_optimized(ins.data(), rad.data(), n, 61, -2.35619449f, 2.35619449f);
 
+    // the pruned table through serializeJson / loadJson into an unpruned method
+    std::stringstream js, js7;
+    p.serializeJson(&js);
+    p.serializeJson(&js7, 7);
+    std::ofstream(std::string(argv[2]) + ".json") << js.str();
+    std::ofstream(std::string(argv[2]) + ".json7") << js7.str();
+    CDDTCast q(map, 150.0f, 108);
+    q.loadJson(js.str());
+    std::vector<float> qcd(n);
+    q.numpy_calc_range(ins.data(), qcd.data(), n);
+
     FILE* o = fopen(argv[2], "wb");
     wr(o, bl.data(), n);
     wr(o, rm.data(), n);
@@ -98,11 +114,19 @@ int main(int argc, char** argv) {
     wr(o, lut.data(), lut.size());
     wr(o, pr.data(), pr.size());
     wr(o, rad.data(), rad.size());
+    wr(o, qcd.data(), n);
     fclose(o);
     // a bad call surfaces as an exception, not a crash
     try {
         r.eval_sensor_model(obs.data(), ranges_.data(), ev.data(), -1, n);
         return 5;
+    } catch (const RangeLibError& e) {
+    }
+    // a table of another theta_discretization is refused
+    try {
+        CDDTCast other(map, 150.0f, 54);
+        other.loadJson(js.str());
+        return 7;
     } catch (const RangeLibError& e) {
     }
     return 0;

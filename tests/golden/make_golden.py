@@ -15,7 +15,9 @@ sensor tables, what the reference's own classes return:
   * CDDT tables (compressed_lut, lut_translations), unpruned and pruned;
   * CDDTCast::calc_range_pair and calc_range_many_radial_optimized on the
     particle-filter map and poses;
-  * a GiantLUTCast table (giant_lut) and its calc_range queries.
+  * a GiantLUTCast table (giant_lut) and its calc_range queries;
+  * CDDTCast::serializeJson documents (unpruned and pruned), one of them for a
+    map loaded from a PNG so that its "path" field is set.
 
 Alongside, it stores the per-ray cosf/sinf of every BL/RM heading and the
 cosf/sinf of every CDDT slice angle as this host's libm computes them, so a
@@ -182,6 +184,27 @@ def case_pairs_radial_glt(out):
     out["glt/ranges"] = np.array([g.calc_range(*v) for v in qg], np.float32)
 
 
+def case_json(out):
+    here = os.getcwd()
+    os.chdir(os.path.join(REF, "maps"))   # the document records the PNG path as given
+    try:
+        pm = O.RefMap(png="small.map.png", threshold=128.0)
+    finally:
+        os.chdir(here)
+    out["json/small/occ"] = pm.occ
+    out["json/small/slice_trig_12"] = slice_trig(12)
+    out["json/small/pcddt_td12"] = np.array(_pruned(O.RefMethod(pm, "cddt", 30.0, 12)).cddt_json())
+    occ = np.ascontiguousarray(W.rect_disk_map(96, 101)[:40, :56])
+    out["json/rect/occ"] = occ
+    out["json/rect/slice_trig_18"] = slice_trig(18)
+    out["json/rect/cddt_td18"] = np.array(O.RefMethod(O.RefMap(occ), "cddt", 25.0, 18).cddt_json())
+
+
+def _pruned(m):
+    m.prune()
+    return m
+
+
 def main():
     O.build(reference=True)
     out = {}
@@ -200,6 +223,7 @@ def main():
         case_map(name, occ, out, mr=60.0, td=108, worlds=worlds)
     case_particle_filter(out)
     case_pairs_radial_glt(out)
+    case_json(out)
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path}: {len(out)} arrays, {os.path.getsize(path) / 1e6:.2f} MB")

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from range_libc_gb300 import workloads as W
+from range_libc_gb300.range_libc import cddt_json_dumps
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -51,6 +52,7 @@ def test_cpp_caller(rl, oracle_mod, tmp_path):
     lut = take(np.uint16, Wd * Hd * 36).reshape(Wd, Hd, 36)
     pair = take(np.float32, n * 2).reshape(n, 2)
     radial = take(np.float32, n * 61)
+    from_json = take(np.float32, n)
     O = oracle_mod
     og = O.OracleMethod(wl.occ, "glt", 150.0, td=36, world=world, nthreads=os.cpu_count() or 1)
     assert np.array_equal(lut, og.glt_table())
@@ -67,6 +69,14 @@ def test_cpp_caller(rl, oracle_mod, tmp_path):
         assert np.mean(got != exp) < 1e-3
     for got, kind in ((cd, "cddt"), (pcd, "pcddt")):
         assert np.array_equal(got, O.OracleMethod(wl.occ, kind, 150.0, td=108, world=world).calc_range_many(wl.ins))
+    # serializeJson of the pruned table: the document of the Python serialiser (pinned to the
+    # reference's text at 7 digits by the CPU tests), and loadJson restores the table exactly
+    op = O.OracleMethod(wl.occ, "pcddt", 150.0, td=108, world=world)
+    widths, trans, bin_len, zeros = op.cddt_table()
+    for suffix, prec in ((".json", 9), (".json7", 7)):
+        text = open(str(tmp_path / "out.bin") + suffix).read()
+        assert text == cddt_json_dumps(108, 150.0, trans, widths, bin_len, zeros, wl.occ, "", prec)
+    assert np.array_equal(from_json, pcd)
     orm = O.OracleMethod(wl.occ, "rm", 150.0, world=world)
     orm.set_sensor_model(wl.table)
     assert np.mean(ranges != orm.calc_range_repeat_angles(wl.ins, wl.angles)) < 1e-3

@@ -149,3 +149,33 @@ def test_giant_lut(rl, gold):
     out = np.empty(len(q), np.float32)
     rl._lib.call("rlc_calc_range_many", g.handle, q.ctypes.data, out.ctypes.data, len(q), rl._lib.RLC_NO_WORLD, None)
     assert np.array_equal(_bits(out), _bits(gold["glt/ranges"]))
+
+
+@pytest.mark.parametrize("case", ["small/pcddt_td12", "rect/cddt_td18"])
+def test_cddt_json(rl, gold, case):
+    """serializeJson of the GPU-built table is the reference's document (7 digits); at 9 digits
+    it restores the table exactly, through load_json and through from_json."""
+    name, key = case.split("/")
+    td = int(key.split("_td")[1])
+    trig = gold[f"json/{name}/slice_trig_{td}"]
+    ref = str(gold[f"json/{case}"])
+    occ = gold[f"json/{name}/occ"]
+    m = _map(rl, occ)
+    m.fn = "small.map.png" if name == "small" else ""
+    g = rl.PyCDDTCast(m, 30.0 if name == "small" else 25.0, td, trig=(trig[:, 0], trig[:, 1]))
+    if key.startswith("pcddt"):
+        g.prune()
+    assert g.serialize_json(precision=7) == ref
+    doc = g.serialize_json()
+    w, t, bl, z = g.table()
+    h = rl.PyCDDTCast.from_json(doc, trig=(trig[:, 0], trig[:, 1]))
+    w2, t2, bl2, z2 = h.table()
+    assert np.array_equal(w2, w) and np.array_equal(bl2, bl)
+    assert np.array_equal(_bits(t2), _bits(t)) and np.array_equal(_bits(z2), _bits(z))
+    assert h.serialize_json() == doc
+    u = rl.PyCDDTCast(_map(rl, occ), 25.0, td, trig=(trig[:, 0], trig[:, 1]))
+    u.load_json(ref)   # the reference's 7-digit document
+    assert np.array_equal(u.table()[2], bl)
+    assert np.allclose(u.table()[3], z, rtol=6e-7, atol=0)
+    with pytest.raises(ValueError):
+        rl.PyCDDTCast(_map(rl, occ), 25.0, td + 1).load_json(ref)

@@ -580,3 +580,20 @@ def test_host_buffers_in_place_and_staged(rl, oracle_mod):
         assert np.array_equal(np.asarray(a), np.asarray(b))
     assert (results["auto"][4] == -7.0).any()
     assert isinstance(rl.host_path_direct(), bool)
+
+
+def test_cddt_json_round_trip_full_size(rl):
+    """The 2048^2 rectangles-and-disks map's pruned td-108 table through serialize_json /
+    from_json: the same table bit for bit and the same ranges for 1M queries."""
+    wl = W.cddt_queries(side=2048, n=1_000_000, td=108, max_range=300.0)
+    g = rl.PyCDDTCast(_pymap(rl, wl.occ, None), 300.0, 108)
+    g.prune()
+    doc = g.serialize_json()
+    h = rl.PyCDDTCast.from_json(doc)
+    for a, b in zip(g.table(), h.table()):
+        assert np.array_equal(np.ascontiguousarray(a).view(np.uint8), np.ascontiguousarray(b).view(np.uint8))
+    r1 = np.empty(len(wl.ins), np.float32)
+    r2 = np.empty(len(wl.ins), np.float32)
+    g.calc_range_many(wl.ins, r1)
+    h.calc_range_many(wl.ins, r2)
+    assert np.array_equal(_bits(r1), _bits(r2))

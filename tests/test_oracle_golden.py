@@ -138,3 +138,23 @@ def test_giant_lut(gold, oracle_mod):
     assert np.array_equal(m.glt_table(), gold["glt/lut"])
     got = np.array([m.calc_range(*v) for v in gold["glt/ins"]], np.float32)
     assert np.array_equal(_bits(got), _bits(gold["glt/ranges"]))
+
+
+@pytest.mark.parametrize("case", ["small/pcddt_td12", "rect/cddt_td18"])
+def test_cddt_json(gold, oracle_mod, case):
+    """CDDTCast::serializeJson (RangeLib.h:1690-1735): the library's serialiser over the oracle's
+    table prints the reference's document byte for byte at 7 digits, and reads it back."""
+    from range_libc_gb300.range_libc import cddt_json_dumps, cddt_json_loads
+    name, key = case.split("/")
+    td = int(key.split("_td")[1])
+    if not np.array_equal(_host_slice_trig(td), gold[f"json/{name}/slice_trig_{td}"]):
+        pytest.skip("this host's cosf/sinf of the slice angles differ from the recorded ones")
+    ref = str(gold[f"json/{case}"])
+    d = cddt_json_loads(ref)
+    occ = gold[f"json/{name}/occ"]
+    assert np.array_equal(d["occ"], occ) and d["theta_disc"] == td
+    m = oracle_mod.OracleMethod(occ, key.split("_")[0], d["max_range"], td=td)
+    w, t, bl, z = m.cddt_table()
+    assert cddt_json_dumps(td, d["max_range"], t, w, bl, z, occ, d["path"], precision=7) == ref
+    assert np.array_equal(d["widths"], w) and np.array_equal(d["bin_len"], bl)
+    assert np.allclose(d["zeros"], z, rtol=6e-7, atol=0)   # 7 significant digits

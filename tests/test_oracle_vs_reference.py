@@ -148,3 +148,21 @@ def test_cddt_radial(O, num_rays, span):
     ref.calc_range_many_radial_optimized(num_rays, lo, hi, wl.ins, o_ref)
     orc.calc_range_many_radial_optimized(num_rays, lo, hi, wl.ins, o_orc)
     assert np.array_equal(_bits(o_orc), _bits(o_ref[: n * num_rays]))
+
+
+@pytest.mark.parametrize("kind,td", [("cddt", 108), ("pcddt", 108), ("pcddt", 7)])
+def test_cddt_json(O, kind, td):
+    """serializeJson: the library's serialiser prints the reference's document byte for byte at 7
+    significant digits; at 9 its document reads back to the table bit for bit."""
+    from range_libc_gb300.range_libc import cddt_json_dumps, cddt_json_loads
+    occ = np.ascontiguousarray(MAPS["corridor_384x256"]()[:200, :150])
+    ref = O.RefMethod(O.RefMap(occ), "cddt", 120.0, td)
+    orc = O.OracleMethod(occ, kind, 120.0, td=td)
+    if kind == "pcddt":
+        ref.prune()
+    w, t, bl, z = orc.cddt_table()
+    assert cddt_json_dumps(td, 120.0, t, w, bl, z, occ, "", precision=7) == ref.cddt_json()
+    d = cddt_json_loads(cddt_json_dumps(td, 120.0, t, w, bl, z, occ))
+    for k, v in (("trans", t), ("widths", w), ("bin_len", bl), ("zeros", z), ("occ", occ)):
+        assert np.array_equal(_bits(d[k]) if k in ("trans", "zeros") else d[k],
+                              _bits(v) if k in ("trans", "zeros") else v), k
