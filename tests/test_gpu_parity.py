@@ -169,6 +169,67 @@ def test_repeat_angles_parity(rl, oracle_mod, kind):
         g.set_schedule(0, 0, 1, 0)
         g.calc_range_repeat_angles(ins, angles, out)
         assert np.array_equal(_bits(out), _bits(exp))
+    if kind == "rm":     # every distance-transform layout, with and without prefetch
+        for layout in (0, 1, 2):
+            for pf in (0, 1):
+                g.set_schedule(layout, 0, pf, 0)
+                g.calc_range_repeat_angles(ins, angles, out)
+                assert np.array_equal(_bits(out), _bits(exp)), (layout, pf)
+
+
+def _corridors(W_, H_, seed):
+    """Walls along x every 3-9 rows with door gaps: most march steps read distances 1, 2 and 3."""
+    rng = np.random.default_rng(seed)
+    occ = np.zeros((W_, H_), np.uint8)
+    occ[:, :2] = occ[:, -2:] = 1
+    y = 2
+    while y < H_ - 4:
+        y += int(rng.integers(3, 10))
+        occ[2:W_ - 2, y:y + 1] = 1
+        for _ in range(3):
+            g0 = int(rng.integers(2, W_ - 12))
+            occ[g0:g0 + int(rng.integers(3, 9)), y] = 0
+    return occ
+
+
+@pytest.mark.parametrize("mr", [6.0, 8.5, 9.998, 10.0, 31.7, 150.0, 1000.0])
+def test_narrow_corridor_parity(rl, oracle_mod, mr):
+    """Rays along corridors 2-8 px wide -- long chains of 1 px steps, the longest rays of a
+    particle-filter step -- that end on walls, leave the map or reach max_range after a fractional
+    step; every layout and prefetch, per-ray and fused calls, against the oracle."""
+    occ = _corridors(420, 300, 7)
+    m = _pymap(rl, occ)
+    g = rl.PyRayMarching(m, mr)
+    ref = oracle_mod.OracleMethod(occ, "rm", mr, world=m.world)
+    rng = np.random.default_rng(8)
+    fs = W.free_cell_queries(occ, 6000, 13)
+    head = np.where(rng.random(len(fs)) < 0.7,
+                    rng.integers(0, 4, len(fs)) * (np.pi / 2) + rng.normal(0, 0.02, len(fs)),
+                    rng.uniform(-np.pi, np.pi, len(fs)))
+    q = np.stack([fs[:, 0], fs[:, 1], head], 1).astype(np.float32)
+    q[:200, 0] = rng.uniform(-3, 3, 200)            # near and beyond the map's edge
+    q[200:400, 1] = rng.uniform(296, 303, 200)
+    _, trig = oracle_mod.world_rays(m.world, q)
+    exp = ref.calc_range_many(q)
+    table = W.sensor_table(int(mr) + 1 if mr < 400 else 201)
+    g.set_sensor_model(table)
+    ref.set_sensor_model(table)
+    angles = W.laser_angles(31)
+    ins = q[:500]
+    _, trig_a = oracle_mod.world_rays(m.world, ins, angles)
+    obs = (np.linspace(1, 30, 31) % mr).astype(np.float32)
+    exp_w = ref.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs)
+    for layout in (0, 1, 2):
+        for pf in (0, 1):
+            g.set_schedule(layout, 0, pf, 0)
+            g.set_trig_override(trig)
+            out = np.empty(len(q), np.float32)
+            g.calc_range_many(q, out)
+            assert np.array_equal(_bits(out), _bits(exp)), (layout, pf)
+            g.set_trig_override(trig_a)
+            w = np.empty(len(ins), np.float64)
+            g.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs, w)
+            assert np.array_equal(_bits(w), _bits(exp_w)), (layout, pf)
 
 
 @pytest.mark.parametrize("name", ["quad", "small_5x6", "rect_128", "rect_200x120", "corridor_512"])
