@@ -9,8 +9,6 @@
 // Differences a caller may notice:
 //  * errors throw ranges::RangeLibError (std::runtime_error) instead of
 //    printing (the reference prints, throws std::string or invokes UB);
-//  * OMap(std::string[, float]) (PNG loading) is not provided in C++ -- build
-//    the grid from memory; the Python module loads PNGs;
 //  * CDDTCast::serializeJson prints 9 significant digits by default (the
 //    reference prints 7, which does not restore every float) and loadJson
 //    reads the document back; serializeYaml and saveTrace are not provided.
@@ -20,6 +18,7 @@
 #include "rangelibc.h"
 
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -58,6 +57,38 @@ struct OMap {
     OMap(int w, int h)
         : has_error(false), width((unsigned)w), height((unsigned)h),
           grid((size_t)w, std::vector<bool>((size_t)h, false)) {}
+
+    // OMap(std::string[, float]) (RangeLib.h:158-201): a PNG map; pixel (x, y) is occupied when
+    // (int)rgb2gray(r, g, b) < threshold.  A file that cannot be read prints the error and sets
+    // has_error, as in the reference.
+    explicit OMap(const std::string& filename, float threshold = 128.0f)
+        : has_error(false), width(0), height(0), fn(filename) {
+        int w = 0, h = 0;
+        int rc = rlc_png_occupancy(filename.c_str(), threshold, nullptr, &w, &h);
+        std::vector<uint8_t> occ;
+        if (rc == RLC_OK) {
+            occ.resize((size_t)w * h);
+            rc = rlc_png_occupancy(filename.c_str(), threshold, occ.data(), &w, &h);
+        }
+        if (rc != RLC_OK) {
+            std::printf("ERROR %d: %s\n", rc, rlc_last_error());
+            has_error = true;
+            return;
+        }
+        width = (unsigned)w;
+        height = (unsigned)h;
+        grid.assign(width, std::vector<bool>(height, false));
+        for (unsigned x = 0; x < width; ++x)
+            for (unsigned y = 0; y < height; ++y) grid[x][y] = occ[(size_t)x * height + y] != 0;
+    }
+
+    // save (RangeLib.h:263-291): occupied black, free white; true when the file could not be written
+    bool save(const std::string& filename) {
+        const std::vector<uint8_t> occ = occupancy();
+        const int rc = rlc_png_save_occupancy(filename.c_str(), occ.data(), (int)width, (int)height);
+        if (rc != RLC_OK) std::cout << "encoder error " << rc << ": " << rlc_last_error() << std::endl;
+        return rc != RLC_OK;
+    }
 
     bool get(int x, int y) { return grid[x][y]; }
     bool isOccupied(int x, int y) {

@@ -61,7 +61,8 @@ enum rlc_status {
     RLC_ERR_ARG = 1,      /* invalid argument (null pointer, size, kind) */
     RLC_ERR_CUDA = 2,     /* CUDA runtime error (message in rlc_last_error) */
     RLC_ERR_STATE = 3,    /* call not valid in the handle's state (e.g. no sensor model) */
-    RLC_ERR_NOMEM = 4     /* device allocation failed */
+    RLC_ERR_NOMEM = 4,    /* device allocation failed */
+    RLC_ERR_IO = 5        /* a file could not be read, decoded or written */
 };
 
 enum rlc_kind {
@@ -96,6 +97,16 @@ RLC_API int rlc_device_count(void);
 /* ---- maps: OMap (RangeLib.h:121-322) ---------------------------------- */
 /* OMap(int w, int h) + grid fill (RangeLib.h:143-156; PyOMap(ndarray), RangeLibc.pyx:140-145). */
 RLC_API int rlc_map_create(const uint8_t* occ, int width, int height, rlc_map** out);
+/* OMap(std::string filename, float threshold) (RangeLib.h:158-201): the PNG's pixel (x, y) is
+ * occupied when (int)rgb2gray(r, g, b) < threshold, with r, g, b the pixel's blue, green and red
+ * (the reference reads bytes 2, 1, 0 of each RGBA pixel).  Host code, no GPU.  Call with
+ * occ = NULL to read width and height; then again with those and occ[width * height] to get
+ * occ[x * height + y].  Non-interlaced PNGs of every colour type and bit depth; RLC_ERR_IO with
+ * the reason in rlc_last_error() for files that cannot be read or decoded. */
+RLC_API int rlc_png_occupancy(const char* path, float threshold, uint8_t* occ, int* width, int* height);
+/* OMap::save (RangeLib.h:263-291): occ[x * height + y] as an 8-bit grey PNG, occupied black and
+ * free white.  Host code, no GPU. */
+RLC_API int rlc_png_save_occupancy(const char* path, const uint8_t* occ, int width, int height);
 /* World parameters of the ROS conversion (RangeLib.h:134-141; RangeLibc.pyx:160-180). */
 RLC_API int rlc_map_set_world(rlc_map* map, float scale, float angle, float origin_x, float origin_y,
                               float sin_angle, float cos_angle);

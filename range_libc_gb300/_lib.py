@@ -12,7 +12,7 @@ import threading
 
 from .build import LIB_PATH as _LIB_PATH, build as _build_library
 
-RLC_OK, RLC_ERR_ARG, RLC_ERR_CUDA, RLC_ERR_STATE, RLC_ERR_NOMEM = range(5)
+RLC_OK, RLC_ERR_ARG, RLC_ERR_CUDA, RLC_ERR_STATE, RLC_ERR_NOMEM, RLC_ERR_IO = range(6)
 RLC_BL, RLC_RM, RLC_CDDT, RLC_PCDDT, RLC_RMGPU, RLC_GLT = range(6)
 RLC_DEVICE_PTRS = 1
 RLC_HOST_AUTO, RLC_HOST_STAGED = 0, 1
@@ -49,6 +49,8 @@ SIGNATURES = {
     "rlc_last_error": (C.c_char_p, []),
     "rlc_device_count": (C.c_int, []),
     "rlc_map_create": (C.c_int, [_u8p, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "rlc_png_occupancy": (C.c_int, [C.c_char_p, C.c_float, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "rlc_png_save_occupancy": (C.c_int, [C.c_char_p, _vp, C.c_int, C.c_int]),
     "rlc_map_set_world": (C.c_int, [_vp] + [C.c_float] * 6),
     "rlc_map_destroy": (C.c_int, [_vp]),
     "rlc_map_size": (C.c_int, [_vp, _i32p, _i32p]),

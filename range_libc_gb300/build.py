@@ -24,7 +24,7 @@ LIB_NAME = "librangelibc_gb300.so"
 LIB_PATH = os.path.join(BUILD, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["rlc_map.cu", "rlc_cast.cu", "rlc_cddt.cu", "rlc_api.cu", "rlc_mlp.cu"]
+SOURCES = ["rlc_map.cu", "rlc_cast.cu", "rlc_cddt.cu", "rlc_api.cu", "rlc_mlp.cu", "rlc_png.cu"]
 
 
 def nvcc() -> str:

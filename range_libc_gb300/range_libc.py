@@ -21,9 +21,7 @@ those of the reference's typed buffers: float32 C-contiguous poses
 from __future__ import annotations
 
 import ctypes as C
-import struct
 import sys
-import zlib
 
 import numpy as np
 
@@ -88,121 +86,19 @@ def _flags_stream(dev_flags, first):
 
 
 # ---------------------------------------------------------------- PNG
-def _read_png_rgba(path: str) -> np.ndarray:
-    """Decode a non-interlaced PNG (grey, RGB, palette, grey+alpha, RGBA; 1-8 bit) to RGBA8 [H, W, 4]."""
-    with open(path, "rb") as f:
-        data = f.read()
-    if data[:8] != b"\x89PNG\r\n\x1a\n":
-        raise IOError(f"{path}: not a PNG file")
-    pos, idat, plte, trns = 8, [], None, None
-    w = h = bd = ct = il = None
-    while pos < len(data):
-        ln, typ = struct.unpack(">I4s", data[pos:pos + 8])
-        body = data[pos + 8:pos + 8 + ln]
-        pos += 12 + ln
-        if typ == b"IHDR":
-            w, h, bd, ct, _cm, _fm, il = struct.unpack(">IIBBBBB", body)
-        elif typ == b"PLTE":
-            plte = np.frombuffer(body, np.uint8).reshape(-1, 3)
-        elif typ == b"tRNS":
-            trns = body
-        elif typ == b"IDAT":
-            idat.append(body)
-        elif typ == b"IEND":
-            break
-    if il:
-        raise IOError(f"{path}: interlaced PNGs are not supported")
-    channels = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ct]
-    if bd == 16 or (bd < 8 and ct not in (0, 3)):
-        raise IOError(f"{path}: unsupported bit depth {bd} for colour type {ct}")
-    raw = zlib.decompress(b"".join(idat))
-    bpp = max(1, channels * bd // 8)
-    stride = (w * channels * bd + 7) // 8
-    img = np.zeros((h, stride), np.uint8)
-    prev = np.zeros(stride, np.int32)
-    p = 0
-    for y in range(h):
-        ftype = raw[p]
-        line = np.frombuffer(raw, np.uint8, stride, p + 1).astype(np.int32)
-        p += 1 + stride
-        if ftype == 0:
-            cur = line
-        elif ftype == 2:
-            cur = (line + prev) & 255
-        else:
-            cur = np.zeros(stride, np.int32)
-            for i in range(stride):
-                a = cur[i - bpp] if i >= bpp else 0
-                b = prev[i]
-                c = prev[i - bpp] if i >= bpp else 0
-                if ftype == 1:
-                    pred = a
-                elif ftype == 3:
-                    pred = (a + b) >> 1
-                else:
-                    pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
-                    pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
-                cur[i] = (line[i] + pred) & 255
-        img[y] = cur
-        prev = cur
-    if bd < 8:
-        bits = np.unpackbits(img, axis=1)[:, : w * bd].reshape(h, w, bd)
-        vals = np.zeros((h, w), np.int32)
-        for k in range(bd):
-            vals = (vals << 1) | bits[:, :, k]
-        samples = vals.astype(np.uint8)
-        if ct == 0:
-            samples = (vals * 255 // ((1 << bd) - 1)).astype(np.uint8)
-        px = samples[:, :, None]
-    else:
-        px = img[:, : w * channels].reshape(h, w, channels)
-    out = np.empty((h, w, 4), np.uint8)
-    if ct == 0:
-        out[..., :3] = px[..., :1]
-        out[..., 3] = 255
-    elif ct == 2:
-        out[..., :3] = px
-        out[..., 3] = 255
-    elif ct == 3:
-        idx = px[..., 0]
-        out[..., :3] = plte[idx]
-        alpha = np.full(256, 255, np.uint8)
-        if trns:
-            alpha[: len(trns)] = np.frombuffer(trns, np.uint8)
-        out[..., 3] = alpha[idx]
-    elif ct == 4:
-        out[..., :3] = px[..., :1]
-        out[..., 3] = px[..., 1]
-    else:
-        out[...] = px
-    return out
-
-
-def _write_png_gray(path: str, gray: np.ndarray) -> None:
-    h, w = gray.shape
-    raw = b"".join(b"\x00" + gray[y].tobytes() for y in range(h))
-
-    def chunk(t, b):
-        return struct.pack(">I", len(b)) + t + b + struct.pack(">I", zlib.crc32(t + b) & 0xFFFFFFFF)
-
-    with open(path, "wb") as f:
-        f.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 0, 0, 0, 0))
-                + chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
-
-
 def png_occupancy(path: str, threshold: float = 128.0) -> np.ndarray:
-    """grid[x][y] of OMap(path, threshold) (RangeLib.h:159-201) as uint8 (width, height).
+    """grid[x][y] of OMap(path, threshold) (RangeLib.h:158-201) as uint8 (width, height).
 
-    The reference reads r = image[idx+2], g = image[idx+1], b = image[idx]
-    from lodepng's RGBA buffer and marks (int)rgb2gray(r, g, b) < threshold
-    occupied, rgb2gray = 0.229 r + 0.587 g + 0.114 b in double (RangeUtils.h:30-32).
+    Decoded by the library (host code, rlc_png_occupancy): pixel (x, y) is occupied when
+    (int)rgb2gray(r, g, b) < threshold with r, g, b its blue, green and red bytes, as the
+    reference reads them.  Raises RangeLibError for files that cannot be read or decoded.
     """
-    rgba = _read_png_rgba(path)
-    r = rgba[..., 2].astype(np.float64)
-    g = rgba[..., 1].astype(np.float64)
-    b = rgba[..., 0].astype(np.float64)
-    gray = (0.229 * r + 0.587 * g + 0.114 * b).astype(np.float32).astype(np.int32)
-    return np.ascontiguousarray((gray < np.float32(threshold)).T, dtype=np.uint8)
+    w, h = C.c_int(0), C.c_int(0)
+    p = path.encode() if isinstance(path, str) else bytes(path)
+    call("rlc_png_occupancy", p, float(threshold), None, C.byref(w), C.byref(h))
+    occ = np.empty((w.value, h.value), np.uint8)
+    call("rlc_png_occupancy", p, float(threshold), occ.ctypes.data, C.byref(w), C.byref(h))
+    return occ
 
 
 # ---------------------------------------------------------------- CDDT table JSON
@@ -341,7 +237,7 @@ class PyOMap:
     def _from_png(self, path: str, threshold: float) -> np.ndarray:
         try:
             return png_occupancy(path, threshold)
-        except (IOError, OSError, KeyError, zlib.error, struct.error) as e:
+        except _lib.RangeLibError as e:   # the reference prints the decoder's error and flags the map
             print(f"ERROR: {e}")
             self._error = True
             return np.zeros((0, 0), np.uint8)
@@ -374,10 +270,13 @@ class PyOMap:
         return self._occ
 
     def save(self, fn) -> bool:
-        """PNG with white = free, black = occupied (OMap::save, RangeLib.h:263-291)."""
-        gray = np.where(self._occ.T != 0, 0, 255).astype(np.uint8)
-        _write_png_gray(fn if isinstance(fn, str) else fn.decode(), gray)
-        return False   # the reference returns the encoder's error code: 0 = success
+        """PNG with white = free, black = occupied (OMap::save, RangeLib.h:263-291); False on
+        success, like the reference's encoder status."""
+        W, H = self._occ.shape
+        rc = lib().rlc_png_save_occupancy(fn.encode() if isinstance(fn, str) else bytes(fn), self._occ.ctypes.data, W, H)
+        if rc != _lib.RLC_OK:
+            print(f"encoder error {rc}: {lib().rlc_last_error().decode()}")
+        return rc != _lib.RLC_OK
 
     def isOccupied(self, x: int, y: int) -> bool:
         return bool(self._occ[x, y])

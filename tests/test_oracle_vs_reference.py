@@ -166,3 +166,21 @@ def test_cddt_json(O, kind, td):
     for k, v in (("trans", t), ("widths", w), ("bin_len", bl), ("zeros", z), ("occ", occ)):
         assert np.array_equal(_bits(d[k]) if k in ("trans", "zeros") else d[k],
                               _bits(v) if k in ("trans", "zeros") else v), k
+
+
+def test_png_maps_match_reference_loader(O, tmp_path):
+    """The library's PNG decoder against the reference's OMap(filename, 128) on every map the
+    reference ships (1x1 to 10976x10976; grey 1/8-bit, RGB, RGBA), and the reference's loader on
+    a map saved by rlc_png_save_occupancy."""
+    import os
+    from range_libc_gb300 import _lib
+    from range_libc_gb300.range_libc import png_occupancy
+    maps = os.path.join(O.REF_SRC, "maps")
+    names = sorted(f for f in os.listdir(maps) if f.endswith(".png"))
+    assert len(names) >= 10
+    for f in names:
+        assert np.array_equal(png_occupancy(os.path.join(maps, f)), O.RefMap(png=os.path.join(maps, f)).occ), f
+    occ = np.ascontiguousarray(MAPS["corridor_384x256"]())
+    path = str(tmp_path / "saved.png")
+    assert _lib.lib().rlc_png_save_occupancy(path.encode(), occ.ctypes.data, occ.shape[0], occ.shape[1]) == 0
+    assert np.array_equal(O.RefMap(png=path).occ, occ)
