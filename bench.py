@@ -55,19 +55,70 @@ def load_peaks():
 
 # ----------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled during the timed region.
+
+    Polls NVML (libnvidia-ml, read-only queries) every millisecond from a thread, so that even a
+    few-millisecond timed region is sampled; falls back to `nvidia-smi -lms 200` without NVML.
+    """
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.lines = []
         self.t = None
+        self.samples = []          # (sm_mhz, reason bits) from NVML
+        self.max_mhz = None
+        self.stop_flag = threading.Event()
+        self.nvml = self._nvml_handle()
+
+    def _nvml_handle(self):
+        import ctypes as C
+        try:
+            L = C.CDLL("libnvidia-ml.so.1")
+            if L.nvmlInit_v2() != 0:
+                return None
+            h = C.c_void_p()
+            uuid = None
+            try:   # the CUDA device's own UUID: NVML's index order can differ from CUDA's
+                import torch
+                uuid = "GPU-" + str(torch.cuda.get_device_properties(self.index).uuid)
+            except (ImportError, AttributeError, RuntimeError, AssertionError):
+                pass
+            if uuid is None or L.nvmlDeviceGetHandleByUUID(uuid.encode(), C.byref(h)) != 0:
+                if L.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(h)) != 0:
+                    return None
+            mx = C.c_uint(0)
+            if L.nvmlDeviceGetMaxClockInfo(h, C.c_int(1), C.byref(mx)) == 0:   # NVML_CLOCK_SM
+                self.max_mhz = float(mx.value)
+            reasons = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                L.nvmlDeviceGetCurrentClocksThrottleReasons
+            return L, h, reasons
+        except (OSError, AttributeError):
+            return None
+
+    def _poll(self):
+        import ctypes as C
+        L, h, reasons = self.nvml
+        mhz, bits = C.c_uint(0), C.c_ulonglong(0)
+        while not self.stop_flag.is_set():
+            if L.nvmlDeviceGetClockInfo(h, C.c_int(1), C.byref(mhz)) == 0 and reasons(h, C.byref(bits)) == 0:
+                self.samples.append((float(mhz.value), int(bits.value)))
+            time.sleep(0.001)
 
     def start(self):
+        if self.nvml is not None:
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            while not self.samples and self.t.is_alive():   # sampling before the region starts
+                time.sleep(0.0005)
+            return
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -83,6 +134,14 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def stop(self):
+        if self.nvml is not None:
+            self.stop_flag.set()
+            if self.t:
+                self.t.join(timeout=2)
+            sm = [m for m, _ in self.samples]
+            reasons = sorted({n for _, b in self.samples for bit, n in self.REASONS.items() if b & bit})
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.max_mhz,
+                    "reasons": reasons, "samples": len(sm), "source": "nvml, 1 ms polling"}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -107,7 +166,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi -lms 200"}
 
 
 # ----------------------------------------------------------------- distributed
@@ -210,7 +269,7 @@ BATCH6_NCU_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batc
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fused", choices=["fused", "plain", "batch", "cddt", "learned", "glt", "radial"])
