@@ -70,6 +70,7 @@ struct rlc_map {
     float* d_dt_tiled = nullptr;
     uint16_t* d_dt16 = nullptr;
     uint8_t* d_dt8 = nullptr;
+    float* d_step = nullptr;
     std::atomic<int> refs{1};
     std::mutex mu;
 
@@ -79,6 +80,7 @@ struct rlc_map {
         cudaFree(d_dt_tiled);
         cudaFree(d_dt16);
         cudaFree(d_dt8);
+        cudaFree(d_step);
     }
     // distance transform on first use (RayMarching constructor, RangeLib.h:924)
     int ensure_dt() {
@@ -90,17 +92,20 @@ struct rlc_map {
         float* dtt = nullptr;
         uint16_t* dt16 = nullptr;
         uint8_t* dt8 = nullptr;
+        float* step = nullptr;
         void* scratch = nullptr;
         size_t sb = edt_scratch_bytes(W, H);
         cudaError_t e = cudaMalloc(&dt, (n ? n : 1) * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&dtt, (tiled ? tiled : 1) * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&dt16, (tiled ? tiled : 1) * sizeof(uint16_t));
         if (e == cudaSuccess) e = cudaMalloc(&dt8, (tiled ? tiled : 1) * sizeof(uint8_t));
+        if (e == cudaSuccess) e = cudaMalloc(&step, (n ? n : 1) * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&scratch, sb);
         if (e == cudaSuccess) e = launch_edt(d_bits, W, H, TY, dt, scratch, sb, 0);
         if (e == cudaSuccess) e = launch_dt_to_tiled(dt, W, H, dtt, 0);
         if (e == cudaSuccess) e = launch_dt_to_u16(dt, W, H, dt16, 0);
         if (e == cudaSuccess) e = launch_dt_to_u8(dt, W, H, dt8, 0);
+        if (e == cudaSuccess) e = launch_dt_to_step(dt, W, H, step, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         cudaFree(scratch);
         if (e != cudaSuccess) {
@@ -108,12 +113,14 @@ struct rlc_map {
             cudaFree(dtt);
             cudaFree(dt16);
             cudaFree(dt8);
+            cudaFree(step);
             return cuda_fail(e, "distance transform");
         }
         d_dt = dt;
         d_dt_tiled = dtt;
         d_dt16 = dt16;
         d_dt8 = dt8;
+        d_step = step;
         return RLC_OK;
     }
     void retain() { refs.fetch_add(1); }
@@ -188,6 +195,7 @@ struct rlc_method {
         p.map.dt = layout == DT_TILED ? map->d_dt_tiled : map->d_dt;   // linear for DT_U16 / DT_STAGED
         p.map.dt16 = map->d_dt16;
         p.map.dt8 = map->d_dt8;
+        p.map.step = map->d_step;
         p.map.bits = map->d_bits;
         p.cddt.td = td;
         p.cddt.td_div_2pi = td_div_2pi;
@@ -925,7 +933,7 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
 
 int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile) {
     if (int rc = check_method(m)) return rc;
-    if (dt_layout < -1 || dt_layout > 3) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2 or 3");
+    if (dt_layout < -1 || dt_layout > 4) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2, 3 or 4");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
     if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
@@ -968,7 +976,9 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
     SensorDev sm{m->d_table, m->K};
     cudaError_t err = cudaSuccess;
     const bool rm = m->dkind == K_RM;
-    for (int li = 0; li < (rm ? 3 : 1) && err == cudaSuccess; ++li) {
+    static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
+    for (int lk = 0; lk < (rm ? 4 : 1) && err == cudaSuccess; ++lk) {
+        const int li = kLayouts[lk];
         for (int pf = 0; pf < (rm ? 2 : 1) && err == cudaSuccess; ++pf) {
             for (int bi = 0; bi < 3 && err == cudaSuccess; ++bi) {
                 for (int ti = 0; ti < 3 && err == cudaSuccess; ++ti) {
@@ -1206,7 +1216,8 @@ int rlc_batch_create(const rlc_filter_desc* fd, int nf, int block, rlc_batch** o
 
 int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile) {
     if (!b) return fail(RLC_ERR_ARG, "null batch handle");
-    if (dt_layout < 0 || dt_layout > 2) return fail(RLC_ERR_ARG, "dt_layout must be 0, 1 or 2");
+    if (dt_layout < 0 || dt_layout > 4 || dt_layout == DT_STAGED)
+        return fail(RLC_ERR_ARG, "dt_layout must be 0, 1, 2 or 4");
     if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
     if (block != 0 && (block < 32 || block > 512 || block % 32)) return fail(RLC_ERR_ARG, "block must be a multiple of 32 in [32, 512]");
     if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
@@ -1253,9 +1264,10 @@ int rlc_batch_autotune(rlc_batch* b, void* stream) {
     int bl = b->layout, bp = b->prefetch, bb = b->block, bt = b->tile;
     bool bs = b->separate;
     int rc = RLC_OK;
+    static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
     for (int sp = 0; sp < 2 && !rc; ++sp)
-    for (int li = 0; li < 3 && !rc; ++li)
-        for (int pf = 0; pf < 2 && !rc; ++pf)
+    for (int lk = 0; lk < 4 && !rc; ++lk)
+        for (int pf = 0, li = kLayouts[lk]; pf < 2 && !rc; ++pf)
             for (int bi = 0; bi < 2 && !rc; ++bi)
                 for (int ti = 0; ti < 3 && !rc; ++ti) {
                     if (!b->rm_only && (li != 0 || pf != 0)) continue;

@@ -55,6 +55,7 @@ __device__ __forceinline__ float dt_at(const MapDev& m, int x, int y) {
     }
     if (LAYOUT == DT_TILED)
         return __ldg(m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7));
+    if (LAYOUT == DT_STEP) return __ldg(m.step + (size_t)x * m.H + y);   // the step itself (0 on walls)
     return __ldg(m.dt + (size_t)x * m.H + y);
 }
 
@@ -63,6 +64,7 @@ __device__ __forceinline__ const void* dt_ptr(const MapDev& m, int x, int y) {
     if (LAYOUT == DT_U16) return m.dt16 + u16_index(m, x, y);
     if (LAYOUT == DT_TILED)
         return m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7);
+    if (LAYOUT == DT_STEP) return m.step + (size_t)x * m.H + y;
     return m.dt + (size_t)x * m.H + y;
 }
 
@@ -99,9 +101,10 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
             const int qx = __float2int_rz(x0 + c * tp), qy = __float2int_rz(y0 + s * tp);
             if ((unsigned)qx < (unsigned)m.W && (unsigned)qy < (unsigned)m.H) prefetch_l1(dt_ptr<LAYOUT>(m, qx, qy));
         }
+        // DT_STEP reads the step max(d * 0.999, 1) precomputed per cell (0 where d = 0)
         const float d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
         if (steps && !out) ++*steps;
-        const float tn = __fadd_rn(t, ref_maxf(__fmul_rn(d, 0.999f), 1.0f));
+        const float tn = __fadd_rn(t, LAYOUT == DT_STEP ? d : ref_maxf(__fmul_rn(d, 0.999f), 1.0f));
         const bool hit = d <= 0.0f;
         if (out | hit | !(tn < mr)) {
             if (out || !hit) return mr;
@@ -684,6 +687,8 @@ __device__ __forceinline__ float cast_ray(const CastParams& p, const float* __re
     if (KIND == kRmOnly) return cast_one<K_RM, LAYOUT, PF>(p, ax, ay, h, ray);   // every filter ray-marches
     // mixed kinds: dispatch at run time
     if (p.kind == K_RM) {
+        if (layout == DT_STEP)
+            return pf ? cast_one<K_RM, DT_STEP, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_STEP, 0>(p, ax, ay, h, ray);
         if (layout == DT_U16)
             return pf ? cast_one<K_RM, DT_U16, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_U16, 0>(p, ax, ay, h, ray);
         if (layout == DT_TILED)
@@ -1034,10 +1039,12 @@ template <template <int, int, int> class F, class... Args>
 cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
     if (kind == K_RM) {
         if (pf) {
+            if (layout == DT_STEP) return F<K_RM, DT_STEP, kPrefetch>::run(args...);
             if (layout == DT_U16) return F<K_RM, DT_U16, kPrefetch>::run(args...);
             if (layout == DT_TILED) return F<K_RM, DT_TILED, kPrefetch>::run(args...);
             return F<K_RM, DT_LINEAR, kPrefetch>::run(args...);
         }
+        if (layout == DT_STEP) return F<K_RM, DT_STEP, 0>::run(args...);
         if (layout == DT_U16) return F<K_RM, DT_U16, 0>::run(args...);
         if (layout == DT_TILED) return F<K_RM, DT_TILED, 0>::run(args...);
         return F<K_RM, DT_LINEAR, 0>::run(args...);
@@ -1159,10 +1166,12 @@ template <bool SEP>
 static BatchKernel batch_kernel_t(bool rm_only, int layout, int pf) {
     if (!rm_only) return k_batch<kAnyKind, 0, 0, SEP>;
     if (pf) {
+        if (layout == DT_STEP) return k_batch<kRmOnly, DT_STEP, kPrefetch, SEP>;
         if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, kPrefetch, SEP>;
         if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, kPrefetch, SEP>;
         return k_batch<kRmOnly, DT_LINEAR, kPrefetch, SEP>;
     }
+    if (layout == DT_STEP) return k_batch<kRmOnly, DT_STEP, 0, SEP>;
     if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, 0, SEP>;
     if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, 0, SEP>;
     return k_batch<kRmOnly, DT_LINEAR, 0, SEP>;

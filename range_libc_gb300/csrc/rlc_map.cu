@@ -143,6 +143,16 @@ __global__ void k_dt_to_u16(const float* __restrict__ lin, int W, int H, int TY,
     out[i] = v;
 }
 
+// step of the march from each cell, RangeLib.h:957 (t += max(distance * 0.999, 1)); 0 marks an
+// occupied cell (distance 0), where the march ends
+__global__ void k_dt_to_step(const float* __restrict__ lin, long long n, float* __restrict__ step) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float d = lin[i];
+    const float v = __fmul_rn(d, 0.999f);
+    step[i] = d <= 0.0f ? 0.0f : (v < 1.0f ? 1.0f : v);
+}
+
 // 8-bit squared distance in 8x8 tiles of 64 bytes (x-major within the tile):
 // d^2 <= 254 exactly, 255 = "read the float"
 __global__ void k_dt_to_u8(const float* __restrict__ lin, int W, int H, int TY, uint8_t* __restrict__ out) {
@@ -240,6 +250,13 @@ cudaError_t launch_dt_to_u16(const float* d_lin, int W, int H, uint16_t* d_u16, 
     long long n = (long long)TX * TY * 64;
     if (n == 0) return cudaSuccess;
     k_dt_to_u16<<<blocks_for(n, 256), 256, 0, s>>>(d_lin, W, H, TY, d_u16);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dt_to_step(const float* d_lin, int W, int H, float* d_step, cudaStream_t s) {
+    const long long n = (long long)W * H;
+    if (n == 0) return cudaSuccess;
+    k_dt_to_step<<<blocks_for(n, 256), 256, 0, s>>>(d_lin, n, d_step);
     return cudaGetLastError();
 }
 
