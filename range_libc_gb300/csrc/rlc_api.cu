@@ -1111,6 +1111,7 @@ struct rlc_batch {
             it.f.weights = d.weights;
             it.f.n = d.n_particles;
             it.f.na = d.n_angles;
+            it.f.inv_na = d.n_angles > 0 ? 1.0f / (float)d.n_angles : 0.0f;
             it.f.bins = d_bins + bin_ofs;
             bin_ofs += (size_t)d.n_particles * d.n_angles;
             it.f.ppb = tile > 0 ? tile : 32;   // 32 particles: one full lane set of the product warp

@@ -38,6 +38,14 @@ constexpr int kAnyKind = -1;                        // fused_tile: kind, layout 
 constexpr int kRmOnly = -2;                         // fused_tile: every filter ray-marches (LAYOUT, PF given)
 
 __device__ __forceinline__ float ref_maxf(float a, float b) { return (a < b) ? b : a; }
+
+// r / d for 0 <= r < 2^24 and d >= 1, given inv_d = 1 / (float)d rounded to nearest: the float
+// quotient is within one of the true one, and one remainder test corrects it
+__device__ __forceinline__ int div_small(int r, int d, float inv_d) {
+    int q = __float2int_rz(__fmul_rn(__int2float_rn(r), inv_d));
+    const int rem = r - q * d;
+    return q + (rem >= d) - (rem < 0);
+}
 __device__ __forceinline__ float ref_minf(float a, float b) { return (b < a) ? b : a; }
 
 // ---------------------------------------------------------------- map access
@@ -709,8 +717,9 @@ __device__ __forceinline__ void tile_cast(const CastParams& p, const SensorDev& 
                                           const TileSmem& ts, int layout, int pf) {
     tile_obs_bins(p, sm, obs, na, ts.sri);
     const int nr = P * na;
+    const float inv_na = __frcp_rn(__int2float_rn(na));
     for (int r = threadIdx.x; r < nr; r += blockDim.x) {
-        const int li = r / na, a = r - li * na, i = first + li;
+        const int li = div_small(r, na, inv_na), a = r - li * na, i = first + li;
         if (i < n) {
             const float d = cast_ray<KIND, LAYOUT, PF>(p, ins, angles, i, a, na, layout, pf);
             if (ranges) ranges[(size_t)i * na + a] = d;
@@ -804,7 +813,7 @@ __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ 
             if (base >= (unsigned)nr) break;
             const int r = (int)base + lane;
             if (r < nr) {
-                const int li = r / na, a = r - li * na;
+                const int li = div_small(r, na, F.inv_na), a = r - li * na;
                 const float d = cast_ray<MODE, LAYOUT, PF>(F.p, F.ins, F.angles, first + li, a, na, F.layout, F.prefetch);
                 if (F.ranges) F.ranges[(size_t)(first + li) * na + a] = d;
                 bins[r] = (uint16_t)sensor_bin(d, F.sm.K, F.p.err);

@@ -155,6 +155,7 @@ struct FilterDev {
     double* weights;
     uint16_t* bins;           // n x na range bins (batch scratch)
     int n, na, ppb;           // particles, beams, particles per tile
+    float inv_na;             // 1 / (float)na rounded to nearest (tile ray -> particle, beam)
     unsigned tile_begin;      // first global tile of this filter
     unsigned part_begin;      // first global particle of this filter
 };
