@@ -281,7 +281,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", default=None,
                     help="fixed schedule instead of the autotuner (for profiling): fused 'layout,block,prefetch,tile', "
-                         "batch 'layout,prefetch,block,tile'")
+                         "batch 'layout,prefetch,block,tile[,separate products 0/1]'")
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -497,7 +497,10 @@ def run_batch(args):
             m.autotune(ins, ang, obs, w)
     batch = rl.PyFilterBatch(filters)
     if args.schedule:
-        batch.set_schedule(*[int(v) for v in args.schedule.split(",")])
+        sched = [int(v) for v in args.schedule.split(",")]
+        batch.set_schedule(*sched[:4])
+        if len(sched) > 4:   # fifth field: products overlapped (0) or in a separate launch (1)
+            batch.set_product_mode(bool(sched[4]))
     else:
         batch.autotune()
 

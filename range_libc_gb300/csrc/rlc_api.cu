@@ -1058,7 +1058,9 @@ struct rlc_batch {
     int nf = 0;
     FilterDev* d_filters = nullptr;
     unsigned* d_queue = nullptr;
-    uint16_t* d_bins = nullptr;   // every filter's n x na range bins
+    uint16_t* d_bins = nullptr;   // every filter's range bins, tile by tile (batch_tile_bins)
+    size_t bins_cap = 0;          // entries of d_bins
+    uint16_t* d_obs_bins = nullptr;   // every filter's observation bins
     unsigned total_tiles = 0;
     unsigned total_particles = 0;
     long long rays = 0;
@@ -1080,6 +1082,7 @@ struct rlc_batch {
         cudaFree(d_filters);
         cudaFree(d_queue);
         cudaFree(d_bins);
+        cudaFree(d_obs_bins);
     }
 
     // (re)build the device filter table for the current schedule
@@ -1087,12 +1090,21 @@ struct rlc_batch {
         drop_graph();
         struct Item { FilterDev f; double cost; };
         std::vector<Item> items;
-        if (!d_bins) {
-            size_t total = 0;
-            for (const rlc_filter_desc& d : descs) total += (size_t)d.n_particles * d.n_angles;
-            CUDA_OR_FAIL(cudaMalloc(&d_bins, (total ? total : 1) * sizeof(uint16_t)), "batch range bins");
+        const int ppb = tile > 0 ? tile : 32;   // 32 particles: one full lane set of the product warp
+        size_t need = 0, nobs = 0;
+        for (const rlc_filter_desc& d : descs) {
+            need += (size_t)((d.n_particles + ppb - 1) / ppb) * batch_tile_bins(d.n_angles, ppb);
+            nobs += (size_t)d.n_angles;
         }
-        size_t bin_ofs = 0;
+        if (need > bins_cap) {
+            cudaFree(d_bins);
+            d_bins = nullptr;
+            bins_cap = 0;
+            CUDA_OR_FAIL(cudaMalloc(&d_bins, (need ? need : 1) * sizeof(uint16_t)), "batch range bins");
+            bins_cap = need;
+        }
+        if (!d_obs_bins) CUDA_OR_FAIL(cudaMalloc(&d_obs_bins, (nobs ? nobs : 1) * sizeof(uint16_t)), "batch observation bins");
+        size_t bin_ofs = 0, obs_ofs = 0;
         for (const rlc_filter_desc& d : descs) {
             rlc_method* m = d.method;
             Item it{};
@@ -1112,9 +1124,11 @@ struct rlc_batch {
             it.f.n = d.n_particles;
             it.f.na = d.n_angles;
             it.f.inv_na = d.n_angles > 0 ? 1.0f / (float)d.n_angles : 0.0f;
+            it.f.ppb = ppb;
             it.f.bins = d_bins + bin_ofs;
-            bin_ofs += (size_t)d.n_particles * d.n_angles;
-            it.f.ppb = tile > 0 ? tile : 32;   // 32 particles: one full lane set of the product warp
+            bin_ofs += (size_t)((d.n_particles + ppb - 1) / ppb) * batch_tile_bins(d.n_angles, ppb);
+            it.f.obs_bins = d_obs_bins + obs_ofs;
+            obs_ofs += (size_t)d.n_angles;
             // heavier tiles first: rays per tile x march length
             it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
             items.push_back(it);

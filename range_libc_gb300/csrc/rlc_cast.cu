@@ -604,17 +604,15 @@ __device__ __forceinline__ TileSmem tile_layout(unsigned char* base, int P, int 
 // requested while group g is multiplied, so the dependent bin -> factor ->
 // multiply chain of one group no longer waits on memory.  Groups past na
 // multiply by 1.0, which leaves every double (subnormals included) as is.
-// Registers: 2 x kGroup doubles and 2 x kGroup bins.
-template <int kGroup, class SriF, class BinF>
-__device__ __forceinline__ double product_chain(const SensorDev& sm, int na, SriF sri, BinF bin) {
+// group_bins(g, b) delivers the kGroup bins of group g (entries past na are
+// not used).  Registers: 2 x kGroup doubles and 2 x kGroup bins.
+template <int kGroup, class SriF, class GroupF>
+__device__ __forceinline__ double product_chain(const SensorDev& sm, int na, SriF sri, GroupF group_bins) {
     unsigned bx[kGroup], by[kGroup];
     double f0[kGroup], f1[kGroup];
+    const int ng = (na + kGroup - 1) / kGroup;
     auto load_bins = [&](unsigned* b, int g) {
-#pragma unroll
-        for (int u = 0; u < kGroup; ++u) {
-            const int a = g * kGroup + u;
-            b[u] = a < na ? bin(a) : 0u;
-        }
+        if (g < ng) group_bins(g, b);
     };
     auto load_factors = [&](double* f, const unsigned* b, int g) {
 #pragma unroll
@@ -628,7 +626,6 @@ __device__ __forceinline__ double product_chain(const SensorDev& sm, int na, Sri
         for (int u = 0; u < kGroup; ++u) w = __dmul_rn(w, f[u]);
         return w;
     };
-    const int ng = (na + kGroup - 1) / kGroup;
     double w = 1.0;
     load_bins(bx, 0);
     load_factors(f0, bx, 0);
@@ -761,17 +758,24 @@ __global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const
 // descending per-tile cost, so heavy tiles are handed out first.  There is
 // no waiting on other blocks: a block that finds the queue exhausted
 // multiplies its last tile and exits.
-__device__ __forceinline__ void batch_products(const FilterDev& F, int first, int np) {
+// the four range bins of beams 4g .. 4g + 3 of tile particle li: one 8-byte read (batch bin layout)
+__device__ __forceinline__ void tile_bins4(const uint16_t* tile, int P, int li, int g, unsigned* b) {
+    const uint2 v = *reinterpret_cast<const uint2*>(tile + ((size_t)g * P + li) * 4);
+    b[0] = v.x & 0xFFFFu;
+    b[1] = v.x >> 16;
+    b[2] = v.y & 0xFFFFu;
+    b[3] = v.y >> 16;
+}
+
+__device__ __forceinline__ void batch_products(const FilterDev& F, int tile, int np) {
     const int lane = threadIdx.x & 31;
-    const float* obs = F.obs;
-    const float inv_s = F.p.world.inv_s;
-    const int K = F.sm.K;
-    unsigned* err = F.p.err;
+    const uint16_t* obs_bins = F.obs_bins;
+    const uint16_t* tb = F.bins + batch_tile_offset(F, tile);
+    const int P = F.ppb, first = tile * P;
     for (int li = lane; li < np; li += 32) {
-        const uint16_t* row = F.bins + (size_t)(first + li) * F.na;
         F.weights[first + li] = product_chain<4>(
-            F.sm, F.na, [&](int a) { return (unsigned)sensor_bin(__fmul_rn(__ldg(obs + a), inv_s), K, err); },
-            [&](int a) { return (unsigned)row[a]; });
+            F.sm, F.na, [&](int a) { return (unsigned)__ldg(obs_bins + a); },
+            [&](int g, unsigned* b) { tile_bins4(tb, P, li, g, b); });
     }
 }
 
@@ -783,7 +787,7 @@ __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ 
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const bool mult = threadIdx.x < 32;   // warp 0 multiplies the previous tile
-    int prev_f = -1, prev_first = 0, prev_np = 0;
+    int prev_f = -1, prev_tile = 0, prev_np = 0;
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned t = atomicAdd(queue, 1u);
@@ -799,13 +803,13 @@ __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ 
         __syncthreads();
         const unsigned t = s_tile;
         const int f = s_f;
-        if (!SEPARATE && mult && prev_f >= 0) batch_products(filters[prev_f], prev_first, prev_np);
+        if (!SEPARATE && mult && prev_f >= 0) batch_products(filters[prev_f], prev_tile, prev_np);
         if (t >= total_tiles) break;
         const FilterDev& F = filters[f];
         const int P = F.ppb, na = F.na, n = F.n;
-        const int first = (int)(t - F.tile_begin) * P;
+        const int tile = (int)(t - F.tile_begin), first = tile * P;
         const int nr = min(P, n - first) * na;
-        uint16_t* bins = F.bins + (size_t)first * na;
+        uint16_t* bins = F.bins + batch_tile_offset(F, tile);
         for (;;) {
             unsigned base = 0u;
             if (lane == 0) base = atomicAdd(&s_next, 32u);
@@ -816,12 +820,12 @@ __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ 
                 const int li = div_small(r, na, F.inv_na), a = r - li * na;
                 const float d = cast_ray<MODE, LAYOUT, PF>(F.p, F.ins, F.angles, first + li, a, na, F.layout, F.prefetch);
                 if (F.ranges) F.ranges[(size_t)(first + li) * na + a] = d;
-                bins[r] = (uint16_t)sensor_bin(d, F.sm.K, F.p.err);
+                bins[((size_t)(a >> 2) * P + li) * 4 + (a & 3)] = (uint16_t)sensor_bin(d, F.sm.K, F.p.err);
             }
         }
         __syncthreads();   // the tile's bins are written; s_tile, s_f and s_next may be reused
         prev_f = f;
-        prev_first = first;
+        prev_tile = tile;
         prev_np = min(P, n - first);
     }
 }
@@ -841,14 +845,19 @@ __global__ void __launch_bounds__(256) k_batch_products(const FilterDev* __restr
     }
     const FilterDev& F = filters[lo];
     const int i = (int)(g - F.part_begin);
-    const float* obs = F.obs;
-    const float inv_s = F.p.world.inv_s;
-    const int K = F.sm.K;
-    unsigned* err = F.p.err;
-    const uint16_t* row = F.bins + (size_t)i * F.na;
-    F.weights[i] = product_chain<8>(
-        F.sm, F.na, [&](int a) { return (unsigned)sensor_bin(__fmul_rn(__ldg(obs + a), inv_s), K, err); },
-        [&](int a) { return (unsigned)row[a]; });
+    const int P = F.ppb, tile = i / P, li = i - tile * P;
+    const uint16_t* obs_bins = F.obs_bins;
+    const uint16_t* tb = F.bins + batch_tile_offset(F, tile);
+    F.weights[i] = product_chain<4>(
+        F.sm, F.na, [&](int a) { return (unsigned)__ldg(obs_bins + a); },
+        [&](int gr, unsigned* b) { tile_bins4(tb, P, li, gr, b); });
+}
+
+// the observation bin of every beam of every filter, once per batch run (products read them)
+__global__ void k_batch_obs_bins(const FilterDev* __restrict__ filters) {
+    const FilterDev& F = filters[blockIdx.x];
+    for (int a = threadIdx.x; a < F.na; a += blockDim.x)
+        F.obs_bins[a] = (uint16_t)sensor_bin(__fmul_rn(__ldg(F.obs + a), F.p.world.inv_s), F.sm.K, F.p.err);
 }
 
 
@@ -1256,6 +1265,9 @@ cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tile
     if (total_tiles == 0 || nf == 0) return cudaSuccess;
     BatchKernel k = batch_kernel(rm_only, layout, pf, separate);
     cudaError_t e = set_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    k_batch_obs_bins<<<nf, 256, 0, s>>>(d_filters);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k<<<grid, block, smem, s>>>(d_filters, nf, total_tiles, queue);
     e = cudaGetLastError();

@@ -153,12 +153,19 @@ struct FilterDev {
     const float* obs;
     float* ranges;            // optional pixel ranges
     double* weights;
-    uint16_t* bins;           // n x na range bins (batch scratch)
+    uint16_t* bins;           // range bins (batch scratch), per tile beam-major in groups of 4 beams
+    uint16_t* obs_bins;       // na observation bins (batch scratch, written at the start of each run)
     int n, na, ppb;           // particles, beams, particles per tile
     float inv_na;             // 1 / (float)na rounded to nearest (tile ray -> particle, beam)
     unsigned tile_begin;      // first global tile of this filter
     unsigned part_begin;      // first global particle of this filter
 };
+// Range bins of a batch tile: ceil(na / 4) groups x ppb particles x 4 beams, so that a lane
+// reads a particle's four bins of one group with one 8-byte load; tiles follow one another.
+__host__ __device__ inline size_t batch_tile_bins(int na, int ppb) { return (size_t)((na + 3) >> 2) * ppb * 4; }
+__host__ __device__ inline size_t batch_tile_offset(const FilterDev& F, int tile) {
+    return (size_t)tile * batch_tile_bins(F.na, F.ppb);
+}
 // Persistent launch: `grid` blocks of `block` threads draw tiles from *queue
 // (which must be zero) until all `total_tiles` are done.  rm_only selects the
 // kernel specialised for batches whose filters all ray-march, with the
