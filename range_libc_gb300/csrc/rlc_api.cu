@@ -911,6 +911,7 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
     if (!ins || !angles) return fail(RLC_ERR_ARG, "null array");
     if (int rc = check_trig(m, (long long)n * na)) return rc;
     CastParams p = m->params();
+    p.map.dt = m->map->d_dt;   // the counting kernel marches the linear distance transform whatever the schedule
     const float* d_in = ins;
     const float* d_ang = angles;
     void* st = nullptr;

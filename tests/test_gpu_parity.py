@@ -658,3 +658,19 @@ def test_cddt_json_round_trip_full_size(rl):
     g.calc_range_many(wl.ins, r1)
     h.calc_range_many(wl.ins, r2)
     assert np.array_equal(_bits(r1), _bits(r2))
+
+
+def test_count_steps_matches_oracle_under_every_schedule(rl, oracle_mod):
+    """rlc_count_steps (the S of the roofline's algorithmic bytes) equals the oracle's march-step
+    count, whatever distance-transform layout the method is scheduled with."""
+    wl = _pf(n=300, side=512)
+    m = _pymap(rl, wl.occ, wl.world)
+    for kind in ("rm", "bl"):
+        g = (rl.PyRayMarching if kind == "rm" else rl.PyBresenhamsLine)(m, wl.max_range)
+        ref = oracle_mod.OracleMethod(wl.occ, kind, wl.max_range, world=m.world)
+        _, trig = oracle_mod.world_rays(m.world, wl.ins, wl.angles)
+        g.set_trig_override(trig)
+        exp = ref.mean_steps(wl.ins, wl.angles) * len(wl.ins) * len(wl.angles)
+        for layout in ((0, 1, 2, 3, 4) if kind == "rm" else (0,)):
+            g.set_schedule(layout, 0, 0, 0)
+            assert g.count_steps(wl.ins, wl.angles) == round(exp), (kind, layout)
