@@ -109,8 +109,15 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
             const int qx = __float2int_rz(x0 + c * tp), qy = __float2int_rz(y0 + s * tp);
             if ((unsigned)qx < (unsigned)m.W && (unsigned)qy < (unsigned)m.H) prefetch_l1(dt_ptr<LAYOUT>(m, qx, qy));
         }
-        // DT_STEP reads the step max(d * 0.999, 1) precomputed per cell (0 where d = 0)
-        const float d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
+        // DT_STEP reads the step max(d * 0.999, 1) precomputed per cell (0 where d = 0).  The
+        // linear layouts form the cell index in 32 bits (W * H < 2^31) and select it once.
+        float d;
+        if (LAYOUT == DT_LINEAR || LAYOUT == DT_STEP) {
+            const unsigned cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
+            d = __ldg((LAYOUT == DT_STEP ? m.step : m.dt) + cell);
+        } else {
+            d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
+        }
         if (steps && !out) ++*steps;
         const float tn = __fadd_rn(t, LAYOUT == DT_STEP ? d : ref_maxf(__fmul_rn(d, 0.999f), 1.0f));
         const bool hit = d <= 0.0f;
