@@ -259,9 +259,9 @@ def run_reference(args):
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one `ncu --set full` capture
 # of the same workload (profiles/k_fused_corridor2048_pf4000x61.md, profiles/k_batch_uneven32.md)
-FUSED_NCU_TRAFFIC = 511_488
+FUSED_NCU_TRAFFIC = 512_256
 FUSED_NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"
-BATCH6_NCU_TRAFFIC = 559_306_752 + 32_608_512
+BATCH6_NCU_TRAFFIC = 539_045_376 + 38_185_216
 BATCH6_NCU_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 filters "
                      "(--filters 6); the 32-filter launch is not captured")
 
