@@ -231,8 +231,16 @@ def cpu_reference_pf(wl, world, steps, warmup, budget_s, nthreads):
     return rays / el, done, el
 
 
+def pf_config(kind: str, n: int, na: int) -> dict:
+    """The `config` of the particle-filter lines (both arms)."""
+    return {"workload": f"particle-filter step ({kind}): corridor 2048^2 @0.05 m/px, "
+                        f"{n} particles x {na} beams over 270 deg, RM max_range 200 px, 201x201 f64 sensor table",
+            "particles": n, "beams": na, "map": "2048x2048 corridor, seed 2000"}
+
+
 def run_reference(args):
-    """--impl reference: the reference's CPU implementation on the host cores."""
+    """--impl reference: the reference's CPU implementation on the host cores (all threads; one
+    thread reported beside it)."""
     from range_libc_gb300 import workloads as W
     rank, ws, dist = dist_init()
     if rank != 0:
@@ -241,16 +249,18 @@ def run_reference(args):
     world = tuple(float(np.float32(v)) for v in (wl.world[0], wl.world[1], wl.world[2], wl.world[3], 0.0, 1.0))
     nthreads = os.cpu_count() or 1
     val, done, el = cpu_reference_pf(wl, world, args.steps, args.warmup, budget_s=60.0, nthreads=nthreads)
+    v1, d1, e1 = cpu_reference_pf(wl, world, 1000, 1, budget_s=5.0, nthreads=1)
+    n, na = len(wl.ins), len(wl.angles)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": 0,
         "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
-        "config": {"workload": "particle-filter step, corridor 2048^2 @0.05 m/px, 4000 particles x 61 beams, "
-                               "RM max_range 200 px, 201x201 sensor table, fused cast+sensor model",
-                   "particles": len(wl.ins), "beams": len(wl.angles)},
-        "particle_updates_per_s": val / len(wl.angles),
+        "config": pf_config(args.workload if args.workload in ("fused", "plain") else "fused", n, na),
+        "particle_updates_per_s": val / na,
         "cpu_baseline": {"value": val, "unit": "rays/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{done} full steps ({len(wl.ins)}x{len(wl.angles)} rays each)"},
+                         "sample": f"{done} full steps ({n}x{na} rays each), oracle/ C restatement, "
+                                   f"{nthreads} threads",
+                         "single_thread": {"value": v1, "sample": f"{d1} full steps in {e1:.1f} s, 1 thread"}},
         "e2e": {"value": val, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -411,22 +421,20 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        v1, d1, e1 = cpu_reference_pf(wl, omap.world, steps=1000, warmup=1, budget_s=10.0, nthreads=nthreads)
+        v1, d1, e1 = cpu_reference_pf(wl, omap.world, steps=100000, warmup=1, budget_s=10.0, nthreads=nthreads)
+        s1, sd, se = cpu_reference_pf(wl, omap.world, steps=100000, warmup=1, budget_s=3.0, nthreads=1)
         cpu = {"value": v1, "unit": "rays/s", "cores": nthreads, "kind": "port",
                "sample": f"{d1} full steps ({n}x{na} rays each) in {e1:.1f} s, oracle/ C restatement, "
-                         f"{nthreads} threads"}
+                         f"{nthreads} threads",
+               "single_thread": {"value": s1, "sample": f"{sd} full steps in {se:.1f} s, 1 thread"}}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
-            "config": {"workload": f"particle-filter step ({args.workload}): corridor 2048^2 @0.05 m/px, "
-                                   f"{n} particles x {na} beams over 270 deg, RM max_range 200 px, "
-                                   f"201x201 f64 sensor table",
-                       "particles": n, "beams": na, "map": "2048x2048 corridor, seed 2000",
-                       "l2": "flushed before every step (256 MiB write)",
-                       "schedule": dict(zip(("dt_layout", "block", "prefetch", "tile"), method.schedule()))},
+            "config": dict(pf_config(args.workload, n, na), l2="flushed before every step (256 MiB write)",
+                           schedule=dict(zip(("dt_layout", "block", "prefetch", "tile"), method.schedule()))),
             "particle_updates_per_s": value / na,
             "e2e": {"value": e2e, "unit": "rays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "particle_updates_per_s": e2e / na},
