@@ -630,7 +630,7 @@ def run_cddt(args):
         return 1
 
     per_mode = {}
-    for warp_search in (0, 1):   # per-thread and warp-cooperative bin search
+    for warp_search in (0, 1, 2):   # per-thread binary, warp-cooperative and sector bin search
         m.set_schedule(0, 0, warp_search, 0)
         for _ in range(args.warmup):
             step()
@@ -662,7 +662,8 @@ def run_cddt(args):
                 "d2h_bytes_per_step": h_out.nbytes},
         "host_equals_device": same, "gpu_launches": launches, "clocks": clk,
         "search": {"per_thread_rays_per_s": n * args.steps / (per_mode[0] / 1e3),
-                   "warp_cooperative_rays_per_s": n * args.steps / (per_mode[1] / 1e3), "chosen": int(best)},
+                   "warp_cooperative_rays_per_s": n * args.steps / (per_mode[1] / 1e3),
+                   "sector_rays_per_s": n * args.steps / (per_mode[2] / 1e3), "chosen": int(best)},
     }
     if rank == 0:
         print(json.dumps(line))

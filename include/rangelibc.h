@@ -208,9 +208,10 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
  * max(d * 0.999, 1) (0 on occupied cells), 3 = beam-major fused update that stages each bundle's
  * window of 8-bit squared distances in shared memory (RM only; tile = particle chunks per beam,
  * 0 = one block per SM) (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
- * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray, and for CDDT
- * methods a warp-cooperative bin search (32 zero points per step, ballot) in calc_range_many and
- * calc_range_repeat_angles; tile =
+ * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray; for CDDT
+ * methods prefetch selects the bin search: 0 binary, 1 warp-cooperative (32 zero points per
+ * step, ballot; calc_range_many and calc_range_repeat_angles), 2 by 32-byte sectors for bins of
+ * more than 32 zero points (fewer dependent reads; pays when queries spread over the map); tile =
  * particles per tile of the fused and batched kernels (0 = automatic).  Results are identical
  * under every schedule. */
 RLC_API int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile);

@@ -601,9 +601,13 @@ int rlc_cddt_table_load(rlc_method* m, const float* trans, const int64_t* bin_le
     uint32_t* d_st = nullptr;
     float* d_z = nullptr;
     if (int rc = upload((void**)&d_st, st.data(), st.size() * sizeof(uint32_t), "CDDT load")) return rc;
-    if (int rc = upload((void**)&d_z, zeros, (size_t)num_zeros * sizeof(float), "CDDT load")) {
+    cudaError_t ez = cudaMalloc((void**)&d_z, cddt_zeros_bytes((size_t)num_zeros));
+    if (ez == cudaSuccess && num_zeros)
+        ez = cudaMemcpy(d_z, zeros, (size_t)num_zeros * sizeof(float), cudaMemcpyHostToDevice);
+    if (ez != cudaSuccess) {
         cudaFree(d_st);
-        return rc;
+        cudaFree(d_z);
+        return cuda_fail(ez, "CDDT load");
     }
     cudaFree(m->tab.bin_start);
     cudaFree(m->tab.zeros);
@@ -937,7 +941,8 @@ int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int p
     if (dt_layout < -1 || dt_layout > 4) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2, 3 or 4");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
-    if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
+    if (prefetch < 0 || prefetch > (m->dkind == K_CDDT ? 2 : 1))
+        return fail(RLC_ERR_ARG, m->dkind == K_CDDT ? "prefetch must be 0, 1 or 2" : "prefetch must be 0 or 1");
     if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
     if (dt_layout == -1) {
         m->autotune_pending = true;
@@ -980,7 +985,9 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
     static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
     for (int lk = 0; lk < (rm ? 4 : 1) && err == cudaSuccess; ++lk) {
         const int li = kLayouts[lk];
-        for (int pf = 0; pf < (rm ? 2 : 1) && err == cudaSuccess; ++pf) {
+        // march variants: RM plain / prefetching; CDDT binary / sector search
+        for (int pk = 0; pk < (rm || m->dkind == K_CDDT ? 2 : 1) && err == cudaSuccess; ++pk) {
+            const int pf = (m->dkind == K_CDDT && pk) ? 2 : pk;
             for (int bi = 0; bi < 3 && err == cudaSuccess; ++bi) {
                 for (int ti = 0; ti < 3 && err == cudaSuccess; ++ti) {
                     if (ti > 0 && tile_particles(na, blocks[bi], tiles[ti]) == tile_particles(na, blocks[bi], 0))

@@ -224,15 +224,48 @@ __device__ __forceinline__ void cddt_discretize(const CddtDev& c, float theta, i
     flipped = fl;
 }
 
-// first index i of the sorted bin with bin[i] > v (upper) or bin[i] >= v (lower); n if none
+// first index i of the sorted bin with bin[i] > v (upper) or bin[i] >= v (lower); n if none.
+// bound_g: binary search.  bound_s (the sector schedule of CDDT methods) searches bins of more
+// than kSectorSearch entries by whole sectors: each step reads the
+// aligned 32-byte sector (8 zero points) around the midpoint with two 16-byte loads and settles
+// every entry of it that lies in [lo, hi), so a bin of n entries takes about log2(n / 8) + 1
+// dependent reads instead of log2(n), then finishes with the binary search.  It pays where the
+// reads miss the L1 (queries spread over the map); where neighbouring queries share their bins'
+// cache lines the plain search's fewer instructions win.  Zero-point arrays are allocated in whole sectors (cddt_zeros_bytes),
+// so the sector reads stay inside the allocation; entries outside [lo, hi) are never used.
+constexpr int kSectorSearch = 32;
+
 __device__ __forceinline__ int bound_g(const float* __restrict__ bin, int n, float v, bool upper) {
     int lo = 0, hi = n;
     while (lo < hi) {
-        int mid = (lo + hi) >> 1;
+        const int mid = (lo + hi) >> 1;
         const float z = __ldg(bin + mid);
         if (upper ? (v < z) : (v <= z)) hi = mid; else lo = mid + 1;
     }
     return lo;
+}
+
+__device__ __forceinline__ int bound_s(const float* __restrict__ bin, int n, float v, bool upper) {
+    int lo = 0, hi = n;
+    while (hi - lo > kSectorSearch) {
+        const int mid = (lo + hi) >> 1;
+        const uintptr_t pm = reinterpret_cast<uintptr_t>(bin + mid);
+        const float4* sec = reinterpret_cast<const float4*>(pm & ~(uintptr_t)31);
+        const int s0 = mid - (int)((pm & 31) >> 2);   // index in the bin of the sector's first entry
+        const float4 a = __ldg(sec), b = __ldg(sec + 1);
+        const float z[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        const int w0 = max(lo, s0), w1 = min(hi, s0 + 8);   // the sector's entries inside [lo, hi)
+        int k = w1;                                          // first of them at or past the bound
+#pragma unroll
+        for (int j = 7; j >= 0; --j) {
+            const int idx = s0 + j;
+            if (idx >= w0 && idx < w1 && (upper ? (v < z[j]) : (v <= z[j]))) k = idx;
+        }
+        if (k == w1) lo = w1;                 // the whole window precedes the bound
+        else if (k > w0) lo = hi = k;         // entry k - 1 precedes it and entry k does not
+        else hi = w0;                         // the bound is at or before the window's start
+    }
+    return lo + bound_g(bin + lo, hi - lo, v, upper);
 }
 
 // The same bound computed by a whole warp for one query: 32 pivots per
@@ -321,11 +354,13 @@ __device__ __forceinline__ float cddt_finish(const CastParams& p, const CddtPend
     return __fsub_rn(__ldg(q.bin + idx), q.lx);
 }
 
+template <bool SECTOR = false>
 __device__ float cddt_cast(const CastParams& p, float x, float y, float heading) {
     CddtPending q;
     const float r = cddt_front(p, x, y, heading, q);
     if (q.mode == 0) return r;
-    return cddt_finish(p, q, bound_g(q.bin, q.n, q.lx, q.mode != 3));
+    const bool upper = q.mode != 3;
+    return cddt_finish(p, q, SECTOR ? bound_s(q.bin, q.n, q.lx, upper) : bound_g(q.bin, q.n, q.lx, upper));
 }
 
 // warp-cooperative variant: every lane resolves its own query up to the bin,
@@ -447,7 +482,7 @@ __global__ void k_cddt_pair(CastParams p, float x, float y, float heading, float
 // ------------------------------------------------------------- dispatch
 template <int KIND, int LAYOUT, int PF = 0>
 __device__ __forceinline__ float cast_one(const CastParams& p, float x, float y, float h, long long ray) {
-    if (KIND == K_CDDT) return cddt_cast(p, x, y, h);
+    if (KIND == K_CDDT) return cddt_cast<PF == 2>(p, x, y, h);   // PF 2: sector search
     if (KIND == K_GLT) return glt_cast(p, x, y, h);
     float c, s;
     if (p.trig) {
@@ -523,7 +558,7 @@ template <int KIND, int LAYOUT, int PF, bool WORLD>
 __global__ void __launch_bounds__(256) k_calc_range_many(CastParams p, const float* __restrict__ ins,
                                                          float* __restrict__ outs, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (KIND == K_CDDT && PF) {   // warp-cooperative bin search: every lane of the warp takes part
+    if (KIND == K_CDDT && PF == 1) {   // warp-cooperative bin search: every lane of the warp takes part
         const bool act = i < n;
         float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f;
         if (act) { q0 = __ldg(ins + 3 * (size_t)i); q1 = __ldg(ins + 3 * (size_t)i + 1); q2 = __ldg(ins + 3 * (size_t)i + 2); }
@@ -555,7 +590,7 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
                                                        const float* __restrict__ angles,
                                                        float* __restrict__ outs, int n, int na) {
     long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (KIND == K_CDDT && PF) {   // warp-cooperative bin search
+    if (KIND == K_CDDT && PF == 1) {   // warp-cooperative bin search
         const bool act = g < (long long)n * na;
         float ax = 0.0f, ay = 0.0f, h = 0.0f;
         if (act) {
@@ -1076,7 +1111,8 @@ cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
     }
     if (kind == K_BL) return F<K_BL, DT_LINEAR, 0>::run(args...);
     if (kind == K_GLT) return F<K_GLT, DT_LINEAR, 0>::run(args...);
-    if (pf) return F<K_CDDT, DT_LINEAR, 1>::run(args...);   // warp-cooperative bin search
+    if (pf == 1) return F<K_CDDT, DT_LINEAR, 1>::run(args...);   // warp-cooperative bin search
+    if (pf == 2) return F<K_CDDT, DT_LINEAR, 2>::run(args...);   // sector search
     return F<K_CDDT, DT_LINEAR, 0>::run(args...);
 }
 

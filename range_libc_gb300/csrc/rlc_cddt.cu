@@ -485,7 +485,7 @@ cudaError_t cddt_build(const uint64_t* d_bits, int W, int H, int TY, unsigned td
     cudaError_t e = scan_exclusive_u32(ucount.as<uint32_t>(), d_bin_start, nb, s);
     uint32_t nz = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&nz, d_bin_start + nb, sizeof(uint32_t), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMalloc(&d_zeros, (size_t)(nz ? nz : 1) * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_zeros, cddt_zeros_bytes(nz));
     if (e == cudaSuccess && nb > 0) {
         k_copy_bins<<<nb, 128, 0, s>>>(start.as<uint32_t>(), raw.as<float>(), d_bin_start, d_zeros);
         e = cudaGetLastError();
@@ -560,7 +560,7 @@ cudaError_t cddt_prune(const uint64_t* d_bits, int W, int H, int TY, unsigned td
     RLC_TRY(cudaMemcpy(&nkeep, pos.as<uint32_t>() + nz, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     float* d_new = nullptr;
     uint32_t* d_new_start = nullptr;
-    RLC_TRY(cudaMalloc(&d_new, (size_t)(nkeep ? nkeep : 1) * sizeof(float)));
+    RLC_TRY(cudaMalloc(&d_new, cddt_zeros_bytes(nkeep)));
     cudaError_t e = cudaMalloc(&d_new_start, ((size_t)nb + 1) * sizeof(uint32_t));
     if (e == cudaSuccess && nz > 0) {
         k_compact_entries<<<blocks_for(nz, 256), 256, 0, s>>>(used.as<uint32_t>(), pos.as<uint32_t>(), nz,

@@ -166,6 +166,9 @@ __host__ __device__ inline size_t batch_tile_bins(int na, int ppb) { return (siz
 __host__ __device__ inline size_t batch_tile_offset(const FilterDev& F, int tile) {
     return (size_t)tile * batch_tile_bins(F.na, F.ppb);
 }
+// Bytes of a CDDT zero-point array of nz entries: whole 32-byte sectors, so that the bin search
+// may read the full sector around any entry (bound_s).
+inline size_t cddt_zeros_bytes(size_t nz) { return ((nz + 7) / 8 + (nz == 0)) * 8 * sizeof(float); }
 // Persistent launch: `grid` blocks of `block` threads draw tiles from *queue
 // (which must be zero) until all `total_tiles` are done.  rm_only selects the
 // kernel specialised for batches whose filters all ray-march, with the

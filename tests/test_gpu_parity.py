@@ -252,11 +252,44 @@ def test_cddt_table_and_queries(rl, oracle_mod, name, td):
         q = W.free_cell_queries(occ, 3000, 4) if occ.min() == 0 else _queries(occ, 3000, 4)
         q[:, 2] = np.random.default_rng(td).uniform(-10, 10, len(q))
         exp = ref.calc_range_many(q)
-        for warp_search in (0, 1):   # per-thread and warp-cooperative bin search
+        for warp_search in (0, 1, 2):   # binary, warp-cooperative and sector bin search
             g.set_schedule(0, 0, warp_search, 0)
             out = np.empty(len(q), np.float32)
             g.calc_range_many(q, out)
             assert np.array_equal(_bits(out), _bits(exp)), warp_search
+
+
+@pytest.mark.parametrize("side,td,prune", [(1024, 108, False), (1024, 107, True), (2048, 216, False)])
+def test_cddt_sector_search_long_bins(rl, oracle_mod, side, td, prune):
+    """The sector bin search where bins hold hundreds of zero points (rectangles-and-disks maps,
+    up to ~2000 per bin): every search schedule against the oracle (1024^2) or against the binary
+    search on 1M queries (2048^2), per-ray and repeat-angle calls."""
+    wl = W.cddt_queries(side=side, n=200_000 if side == 1024 else 1_000_000, td=td)
+    m = _pymap(rl, wl.occ)
+    g = rl.PyCDDTCast(m, 300.0, td)
+    if prune:
+        g.prune()
+    assert np.max(g.table()[2]) > 64   # bins long enough for several sector steps
+    if side == 1024:
+        ref = oracle_mod.OracleMethod(wl.occ, "pcddt" if prune else "cddt", 300.0, td=td, nthreads=os.cpu_count() or 1)
+        exp = ref.calc_range_many(wl.ins[:50_000], nthreads=os.cpu_count() or 1)
+    outs = {}
+    for mode in (0, 1, 2):
+        g.set_schedule(0, 0, mode, 0)
+        out = np.empty(len(wl.ins), np.float32)
+        g.calc_range_many(wl.ins, out)
+        outs[mode] = out
+        if side == 1024:
+            assert np.array_equal(_bits(out[:50_000]), _bits(exp)), mode
+    assert np.array_equal(_bits(outs[2]), _bits(outs[0])) and np.array_equal(_bits(outs[1]), _bits(outs[0]))
+    angles = W.laser_angles(31)
+    ra = {}
+    for mode in (0, 2):
+        g.set_schedule(0, 0, mode, 0)
+        r = np.empty(2000 * 31, np.float32)
+        g.calc_range_repeat_angles(wl.ins[:2000], angles, r)
+        ra[mode] = r
+    assert np.array_equal(_bits(ra[0]), _bits(ra[2]))
 
 
 def test_cddt_given_table(rl, oracle_mod):
