@@ -1254,12 +1254,8 @@ cudaError_t launch_fused_staged(const CastParams& p, const SensorDev& sm, const 
     }
     const int P = (n + chunks - 1) / chunks;
     const size_t smem = 1024 + kStagedWindow;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_bm_cast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    if (cudaError_t e = ensure_smem_attr(k_bm_cast, (int)smem, attr)) return e;
     dim3 grid(na, (n + P - 1) / P);
     k_bm_cast<<<grid, kStagedThreads, smem, s>>>(p, sm, ins, angles, n, na, P, bins, kStagedWindow / 64);
     cudaError_t e = cudaGetLastError();

@@ -16,6 +16,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <stdint.h>
 
 struct rlc_method;
@@ -166,6 +168,20 @@ __host__ __device__ inline size_t batch_tile_bins(int na, int ppb) { return (siz
 __host__ __device__ inline size_t batch_tile_offset(const FilterDev& F, int tile) {
     return (size_t)tile * batch_tile_bins(F.na, F.ppb);
 }
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) of `kernel` once per device (the attribute
+// belongs to the device's context); `done` holds one bit per device already set.
+template <class K>
+inline cudaError_t ensure_smem_attr(K kernel, int bytes, std::atomic<unsigned long long>& done) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_release);
+    return e;
+}
+
 // Bytes of a CDDT zero-point array of nz entries: whole 32-byte sectors, so that the bin search
 // may read the full sector around any entry (bound_s).
 inline size_t cddt_zeros_bytes(size_t nz) { return ((nz + 7) / 8 + (nz == 0)) * 8 * sizeof(float); }

@@ -214,12 +214,8 @@ cudaError_t gemm(GemmArgs g, cudaStream_t s) {
     if (g.ksplit <= 0) g.ksplit = g.K;
     if (g.K % g.ksplit || g.ksplit % tc::kKChunk) return cudaErrorInvalidValue;
     if (g.ksplit != g.K && g.epi != EPI_F32_ADD) return cudaErrorInvalidValue;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    if (cudaError_t e = ensure_smem_attr(k_gemm, (int)kGemmSmem, attr)) return e;
     dim3 grid(g.N / kBN, g.M / kBM, g.K / g.ksplit);
     k_gemm<<<grid, 128, kGemmSmem, s>>>(g);
     return cudaGetLastError();
@@ -495,12 +491,8 @@ __global__ void __launch_bounds__(kFwdThreads, 2) k_mlp_forward(FeatParams fp, c
 cudaError_t mlp_forward(const FeatParams& fp, const float* xyt, int n, const bf16* wbf, const float* params, float* y,
                         unsigned* err, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    if (cudaError_t e = ensure_smem_attr(k_mlp_forward, (int)kFwdSmem, attr)) return e;
     k_mlp_forward<<<(n + kBM - 1) / kBM, kFwdThreads, kFwdSmem, s>>>(fp, xyt, n, wbf, params, y, err);
     return cudaGetLastError();
 }
