@@ -268,7 +268,7 @@ def run_reference(args):
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one `ncu --set full` capture
-# of the same workload (profiles/k_fused_corridor2048_pf4000x61.md, profiles/k_batch_uneven32.md)
+# of the same workload (the k_fused and k_batch summaries under profiles/)
 FUSED_NCU_TRAFFIC = 512_256
 FUSED_NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"
 BATCH6_NCU_TRAFFIC = 539_045_376 + 38_185_216
