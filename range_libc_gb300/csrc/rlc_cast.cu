@@ -416,7 +416,8 @@ __device__ __forceinline__ float glt_cast(const CastParams& p, float x, float y,
     return __fmul_rn(__int2float_rn(__ldg(g.lut + cell * g.td + b)), g.max_div_limits);
 }
 
-// one ray per (cell corner, angle bin), angle bins fastest: lut[(x * H + y) * td + i]
+// one ray per (cell corner, angle bin), angle bins fastest: lut[(x * H + y) * td + i]; the march reads
+// the per-cell step map (the same steps as the distance transform's, two instructions fewer)
 __global__ void __launch_bounds__(256) k_glt_build(MapDev m, float mr, unsigned td, const float* __restrict__ cosv,
                                                    const float* __restrict__ sinv, float limits_div_max,
                                                    uint16_t* __restrict__ lut, long long total) {
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(256) k_glt_build(MapDev m, float mr, unsigned 
     const long long cell = idx / td;
     const int i = (int)(idx - cell * td);
     const int x = (int)(cell / m.H), y = (int)(cell - (long long)x * m.H);
-    float r = rm_cast<DT_LINEAR, 0>(m, mr, __int2float_rn(x), __int2float_rn(y), __ldg(cosv + i), __ldg(sinv + i));
+    float r = rm_cast<DT_STEP, 0>(m, mr, __int2float_rn(x), __int2float_rn(y), __ldg(cosv + i), __ldg(sinv + i));
     r = r < mr ? r : mr;   // std::min(max_range, r)
     lut[idx] = (uint16_t)__float2uint_rz(__fmul_rn(r, limits_div_max));
 }
