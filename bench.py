@@ -513,8 +513,8 @@ def run_batch(args):
         batch.autotune()
 
     def batched():
-        batch.run()
-        return 1
+        batch.run()   # one graph: observation bins, the persistent cast (+ the products launch when separate)
+        return 3 if batch.product_mode() == "separate" else 2
 
     def per_filter_fused():
         for m, ins, ang, obs, w in filters:
