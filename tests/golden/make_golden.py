@@ -17,7 +17,9 @@ sensor tables, what the reference's own classes return:
     particle-filter map and poses;
   * a GiantLUTCast table (giant_lut) and its calc_range queries;
   * CDDTCast::serializeJson documents (unpruned and pruned), one of them for a
-    map loaded from a PNG so that its "path" field is set.
+    map loaded from a PNG so that its "path" field is set;
+  * the reference's published benchmark map (basement_hallways_5cm, 1200^2) in a
+    ROS world frame: every method's ranges and checksums of the CDDT tables.
 
 Alongside, it stores the per-ray cosf/sinf of every BL/RM heading and the
 cosf/sinf of every CDDT slice angle as this host's libm computes them, so a
@@ -184,6 +186,37 @@ def case_pairs_radial_glt(out):
     out["glt/ranges"] = np.array([g.calc_range(*v) for v in qg], np.float32)
 
 
+def _table_sums(m):
+    widths, trans, bin_len, zeros = m.cddt_table()
+    return np.array([len(bin_len), len(zeros), float(np.sum(zeros.astype(np.float64))),
+                     float(np.sum(bin_len.astype(np.float64) * np.arange(len(bin_len)))),
+                     float(np.sum(trans.astype(np.float64)))], np.float64)
+
+
+def case_basement(out):
+    """The reference's published benchmark map (maps/basement_hallways_5cm.png, 1200^2, max_range
+    500 px, theta_discretization 108 as in its main.cpp) in a ROS world frame at 0.05 m/px: ranges
+    of every method for free-cell queries, and checksums of the CDDT / PCDDT tables."""
+    rm_ = O.RefMap(png=os.path.join(REF, "maps", "basement_hallways_5cm.png"), threshold=128.0)
+    occ = rm_.occ
+    world = O.world_tuple(0.05, 0.0, -30.0, -20.0)
+    wmap = O.RefMap(occ, world=world)
+    g = free_queries(occ, 4000, 71)
+    q = g.copy()
+    q[:, 0], q[:, 1] = W.grid_to_world(g[:, 0].astype(np.float64), g[:, 1].astype(np.float64), world)
+    _, trig = O.world_rays(world, q)
+    out["basement/occ"] = occ
+    out["basement/world"] = np.array(world, np.float32)
+    out["basement/ins"] = q
+    out["basement/trig"] = trig
+    out["basement/slice_trig_108"] = slice_trig(108)
+    for kind in ("bl", "rm", "cddt", "pcddt"):
+        m = O.RefMethod(wmap, kind, 500.0, 108)
+        out[f"basement/{kind}/many"] = m.calc_range_many(q)
+        if kind in ("cddt", "pcddt"):
+            out[f"basement/{kind}/table_sums"] = _table_sums(m)
+
+
 def case_json(out):
     here = os.getcwd()
     os.chdir(os.path.join(REF, "maps"))   # the document records the PNG path as given
@@ -224,6 +257,7 @@ def main():
     case_particle_filter(out)
     case_pairs_radial_glt(out)
     case_json(out)
+    case_basement(out)
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path}: {len(out)} arrays, {os.path.getsize(path) / 1e6:.2f} MB")

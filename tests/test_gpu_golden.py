@@ -22,7 +22,7 @@ def gold():
 
 def _names(gold):
     return sorted({k.split("/")[0] for k in gold
-                   if k.endswith("/occ") and k.count("/") == 1 and k not in ("pf/occ", "glt/occ")})
+                   if k.endswith("/occ") and k.count("/") == 1 and k not in ("pf/occ", "glt/occ", "basement/occ")})
 
 
 def _bits(a):
@@ -179,3 +179,31 @@ def test_cddt_json(rl, gold, case):
     assert np.allclose(u.table()[3], z, rtol=6e-7, atol=0)
     with pytest.raises(ValueError):
         rl.PyCDDTCast(_map(rl, occ), 25.0, td + 1).load_json(ref)
+
+
+def test_basement_benchmark_map(rl, gold):
+    """The reference's published benchmark map (basement_hallways_5cm, 1200^2, max_range 500,
+    td 108) in a ROS frame: every method's ranges and the CDDT / PCDDT table checksums."""
+    occ, world = gold["basement/occ"], gold["basement/world"]
+    q = gold["basement/ins"]
+    for kind, cls in (("bl", rl.PyBresenhamsLine), ("rm", rl.PyRayMarching)):
+        g = cls(_map(rl, occ, world), 500.0)
+        g.set_trig_override(gold["basement/trig"])
+        out = np.empty(len(q), np.float32)
+        g.calc_range_many(q, out)
+        assert np.array_equal(_bits(out), _bits(gold[f"basement/{kind}/many"])), kind
+    t = gold["basement/slice_trig_108"]
+    for kind in ("cddt", "pcddt"):
+        g = rl.PyCDDTCast(_map(rl, occ, world), 500.0, 108, trig=(t[:, 0], t[:, 1]))
+        if kind == "pcddt":
+            g.prune()
+        for search in (0, 2):
+            g.set_schedule(0, 0, search, 0)
+            out = np.empty(len(q), np.float32)
+            g.calc_range_many(q, out)
+            assert np.array_equal(_bits(out), _bits(gold[f"basement/{kind}/many"])), (kind, search)
+        w, tr, bl, z = g.table()
+        sums = np.array([len(bl), len(z), float(np.sum(z.astype(np.float64))),
+                         float(np.sum(bl.astype(np.float64) * np.arange(len(bl)))),
+                         float(np.sum(tr.astype(np.float64)))], np.float64)
+        assert np.array_equal(sums, gold[f"basement/{kind}/table_sums"]), kind

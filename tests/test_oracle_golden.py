@@ -21,7 +21,7 @@ def gold():
 
 def _names(gold):
     return sorted({k.split("/")[0] for k in gold
-                   if k.endswith("/occ") and k.count("/") == 1 and k not in ("pf/occ", "glt/occ")})
+                   if k.endswith("/occ") and k.count("/") == 1 and k not in ("pf/occ", "glt/occ", "basement/occ")})
 
 
 def _bits(a):
@@ -158,3 +158,30 @@ def test_cddt_json(gold, oracle_mod, case):
     assert cddt_json_dumps(td, d["max_range"], t, w, bl, z, occ, d["path"], precision=7) == ref
     assert np.array_equal(d["widths"], w) and np.array_equal(d["bin_len"], bl)
     assert np.allclose(d["zeros"], z, rtol=6e-7, atol=0)   # 7 significant digits
+
+
+def _table_sums(widths, trans, bin_len, zeros):
+    return np.array([len(bin_len), len(zeros), float(np.sum(zeros.astype(np.float64))),
+                     float(np.sum(bin_len.astype(np.float64) * np.arange(len(bin_len)))),
+                     float(np.sum(trans.astype(np.float64)))], np.float64)
+
+
+def test_basement_benchmark_map(gold, oracle_mod):
+    """The reference's published benchmark map (basement_hallways_5cm, 1200^2, max_range 500,
+    td 108) in a ROS frame: BL / RM ranges with the recorded per-ray trig; CDDT / PCDDT ranges and
+    table checksums where this host's slice trig is the recorded one."""
+    occ = gold["basement/occ"]
+    world = tuple(float(v) for v in gold["basement/world"])
+    q, trig = gold["basement/ins"], gold["basement/trig"]
+    xyh, _ = oracle_mod.world_rays(world, q)
+    for kind in ("bl", "rm"):
+        m = oracle_mod.OracleMethod(occ, kind, 500.0, world=world)
+        out = np.array([m.calc_range_trig(float(a), float(b), float(c), float(d))
+                        for (a, b, _), (c, d) in zip(xyh, trig)], np.float32) * np.float32(world[0])
+        assert np.array_equal(_bits(out.astype(np.float32)), _bits(gold[f"basement/{kind}/many"])), kind
+    if not np.array_equal(_host_slice_trig(108), gold["basement/slice_trig_108"]):
+        pytest.skip("this host's cosf/sinf of the slice angles differ from the recorded ones")
+    for kind in ("cddt", "pcddt"):
+        m = oracle_mod.OracleMethod(occ, kind, 500.0, td=108, world=world, nthreads=os.cpu_count() or 1)
+        assert np.array_equal(_bits(m.calc_range_many(q)), _bits(gold[f"basement/{kind}/many"])), kind
+        assert np.array_equal(_table_sums(*m.cddt_table()), gold[f"basement/{kind}/table_sums"]), kind
