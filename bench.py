@@ -18,7 +18,8 @@ Other workloads (--workload): plain (cast to ranges, then the separate
 sensor model), batch (32 uneven filters in one persistent launch),
 cddt (1M queries, td 108/216, 2048^2 map, --prune for PCDDT), glt
 (GiantLUTCast build + 1M queries), radial (CDDT radial pairs), learned
-(the MLP surrogate).
+(the MLP surrogate), published (the reference's own random / grid query
+benchmark on its basement map, every method, its published figures beside).
 
 --impl reference times the reference algorithm on the host cores instead
 (the C restatement in oracle/, all threads).  Multi-GPU: every rank runs
@@ -276,13 +277,107 @@ BATCH6_NCU_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batc
                      "(--filters 6); the 32-filter launch is not captured")
 
 
+# The reference's published single-call figures (Jetson TX1; CPU methods on one thread, RMGPU on
+# its GPU) for its own benchmark: maps/basement_hallways_5cm.png, max_range 500, theta_disc 108,
+# queries per second of Benchmark::random_sample and grid_sample.
+PUBLISHED_TX1 = {"bl": (297e3, 360e3), "rm": (1.17e6, 1.6e6), "rmgpu": (18e6, 28e6), "cddt": (2.09e6, 4.25e6),
+                 "pcddt": (2.26e6, 4.47e6), "glt": (2.16e6, 4.85e6)}
+
+
+def run_published(args):
+    """The reference's own benchmark on its own map, with the published figures beside ours:
+    basement_hallways_5cm (1200^2, the reference's PNG loaded by its own loader, kept as a golden
+    fixture), max_range 500 px, theta_discretization 108; `random`: queries x ~ U[1, W-1),
+    y ~ U[1, H-1), theta ~ U[0, 2 pi) (Benchmark::random_sample, 10x its 200,000 queries per step);
+    `grid`: every 10 px in x and y at 40 angles i * 2 pi / 40 (Benchmark::get_grid_samples,
+    576,000 queries).  calc_range in the grid frame (no world transform), device-resident queries,
+    CUDA events per call, L2 flushed before each."""
+    import torch
+    import range_libc_gb300.range_libc as rl
+    from range_libc_gb300 import _lib
+
+    rank, ws, dist = dist_init()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "reference_vectors.npz"))
+    occ = gold["basement/occ"]
+    W_, H_ = occ.shape
+    omap = rl.PyOMap(np.ascontiguousarray(occ.T))
+    rng = np.random.default_rng(1903)
+    n_rand = 2_000_000
+    qr = np.stack([rng.uniform(1.0, W_ - 1.0, n_rand), rng.uniform(1.0, H_ - 1.0, n_rand),
+                   rng.uniform(0.0, 6.28318530718, n_rand)], 1).astype(np.float32)
+    coeff = np.float32(2.0 * math.pi / 40)
+    gx, gy = np.meshgrid(np.arange(0, W_, 10), np.arange(0, H_, 10), indexing="ij")
+    qg = np.concatenate([np.stack([gx.ravel(), gy.ravel(), np.full(gx.size, np.float32(i) * coeff)], 1)
+                         for i in range(40)]).astype(np.float32)
+    t0 = time.perf_counter()
+    methods = {"bl": rl.PyBresenhamsLine(omap, 500.0), "rm": rl.PyRayMarchingGPU(omap, 500.0),
+               "cddt": rl.PyCDDTCast(omap, 500.0, 108)}
+    pc = rl.PyCDDTCast(omap, 500.0, 108)
+    pc.prune()
+    methods["pcddt"] = pc
+    methods["glt"] = rl.PyGiantLUTCast(omap, 500.0, 108)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    dq = {"random": torch.from_numpy(qr).to(dev), "grid": torch.from_numpy(qg).to(dev)}
+    outs = {k: torch.empty(len(v), dtype=torch.float32, device=dev) for k, v in dq.items()}
+    res, launches = {}, 0
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    for name, m in methods.items():
+        res[name] = {}
+        for bench_name, q in dq.items():
+            o = outs[bench_name]
+            best = None
+            for search in ((0, 2) if name in ("cddt", "pcddt") else (0,)):   # CDDT: binary / sector search
+                if name in ("cddt", "pcddt"):
+                    m.set_schedule(0, 0, search, 0)
+
+                def step():
+                    _lib.call("rlc_calc_range_many", m.handle, C_vp(q.data_ptr()), C_vp(o.data_ptr()), len(q),
+                              _lib.RLC_NO_WORLD | _lib.RLC_DEVICE_PTRS, C_vp(stream.cuda_stream))
+                    return 1
+                for _ in range(args.warmup):
+                    step()
+                t, nl = _event_steps(torch, stream, args.steps, flush, step)
+                launches += nl
+                rate = len(q) * args.steps / (sum(t) / 1e3)
+                best = rate if best is None else max(best, rate)
+            pub = PUBLISHED_TX1["rmgpu" if name == "rm" else name][0 if bench_name == "random" else 1]
+            res[name][bench_name] = {"queries_per_s": best, "published_tx1": pub, "ratio": best / pub}
+    clk = clocks.stop()
+    if rank != 0:
+        return 0
+    value = res["rm"]["random"]["queries_per_s"] * ws
+    line = {
+        "metric": "queries/s of the reference's random_sample benchmark (RM; every method beside it)", "value": value,
+        "unit": "queries/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": value / PUBLISHED_TX1["rmgpu"][0], "dtype": "f32", "data": "the reference's map",
+        "config": {"workload": "reference benchmark: basement_hallways_5cm 1200^2, max_range 500, theta_disc 108, "
+                               f"random {n_rand} / grid {len(qg)} queries per call",
+                   "l2": "flushed before every call (256 MiB write)",
+                   "baseline": "published Jetson TX1 figures (RMGPU on its GPU, CPU methods on one thread)"},
+        "methods": res, "setup_s": setup_s, "gpu_launches": launches, "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def C_vp(v):
+    import ctypes
+    return ctypes.c_void_p(v)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="fused", choices=["fused", "plain", "batch", "cddt", "learned", "glt", "radial"])
+    ap.add_argument("--workload", default="fused",
+                    choices=["fused", "plain", "batch", "cddt", "learned", "glt", "radial", "published"])
     ap.add_argument("--train-rays", type=int, default=64_000_000, help="learned workload: training rays")
     ap.add_argument("--td", type=int, default=108, help="cddt workload: theta discretization")
     ap.add_argument("--prune", action="store_true", help="cddt workload: pruned table (PCDDT)")
@@ -308,6 +403,8 @@ def main():
         return run_glt(args)
     if args.workload == "radial":
         return run_radial(args)
+    if args.workload == "published":
+        return run_published(args)
 
     import torch
     import range_libc_gb300.range_libc as rl
