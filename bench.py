@@ -350,6 +350,18 @@ def run_published(args):
     clk = clocks.stop()
     if rank != 0:
         return 0
+    cpu = None
+    if not args.no_cpu_baseline:   # the oracle (C restatement of the reference) on one host thread
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build(reference=False)
+        cpu = {}
+        sample = qr[:100_000]
+        for name in ("bl", "rm", "cddt", "pcddt"):
+            om = O.OracleMethod(occ, name, 500.0, td=108, nthreads=os.cpu_count() or 1)
+            t0 = time.perf_counter()
+            om.calc_range_many_raw(sample, nthreads=1)
+            cpu[name] = len(sample) / (time.perf_counter() - t0)
     value = res["rm"]["random"]["queries_per_s"] * ws
     line = {
         "metric": "queries/s of the reference's random_sample benchmark (RM; every method beside it)", "value": value,
@@ -360,6 +372,10 @@ def run_published(args):
                    "l2": "flushed before every call (256 MiB write)",
                    "baseline": "published Jetson TX1 figures (RMGPU on its GPU, CPU methods on one thread)"},
         "methods": res, "setup_s": setup_s, "gpu_launches": launches, "clocks": clk,
+        "cpu_baseline": None if cpu is None else {
+            "value": cpu["rm"], "unit": "queries/s", "cores": 1, "kind": "port",
+            "sample": "100,000 of the random queries, oracle/ C restatement, one thread, per method",
+            "methods": cpu},
     }
     print(json.dumps(line))
     return 0
