@@ -10,7 +10,7 @@ import ctypes as C
 import os
 import threading
 
-from .build import LIB_PATH as _LIB_PATH, build as _build_library
+from .build import LIB_PATH as _LIB_PATH, build as _build_library, fast_module_path as _fast_module_path
 
 RLC_OK, RLC_ERR_ARG, RLC_ERR_CUDA, RLC_ERR_STATE, RLC_ERR_NOMEM, RLC_ERR_IO = range(6)
 RLC_BL, RLC_RM, RLC_CDDT, RLC_PCDDT, RLC_RMGPU, RLC_GLT = range(6)
@@ -137,6 +137,31 @@ def lib():
                 raise RuntimeError(f"{path}: ABI version {v}, expected {ABI_VERSION}")
             _lib = L
     return _lib
+
+
+_fast = None   # None: not looked for yet; False: not built
+
+
+def fast():
+    """The CPython entry points of the per-call methods (csrc/rlc_py.c), or None where they were
+    not built.  They call the same C ABI; -1 from them means "argument not a plain buffer of the
+    expected type and shape", and the caller takes its checked ctypes path."""
+    global _fast
+    if _fast is None:
+        lib()   # the library first, so that the module binds to this loaded copy
+        mod = False
+        path = _fast_module_path()
+        if os.path.exists(path):
+            import importlib.util
+            try:
+                spec = importlib.util.spec_from_file_location("_rlcfast", path)
+                m = importlib.util.module_from_spec(spec)
+                spec.loader.exec_module(m)
+                mod = m
+            except ImportError:
+                mod = False
+        _fast = mod
+    return _fast or None
 
 
 def check(rc: int) -> None:

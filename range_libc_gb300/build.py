@@ -14,6 +14,7 @@ import platform
 import shutil
 import subprocess
 import sys
+import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
@@ -75,8 +76,37 @@ def build(verbose: bool = False, force: bool = False) -> str:
             if verbose and err:
                 print(err, file=sys.stderr)
     if force or jobs or _stale(LIB_PATH, objs):
-        run([nvcc(), "-shared", "-o", LIB_PATH] + objs + ARCH + ["-cudart", "shared"])
+        run([nvcc(), "-shared", "-o", LIB_PATH] + objs + ARCH +
+            ["-cudart", "shared", "-Xlinker", f"-soname,{LIB_NAME}"])
+    build_fast(verbose, force)
     return LIB_PATH
+
+
+FAST_SRC = os.path.join(CSRC, "rlc_py.c")
+
+
+def fast_module_path() -> str:
+    return os.path.join(BUILD, "_rlcfast" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+
+
+def build_fast(verbose: bool = False, force: bool = False):
+    """The CPython entry points of the per-call methods (csrc/rlc_py.c) beside the library, linked
+    to it; None where Python's headers or a C compiler are absent (the ctypes path serves then)."""
+    inc = sysconfig.get_paths().get("include")
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not inc or not os.path.exists(os.path.join(inc, "Python.h")) or not cc:
+        return None
+    out = fast_module_path()
+    if not force and not _stale(out, [FAST_SRC, os.path.join(INCLUDE, "rangelibc.h"), LIB_PATH]):
+        return out
+    cmd = [cc, "-O2", "-shared", "-fPIC", "-I", inc, "-I", INCLUDE, FAST_SRC, "-o", out,
+           "-L", BUILD, "-lrangelibc_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        if verbose:
+            print(f"CPython entry points not built:\n{r.stderr}", file=sys.stderr)
+        return None
+    return out
 
 
 if __name__ == "__main__":

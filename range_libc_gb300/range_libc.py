@@ -327,6 +327,11 @@ class _RangeMethod:
         return out.value
 
     def calc_range_many(self, ins, outs) -> None:
+        F = _lib.fast()
+        if F is not None:   # numpy buffers straight to the C ABI; -1: not a plain buffer, check below
+            rc = F.calc_range_many(self._h.value, ins, outs)
+            if rc != -1:
+                return _lib.check(rc)
         pi, di = _arg(ins, np.float32, 2, "ins")
         po, do = _arg(outs, np.float32, 1, "outs")
         flags, stream = _flags_stream([di, do], ins)
@@ -336,6 +341,11 @@ class _RangeMethod:
         call("rlc_calc_range_many", self._h, pi, po, n, flags, stream)
 
     def calc_range_repeat_angles(self, ins, angles, outs) -> None:
+        F = _lib.fast()
+        if F is not None:
+            rc = F.repeat_angles(self._h.value, ins, angles, outs)
+            if rc != -1:
+                return _lib.check(rc)
         pi, di = _arg(ins, np.float32, 2, "ins")
         pa, da = _arg(angles, np.float32, 1, "angles")
         po, do = _arg(outs, np.float32, 1, "outs")
@@ -356,6 +366,11 @@ class _RangeMethod:
         self._table_width = t.shape[0]
 
     def eval_sensor_model(self, observation, ranges, outs, num_rays: int, num_particles: int) -> None:
+        F = _lib.fast()
+        if F is not None:
+            rc = F.eval_sensor_model(self._h.value, observation, ranges, outs, num_rays, num_particles)
+            if rc != -1:
+                return _lib.check(rc)
         po, do = _arg(observation, np.float32, 1, "observation")
         pr, dr = _arg(ranges, np.float32, 1, "ranges")
         pw, dw = _arg(outs, np.float64, 1, "outs")
@@ -365,6 +380,11 @@ class _RangeMethod:
         call("rlc_eval_sensor_model", self._h, po, pr, pw, int(num_rays), int(num_particles), flags, stream)
 
     def calc_range_repeat_angles_eval_sensor_model(self, ins, angles, obs, weights) -> None:
+        F = _lib.fast()
+        if F is not None:
+            rc = F.fused(self._h.value, ins, angles, obs, weights)
+            if rc != -1:
+                return _lib.check(rc)
         pi, di = _arg(ins, np.float32, 2, "ins")
         pa, da = _arg(angles, np.float32, 1, "angles")
         po, do = _arg(obs, np.float32, 1, "obs")
