@@ -69,3 +69,27 @@ def test_python_module_fails_loudly_without_a_device(L):
         pytest.skip("a device is visible")
     with pytest.raises(rl._lib.RangeLibError):
         rl.PyOMap(4, 4)
+
+
+def test_cpython_entry_points(L):
+    """The CPython module of the per-call methods (csrc/rlc_py.c): it is built beside the library,
+    passes the C ABI's status through (a null handle is RLC_ERR_ARG) and returns -1 -- "take the
+    checked path" -- for anything that is not a C-contiguous buffer of the expected type and rank."""
+    import numpy as np
+    from range_libc_gb300 import _lib
+    F = _lib.fast()
+    assert F is not None and os.path.dirname(F.__file__) == os.path.dirname(_lib.library_path())
+    ins, ang, obs = np.zeros((10, 3), np.float32), np.zeros(5, np.float32), np.zeros(5, np.float32)
+    w, r = np.zeros(10, np.float64), np.zeros(50, np.float32)
+    assert F.fused(0, ins, ang, obs, w) == _lib.RLC_ERR_ARG
+    assert F.repeat_angles(0, ins, ang, r) == _lib.RLC_ERR_ARG
+    assert F.calc_range_many(0, ins, r[:10]) == _lib.RLC_ERR_ARG
+    assert F.eval_sensor_model(0, obs, r, w, 5, 10) == _lib.RLC_ERR_ARG
+    assert F.fused(0, ins.astype(np.float64), ang, obs, w) == -1      # dtype
+    assert F.fused(0, ins[:, :2], ang, obs, w) == -1                  # not contiguous
+    assert F.fused(0, ins, ang, obs, w.astype(np.float32)) == -1      # weights must be float64
+    assert F.fused(0, ins, ang, obs[:3], w) == -1                     # too few observations
+    ro = np.zeros(10, np.float64)
+    ro.flags.writeable = False
+    assert F.fused(0, ins, ang, obs, ro) == -1                        # read-only output
+    assert F.repeat_angles(0, ins, ang, [0.0] * 50) == -1             # not a buffer
