@@ -813,5 +813,5 @@ double orc_mean_steps(const orc_method* m, const float* ins, const float* angles
             total += s;
         }
     }
-    return (n * per) ? total / ((double)n * per) : 0.0;
+    return (n > 0 && per > 0) ? total / ((double)n * per) : 0.0;
 }
