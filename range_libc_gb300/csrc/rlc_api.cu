@@ -449,7 +449,7 @@ static int glt_build(rlc_method* m, const float* cos_tab, const float* sin_tab) 
     int rc = upload((void**)&m->d_cos, m->h_cos.data(), m->td * sizeof(float), "GLT cos");
     if (!rc) rc = upload((void**)&m->d_sin, m->h_sin.data(), m->td * sizeof(float), "GLT sin");
     if (rc) return rc;
-    cudaError_t e = cudaMalloc(&m->d_lut, (cells * m->td ? cells * m->td : 1) * sizeof(uint16_t));
+    cudaError_t e = cudaMalloc(&m->d_lut, (cells * m->td > 0 ? cells * m->td : 1) * sizeof(uint16_t));
     if (e != cudaSuccess) {
         m->d_lut = nullptr;
         return fail(RLC_ERR_NOMEM, "GiantLUTCast table of %zu bytes: %s", cells * m->td * sizeof(uint16_t),
@@ -655,7 +655,7 @@ int rlc_cddt_calc_range_pair(rlc_method* m, float x, float y, float heading, flo
     if (int rc = check_method(m)) return rc;
     if (m->dkind != K_CDDT) return fail(RLC_ERR_STATE, "calc_range_pair applies to CDDT methods");
     if (!r || !r_inv) return fail(RLC_ERR_ARG, "null output");
-    void* st;
+    void* st = nullptr;
     if (int rc = m->stage(2 * sizeof(float), &st)) return rc;
     CastParams p = m->params();
     CUDA_OR_FAIL(launch_cddt_pair(p, x, y, heading, (float*)st, 0), "calc_range_pair");
@@ -698,7 +698,7 @@ int rlc_cddt_calc_range_many_radial(rlc_method* m, const float* ins, float* outs
     const size_t b_ang = align256(ang.size() * sizeof(float));
     const size_t b_in = (flags & RLC_DEVICE_PTRS) ? 0 : align256((size_t)n * 3 * sizeof(float));
     const size_t b_out = (flags & RLC_DEVICE_PTRS) ? 0 : (size_t)n * num_rays * sizeof(float);
-    void* st;
+    void* st = nullptr;
     if (int rc = m->stage(b_ang + b_in + b_out, &st)) return rc;
     float* d_ang = (float*)st;
     CUDA_OR_FAIL(cudaMemcpyAsync(d_ang, ang.data(), ang.size() * sizeof(float), cudaMemcpyHostToDevice, s), "H2D");
@@ -744,7 +744,7 @@ int rlc_calc_range_many(rlc_method* m, const float* ins, float* outs, int n, uns
         return RLC_OK;
     }
     size_t bin = align256((size_t)n * 3 * sizeof(float));
-    void* st;
+    void* st = nullptr;
     if (int rc = m->stage(bin + (size_t)n * sizeof(float), &st)) return rc;
     float* d_in = (float*)st;
     float* d_out = (float*)((char*)st + bin);
@@ -774,7 +774,7 @@ int rlc_calc_range_repeat_angles(rlc_method* m, const float* ins, const float* a
     }
     size_t b0 = align256((size_t)n * 3 * sizeof(float));
     size_t b1 = align256((size_t)na * sizeof(float));
-    void* st;
+    void* st = nullptr;
     if (int rc = m->stage(b0 + b1 + (size_t)n * na * sizeof(float), &st)) return rc;
     float* d_in = (float*)st;
     float* d_ang = (float*)((char*)st + b0);
@@ -819,7 +819,7 @@ int rlc_eval_sensor_model(rlc_method* m, const float* obs, const float* ranges, 
     }
     size_t b0 = align256((size_t)na * sizeof(float));
     size_t b1 = align256((size_t)n * na * sizeof(float));
-    void* st;
+    void* st = nullptr;
     if (int rc = m->stage(b0 + b1 + (size_t)n * sizeof(double), &st)) return rc;
     float* d_obs = (float*)st;
     float* d_rng = (float*)((char*)st + b0);
@@ -858,7 +858,7 @@ int rlc_calc_range_repeat_angles_eval_sensor_model(rlc_method* m, const float* i
     size_t b0 = align256((size_t)n * 3 * sizeof(float));
     size_t b1 = align256((size_t)na * sizeof(float));
     size_t b2 = align256((size_t)na * sizeof(float));
-    void* st;
+    void* st = nullptr;
     if (int rc = m->stage(b0 + b1 + b2 + (size_t)n * sizeof(double), &st)) return rc;
     float* d_in = (float*)st;
     float* d_ang = (float*)((char*)st + b0);
