@@ -707,3 +707,27 @@ def test_count_steps_matches_oracle_under_every_schedule(rl, oracle_mod):
         for layout in ((0, 1, 2, 3, 4) if kind == "rm" else (0,)):
             g.set_schedule(layout, 0, 0, 0)
             assert g.count_steps(wl.ins, wl.angles) == round(exp), (kind, layout)
+
+
+def test_png_map_end_to_end(rl, oracle_mod, tmp_path):
+    """A map saved as PNG (OMap::save) and read back by PyOMap(path, threshold) -- the reference's
+    PNG constructor -- gives the grid it was saved from, and ray marching and CDDT over it equal
+    the oracle's over that grid."""
+    occ = np.ascontiguousarray(W.corridor_map(512, 2024)[:400, :300])
+    src = _pymap(rl, occ)
+    path = str(tmp_path / "m.png")
+    assert src.save(path) is False
+    m = rl.PyOMap(path, 128.0)
+    assert not m.error() and np.array_equal(m.occupancy, occ) and m.fn == path
+    q = W.free_cell_queries(occ, 5000, 31)
+    _, trig = oracle_mod.world_rays(m.world, q)
+    g = rl.PyRayMarching(m, 150.0)
+    g.set_trig_override(trig)
+    out = np.empty(len(q), np.float32)
+    g.calc_range_many(q, out)
+    assert np.array_equal(_bits(out), _bits(oracle_mod.OracleMethod(occ, "rm", 150.0).calc_range_many(q)))
+    c = rl.PyCDDTCast(m, 150.0, 108)
+    c.calc_range_many(q, out)
+    assert np.array_equal(_bits(out), _bits(oracle_mod.OracleMethod(occ, "cddt", 150.0, td=108).calc_range_many(q)))
+    bad = rl.PyOMap(str(tmp_path / "missing.png"), 128.0)
+    assert bad.error()
