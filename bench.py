@@ -256,7 +256,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": 0,
         "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
-        "config": pf_config(args.workload if args.workload in ("fused", "plain") else "fused", n, na),
+        "config": dict(pf_config(args.workload if args.workload in ("fused", "plain") else "fused", n, na),
+                       l2="no device cache to flush: host CPU run"),
         "particle_updates_per_s": val / na,
         "cpu_baseline": {"value": val, "unit": "rays/s", "cores": nthreads, "kind": "port",
                          "sample": f"{done} full steps ({n}x{na} rays each), oracle/ C restatement, "
@@ -546,8 +547,8 @@ def main():
             "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
-            "config": dict(pf_config(args.workload, n, na), l2="flushed before every step (256 MiB write)",
-                           schedule=dict(zip(("dt_layout", "block", "prefetch", "tile"), method.schedule()))),
+            "config": dict(pf_config(args.workload, n, na), l2="flushed before every step (256 MiB write)"),
+            "schedule": dict(zip(("dt_layout", "block", "prefetch", "tile"), method.schedule())),
             "particle_updates_per_s": value / na,
             "e2e": {"value": e2e, "unit": "rays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "particle_updates_per_s": e2e / na},
