@@ -731,3 +731,35 @@ def test_png_map_end_to_end(rl, oracle_mod, tmp_path):
     assert np.array_equal(_bits(out), _bits(oracle_mod.OracleMethod(occ, "cddt", 150.0, td=108).calc_range_many(q)))
     bad = rl.PyOMap(str(tmp_path / "missing.png"), 128.0)
     assert bad.error()
+
+
+@pytest.mark.parametrize("kind", ["bl", "rm"])
+def test_fused_and_batch_in_a_rotated_world(rl, oracle_mod, kind):
+    """The sensor-model paths under a rotated ROS frame (world -> grid rotation, RangeLib.h:468-475):
+    the fused call, the separate cast + sensor model and the batched launch equal the oracle."""
+    torch = pytest.importorskip("torch")
+    wl = _pf(n=600)
+    m = _pymap(rl, wl.occ, (0.05, 0.45, -20.0, 15.0))
+    g = (rl.PyBresenhamsLine if kind == "bl" else rl.PyRayMarching)(m, wl.max_range)
+    ref = oracle_mod.OracleMethod(wl.occ, kind, wl.max_range, world=m.world)
+    g.set_sensor_model(wl.table)
+    ref.set_sensor_model(wl.table)
+    _, trig = oracle_mod.world_rays(m.world, wl.ins, wl.angles)
+    g.set_trig_override(trig)
+    n, na = len(wl.ins), len(wl.angles)
+    exp_w = ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs)
+    w = np.empty(n, np.float64)
+    g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, w)
+    assert np.array_equal(_bits(w), _bits(exp_w))
+    r = np.empty(n * na, np.float32)
+    g.calc_range_repeat_angles(wl.ins, wl.angles, r)
+    assert np.array_equal(_bits(r), _bits(ref.calc_range_repeat_angles(wl.ins, wl.angles)))
+    dev = torch.device("cuda:0")
+    t = [torch.from_numpy(a).to(dev) for a in (wl.ins, wl.angles, wl.obs)]
+    tw = torch.zeros(n, dtype=torch.float64, device=dev)
+    batch = rl.PyFilterBatch([(g, t[0], t[1], t[2], tw)])
+    for separate in (False, True):
+        batch.set_product_mode(separate)
+        batch.run()
+        torch.cuda.synchronize()
+        assert np.array_equal(_bits(tw.cpu().numpy()), _bits(exp_w)), separate
