@@ -763,3 +763,35 @@ def test_fused_and_batch_in_a_rotated_world(rl, oracle_mod, kind):
         batch.run()
         torch.cuda.synchronize()
         assert np.array_equal(_bits(tw.cpu().numpy()), _bits(exp_w)), separate
+
+
+def test_sensor_model_clamps_and_widest_scan(rl, oracle_mod):
+    """eval_sensor_model's bin clamping (RangeLib.h:533-555) on observations and ranges below 0,
+    past the table, infinite and NaN; and the fused call at the widest scan the ABI takes
+    (16,384 beams per particle), both against the oracle."""
+    wl = _pf(n=64)
+    m = _pymap(rl, wl.occ, wl.world)
+    g = rl.PyRayMarching(m, wl.max_range)
+    ref = oracle_mod.OracleMethod(wl.occ, "rm", wl.max_range, world=m.world)
+    g.set_sensor_model(wl.table)
+    ref.set_sensor_model(wl.table)
+    n, na = len(wl.ins), len(wl.angles)
+    rng = np.random.default_rng(3)
+    specials = np.array([-5.0, -0.0, 0.0, 1e9, np.inf, -np.inf, np.nan, 9.99, 10.0, 10.01], np.float32)
+    obs = wl.obs.copy()
+    obs[:len(specials)] = specials
+    ranges = rng.uniform(-2.0, 15.0, n * na).astype(np.float32)
+    ranges[::7] = np.resize(specials, len(ranges[::7]))
+    w = np.empty(n, np.float64)
+    g.eval_sensor_model(obs, ranges, w, na, n)
+    assert np.array_equal(_bits(w), _bits(ref.eval_sensor_model(obs, ranges, na, n)))
+    angles = np.linspace(-np.pi, np.pi, 16384, endpoint=False).astype(np.float32)
+    obs_w = rng.uniform(0.0, 12.0, 16384).astype(np.float32)
+    ins = wl.ins[:3]
+    _, trig = oracle_mod.world_rays(m.world, ins, angles)
+    g.set_trig_override(trig)
+    wf = np.empty(3, np.float64)
+    g.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs_w, wf)
+    assert np.array_equal(_bits(wf), _bits(ref.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs_w)))
+    with pytest.raises(rl._lib.RangeLibError):   # one beam past the limit
+        g.calc_range_repeat_angles_eval_sensor_model(ins, np.zeros(16385, np.float32), np.zeros(16385, np.float32), wf)
