@@ -184,3 +184,20 @@ def test_png_maps_match_reference_loader(O, tmp_path):
     path = str(tmp_path / "saved.png")
     assert _lib.lib().rlc_png_save_occupancy(path.encode(), occ.ctypes.data, occ.shape[0], occ.shape[1]) == 0
     assert np.array_equal(O.RefMap(png=path).occ, occ)
+
+
+@pytest.mark.parametrize("case", ["all_free", "all_walls", "one_cell", "td1", "td2"])
+def test_cddt_json_edge_cases(O, case):
+    """serializeJson's document on degenerate tables: no zero points at all, a map of walls only,
+    a 1x1 map, one and two angle slices -- byte for byte at 7 digits, exact round trip at 9."""
+    from range_libc_gb300.range_libc import cddt_json_dumps, cddt_json_loads
+    occ = {"all_free": np.zeros((20, 14), np.uint8), "all_walls": np.ones((9, 11), np.uint8),
+           "one_cell": np.zeros((1, 1), np.uint8)}.get(case, MAPS["corridor_384x256"]()[:60, :40].copy())
+    td = {"td1": 1, "td2": 2}.get(case, 12)
+    ref = O.RefMethod(O.RefMap(np.ascontiguousarray(occ)), "cddt", 30.0, td)
+    orc = O.OracleMethod(occ, "cddt", 30.0, td=td)
+    w, t, bl, z = orc.cddt_table()
+    assert cddt_json_dumps(td, 30.0, t, w, bl, z, occ, "", precision=7) == ref.cddt_json()
+    d = cddt_json_loads(cddt_json_dumps(td, 30.0, t, w, bl, z, occ))
+    assert np.array_equal(d["bin_len"], bl) and np.array_equal(_bits(d["zeros"]), _bits(z))
+    assert np.array_equal(d["occ"], occ) and d["theta_disc"] == td
