@@ -964,8 +964,11 @@ int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_bloc
     return RLC_OK;
 }
 
-// Times every schedule candidate (distance-transform layout x RM prefetch x
-// block size) on the caller's workload with CUDA events and keeps the fastest.
+constexpr int kTuneReps = 8;   // per candidate: one warm-up launch pair, then 7 timed launches
+
+// Times every schedule candidate (distance-transform layout x RM prefetch or CDDT bin search x
+// block size x particles per tile, and the staged update) on the caller's workload with CUDA
+// events and keeps the fastest.
 int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
                         int na, void* stream) {
     if (int rc = check_method(m)) return rc;
@@ -995,7 +998,7 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
                     m->layout = li;
                     CastParams p = m->params();
                     float total = 0.0f;
-                    for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+                    for (int rep = 0; rep < kTuneReps && err == cudaSuccess; ++rep) {
                         err = launch_fused(p, li, pf, sm, ins, angles, obs, w, n, na, blocks[bi], tiles[ti], s);
                         if (err == cudaSuccess) err = cudaEventRecord(e0, s);
                         if (err == cudaSuccess)
@@ -1026,7 +1029,7 @@ int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, co
         m->layout = DT_STAGED;
         CastParams p = m->params();
         float total = 0.0f;
-        for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+        for (int rep = 0; rep < kTuneReps && err == cudaSuccess; ++rep) {
             err = launch_fused_staged(p, sm, ins, angles, obs, w, n, na, 0, m->d_bins, s);
             if (err == cudaSuccess) err = cudaEventRecord(e0, s);
             if (err == cudaSuccess) err = launch_fused_staged(p, sm, ins, angles, obs, w, n, na, 0, m->d_bins, s);
