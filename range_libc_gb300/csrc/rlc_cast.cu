@@ -594,8 +594,8 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
     if (KIND == K_CDDT && PF == 1) {   // warp-cooperative bin search
         const bool act = g < (long long)n * na;
         float ax = 0.0f, ay = 0.0f, h = 0.0f;
-        if (act) {
-            int i = (int)(g / na), a = (int)(g - (long long)i * na);
+        if (act) {   // n * na < 2^31 (the ABI refuses larger calls): 32-bit division
+            const unsigned gu = (unsigned)g, i = gu / (unsigned)na, a = gu - i * (unsigned)na;
             float th;
             world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
                           __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
@@ -606,8 +606,7 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
         return;
     }
     if (g >= (long long)n * na) return;
-    int i = (int)(g / na);
-    int a = (int)(g - (long long)i * na);
+    const unsigned gu = (unsigned)g, i = gu / (unsigned)na, a = gu - i * (unsigned)na;   // n * na < 2^31
     float ax, ay, th;
     world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
                   __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
