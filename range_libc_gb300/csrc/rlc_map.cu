@@ -3,12 +3,16 @@
 //
 // Distance transform: the reference builds it on the CPU with the
 // Felzenszwalb-Huttenlocher lower envelope (vendor/distance_transform.h:984-1030,
-// called from RangeLib.h:345-373).  The kernels below run the same published
+// called from RangeLib.h:345-373).  k_edt_pass_y/x run the same published
 // algorithm, one thread per grid line, with the same float/double operation
 // sequence so that every DT value is bit-identical: the intermediate sums
-// f[q] + q*q are float (they round above 2^24, which matters on 4096^2
+// f[q] + q*q are float (they round above 2^24, which matters on large
 // maps), breakpoints are double, and the per-line output is a float.
-// Pass 1 runs along y for every x, pass 2 along x for every y.
+// Pass 1 runs along y for every x, pass 2 along x for every y.  Maps with
+// both sides <= 4096 take k_edt_cols_exact/k_edt_rows_exact instead: the same
+// results from a closed form of pass 1 and from pass 2 with its breakpoint
+// comparisons decided in integer arithmetic (the argument is given above
+// those kernels).
 #include "rangelibc.h"
 #include "rlc_internal.cuh"
 
@@ -109,6 +113,181 @@ __global__ void k_edt_pass_x(const float* g, int W, int H, float* dt, uint32_t* 
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= H) return;
     fh_line(RowInput{g, H, y}, RowSqrtOutput{dt, H, y}, (unsigned)W, v + y, z + y, (size_t)H);
+}
+
+// ---- exact-comparison passes for maps with both sides <= 4096 ---------------------------------
+//
+// With sides <= 4096 every quantity of the F-H steps above is small enough that a cheaper
+// computation gives the same results bit for bit:
+//  * pass 1 (input 0 on occupied cells, FLT_MAX elsewhere): q*q < 2^24 is exact, a breakpoint
+//    between two occupied cells p < q is (p + q) / 2 (exact in double), a FLT_MAX parabola is
+//    popped by the next occupied cell (their breakpoint is below -FLT_MAX / 8192) or lies
+//    beyond the line's end (its breakpoint is above FLT_MAX / 8192), so the envelope picks the
+//    nearest occupied cell p and stores (q - p)^2, or FLT_MAX + (q - p)^2 = FLT_MAX in a column
+//    without one;
+//  * pass 2: finite keys f(q) + q*q stay below 2^25 and every breakpoint is a quotient a / b
+//    with |a| < 2^25 and 0 < b < 2^13.  Two different such quotients differ by at least 2^-26
+//    while double rounding moves each by at most 2^-29, so a comparison of rounded breakpoints
+//    (s <= z[k], z[k + 1] < q) has the outcome of the exact comparison of the quotients, which
+//    integer cross-multiplication decides.  Comparisons with a FLT_MAX key are evaluated in
+//    double exactly as the reference does.  The stack (v, f(v)) is kept in shared memory and
+//    the breakpoints are recomputed from it instead of stored.
+constexpr int kEdtExactSide = 4096;
+constexpr float kEdtExactKey = 33554432.0f;   // 2^25: finite keys of pass 2 are below it
+
+__host__ __device__ __forceinline__ float edt_fadd(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ float edt_fsub(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+__host__ __device__ __forceinline__ float edt_fmul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+// f(v) + v*v in float (v*v < 2^24 converts exactly)
+__host__ __device__ __forceinline__ float edt_key(float fv, unsigned v) { return edt_fadd(fv, (float)(v * v)); }
+// the reference's breakpoint ((double)kb - (double)ka) / ((double)(2 b) - (double)(2 a))
+__host__ __device__ __forceinline__ double edt_isect(float ka, unsigned a, float kb, unsigned b) {
+#ifdef __CUDA_ARCH__
+    return __ddiv_rn(__dsub_rn((double)kb, (double)ka),
+                     __dsub_rn(__ull2double_rn(2ull * b), __ull2double_rn(2ull * a)));
+#else
+    return ((double)kb - (double)ka) / ((double)(2ull * b) - (double)(2ull * a));
+#endif
+}
+__host__ __device__ __forceinline__ int edt_lsb(unsigned b) {   // b != 0
+#ifdef __CUDA_ARCH__
+    return __ffs(b) - 1;
+#else
+    return __builtin_ctz(b);
+#endif
+}
+__host__ __device__ __forceinline__ int edt_msb(unsigned b) {   // b != 0
+#ifdef __CUDA_ARCH__
+    return 31 - __clz(b);
+#else
+    return 31 - __builtin_clz(b);
+#endif
+}
+
+// Pass 1 of one column (H <= 4096).  col[c] is the bit tile of rows 8c..8c+7, the column's byte at
+// bit offset sh; nx holds TY + 1 entries of scratch; out[q] receives the squared distance.
+__host__ __device__ inline void edt_col_exact(const uint64_t* col, int sh, int H, int TY, uint16_t* nx,
+                                              float* out) {
+    constexpr unsigned kNone = 0xFFFFu;
+    unsigned nxt = kNone;   // first occupied row at or after 8c
+    nx[TY] = (uint16_t)kNone;
+    for (int c = TY - 1; c >= 0; --c) {
+        const unsigned b = (unsigned)(col[c] >> sh) & 0xFFu;
+        if (b) nxt = ((unsigned)c << 3) + (unsigned)edt_lsb(b);
+        nx[c] = (uint16_t)nxt;
+    }
+    int prev = -1;          // last occupied row before 8c
+    for (int c = 0; c < TY; ++c) {
+        const unsigned b = (unsigned)(col[c] >> sh) & 0xFFu;
+        const unsigned beyond = nx[c + 1];
+        const int base = c << 3, m = H - base < 8 ? H - base : 8;
+        for (int j = 0; j < m; ++j) {
+            const int q = base + j;
+            const unsigned lo = b & ((2u << j) - 1u), hi = b >> j;
+            const int p = lo ? base + edt_msb(lo) : prev;
+            const unsigned nq = hi ? (unsigned)(q + edt_lsb(hi)) : beyond;
+            int d = 0x7FFFFFFF;
+            if (p >= 0) d = q - p;
+            if (nq != kNone && (int)nq - q < d) d = (int)nq - q;
+            out[q] = d == 0x7FFFFFFF ? FLT_MAX : (float)(d * d);
+        }
+        if (b) prev = base + edt_msb(b);
+    }
+}
+
+// Pass 2 of one line (W, H <= 4096): the reference's F-H steps with the comparisons decided
+// exactly.  sv/sf hold n entries of stack (vertex, its input value).
+#pragma nv_exec_check_disable
+template <class In, class Out>
+__host__ __device__ void fh_line_exact(const In& f, const Out& out, unsigned n, uint16_t* sv, float* sf) {
+    if (n == 0) return;
+    if (n == 1) { out(0, f(0)); return; }
+    unsigned top = 0, vt = 0;
+    sv[0] = 0;
+    sf[0] = f(0);
+    float kt = edt_key(sf[0], 0), fnext = f(1);
+    for (unsigned q = 1; q < n; ++q) {
+        const float fq = fnext;
+        if (q + 1 < n) fnext = f(q + 1);
+        const float kq = edt_key(fq, q);
+        while (top > 0) {   // z[0] = -DBL_MAX: the bottom vertex is never popped
+            const unsigned vu = sv[top - 1];
+            const float ku = edt_key(sf[top - 1], vu);
+            bool pop;
+            if (kq < kEdtExactKey && kt < kEdtExactKey && ku < kEdtExactKey)
+                pop = (long long)((int)kq - (int)kt) * (int)(vt - vu) <=
+                      (long long)((int)kt - (int)ku) * (int)(q - vt);
+            else
+                pop = edt_isect(kt, vt, kq, q) <= edt_isect(ku, vu, kt, vt);
+            if (!pop) break;
+            --top;
+            vt = vu;
+            kt = ku;
+        }
+        ++top;
+        sv[top] = (uint16_t)q;
+        sf[top] = fq;
+        vt = q;
+        kt = kq;
+    }
+    unsigned k = 0, vk = sv[0];
+    float fk = sf[0], kk = edt_key(fk, vk);
+    for (unsigned q = 0; q < n; ++q) {
+        while (k < top) {   // z[top + 1] = DBL_MAX
+            const unsigned vn = sv[k + 1];
+            const float fn = sf[k + 1], kn = edt_key(fn, vn);
+            bool adv;
+            if (kk < kEdtExactKey && kn < kEdtExactKey)
+                adv = (long long)((int)kn - (int)kk) < (long long)q * (long long)(2u * (vn - vk));
+            else
+                adv = edt_isect(kk, vk, kn, vn) < (double)q;
+            if (!adv) break;
+            ++k;
+            vk = vn;
+            fk = fn;
+            kk = kn;
+        }
+        const float dq = edt_fsub((float)q, (float)vk);
+        out(q, edt_fadd(fk, edt_fmul(dq, dq)));
+    }
+}
+
+// one thread per column; dynamic shared memory: blockDim.x * (TY + 1) uint16
+__global__ void k_edt_cols_exact(const uint64_t* __restrict__ bits, int W, int H, int TY, float* __restrict__ g) {
+    extern __shared__ uint16_t s_next[];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    edt_col_exact(bits + (size_t)(x >> 3) * TY, (x & 7) << 3, H, TY, s_next + (size_t)threadIdx.x * (TY + 1),
+                  g + (size_t)x * H);
+}
+
+// one thread per row; dynamic shared memory: blockDim.x * W * (4 + 2) bytes
+__global__ void k_edt_rows_exact(const float* __restrict__ g, int W, int H, float* __restrict__ dt) {
+    extern __shared__ __align__(16) unsigned char s_stack[];
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= H) return;
+    float* sf = reinterpret_cast<float*>(s_stack) + (size_t)threadIdx.x * W;
+    uint16_t* sv = reinterpret_cast<uint16_t*>(reinterpret_cast<float*>(s_stack) + (size_t)blockDim.x * W) +
+                   (size_t)threadIdx.x * W;
+    fh_line_exact(RowInput{g, H, y}, RowSqrtOutput{dt, H, y}, (unsigned)W, sv, sf);
 }
 
 __global__ void k_dt_to_tiled(const float* __restrict__ lin, int W, int H, int TY, float* __restrict__ tiled) {
@@ -224,6 +403,22 @@ cudaError_t launch_edt(const uint64_t* d_bits, int W, int H, int TY, float* d_dt
     if (scratch_bytes < edt_scratch_bytes(W, H)) return cudaErrorInvalidValue;
     char* base = static_cast<char*>(scratch);
     float* g = reinterpret_cast<float*>(base);
+    if (W <= kEdtExactSide && H <= kEdtExactSide) {
+        k_edt_cols_exact<<<blocks_for(W, 32), 32, 32 * (TY + 1) * sizeof(uint16_t), s>>>(d_bits, W, H, TY, g);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        // rows per block: the stack's shared memory, and about one block per SM of a 152-SM part
+        constexpr int kSmemCap = 227 * 1024;
+        const int per_line = W * (int)(sizeof(float) + sizeof(uint16_t));
+        int lines = (H + 151) / 152;
+        lines = lines < kSmemCap / per_line ? lines : kSmemCap / per_line;
+        lines = lines < 32 ? (lines > 0 ? lines : 1) : 32;
+        static std::atomic<unsigned long long> attr_done{0};
+        e = ensure_smem_attr(k_edt_rows_exact, kSmemCap, attr_done);
+        if (e != cudaSuccess) return e;
+        k_edt_rows_exact<<<blocks_for(H, lines), lines, (size_t)lines * per_line, s>>>(g, W, H, d_dt);
+        return cudaGetLastError();
+    }
     size_t goff = ((size_t)W * H * sizeof(float) + 255) & ~(size_t)255;
     // per pass: z (n+1 doubles per line) first, then v (n uint32 per line)
     double* z1 = reinterpret_cast<double*>(base + goff);

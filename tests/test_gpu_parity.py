@@ -90,6 +90,34 @@ def test_distance_transform_large_map(rl, oracle_mod):
     assert np.array_equal(_bits(dt), _bits(oracle_mod.edt(occ)))
 
 
+def _edt_cases():
+    rng = np.random.default_rng(91)
+    cases = []
+    # both sides <= 4096 take the exact-comparison kernels, a side above 4096 the F-H kernels
+    for w, h in ((4096, 40), (40, 4096), (4097, 40), (40, 4100)):
+        occ = (rng.random((w, h)) < 0.002).astype(np.uint8)
+        cases.append((f"{w}x{h}", occ))
+    # the limit: one corner obstacle, squared distances up to 2 * 4095^2 and keys near 2^25
+    occ = np.zeros((4096, 4096), np.uint8)
+    occ[0, 0] = 1
+    occ[rng.integers(0, 4096, 20), rng.integers(0, 4096, 20)] = 1
+    cases.append(("4096x4096_sparse", occ))
+    # mostly empty columns: pass 2 meets FLT_MAX inputs and compares them in double
+    occ = np.zeros((1500, 1300), np.uint8)
+    for x in rng.integers(0, 1500, 3):
+        occ[x, rng.integers(0, 1300, 4)] = 1
+    cases.append(("empty_columns", occ))
+    return cases
+
+
+@pytest.mark.parametrize("name,occ", _edt_cases(), ids=[c[0] for c in _edt_cases()])
+def test_distance_transform_both_paths(rl, oracle_mod, name, occ):
+    m = _pymap(rl, occ)
+    dt = np.empty(occ.shape, np.float32)
+    rl._lib.call("rlc_map_distance_transform", m.handle, dt.ctypes.data_as(rl._lib._f32p))
+    assert np.array_equal(_bits(dt), _bits(oracle_mod.edt(occ))), name
+
+
 WORLDS = {
     "identity": (1.0, 0.0, 0.0, 0.0),
     "ros": (0.05, 0.0, -3.25, -1.5),
