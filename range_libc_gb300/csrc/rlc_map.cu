@@ -115,25 +115,30 @@ __global__ void k_edt_pass_x(const float* g, int W, int H, float* dt, uint32_t* 
     fh_line(RowInput{g, H, y}, RowSqrtOutput{dt, H, y}, (unsigned)W, v + y, z + y, (size_t)H);
 }
 
-// ---- exact-comparison passes for maps with both sides <= 4096 ---------------------------------
+// ---- exact-comparison passes for maps with both sides <= 16384 --------------------------------
 //
-// With sides <= 4096 every quantity of the F-H steps above is small enough that a cheaper
-// computation gives the same results bit for bit:
-//  * pass 1 (input 0 on occupied cells, FLT_MAX elsewhere): q*q < 2^24 is exact, a breakpoint
-//    between two occupied cells p < q is (p + q) / 2 (exact in double), a FLT_MAX parabola is
-//    popped by the next occupied cell (their breakpoint is below -FLT_MAX / 8192) or lies
-//    beyond the line's end (its breakpoint is above FLT_MAX / 8192), so the envelope picks the
-//    nearest occupied cell p and stores (q - p)^2, or FLT_MAX + (q - p)^2 = FLT_MAX in a column
-//    without one;
-//  * pass 2: finite keys f(q) + q*q stay below 2^25 and every breakpoint is a quotient a / b
-//    with |a| < 2^25 and 0 < b < 2^13.  Two different such quotients differ by at least 2^-26
-//    while double rounding moves each by at most 2^-29, so a comparison of rounded breakpoints
-//    (s <= z[k], z[k + 1] < q) has the outcome of the exact comparison of the quotients, which
-//    integer cross-multiplication decides.  Comparisons with a FLT_MAX key are evaluated in
-//    double exactly as the reference does.  The stack (v, f(v)) is kept in shared memory and
-//    the breakpoints are recomputed from it instead of stored.
-constexpr int kEdtExactSide = 4096;
-constexpr float kEdtExactKey = 33554432.0f;   // 2^25: finite keys of pass 2 are below it
+// For such maps a cheaper computation of the F-H steps above gives the same results bit for bit.
+// Every finite key f(q) + q*q (a float sum, as in the reference) is an integer below 2^29, and
+// every breakpoint is a quotient a / b of integers with |a| < 2^29 and 2 <= b <= 2 (n - 1) < 2^15,
+// computed in double exactly up to the final rounding.  Rounding moves a / b by at most
+// 2^-53 |a| / b, while two different quotients a / b and c / d differ by at least 1 / (b d);
+// since |a| d + |c| b < 2^45 < 2^53, rounding never reverses or merges two different quotients,
+// and equal quotients round alike.  A comparison of rounded breakpoints (s <= z[k],
+// z[k + 1] < q) therefore has the outcome of the exact comparison of the quotients, which integer
+// cross-multiplication decides.  Comparisons with a FLT_MAX key are evaluated in double exactly
+// as the reference does.  The stack holds (v, f(v)) only; breakpoints are recomputed from it.
+//  * sides <= 4096, pass 1 (input 0 on occupied cells, FLT_MAX elsewhere): q*q < 2^24 is exact,
+//    a breakpoint between two occupied cells p < q is (p + q) / 2, a FLT_MAX parabola is popped
+//    by the next occupied cell (their breakpoint is below -FLT_MAX / 8192) or lies beyond the
+//    line's end (its breakpoint is above FLT_MAX / 8192), so the envelope picks the nearest
+//    occupied cell p and stores (q - p)^2, or FLT_MAX + (q - p)^2 = FLT_MAX in a column without
+//    one: a closed form per column (edt_col_exact);
+//  * sides <= 4096, pass 2: the stack of each row in shared memory (k_edt_rows_exact);
+//  * a side above 4096: q*q rounds, the closed form no longer holds, and both passes run the
+//    exact-comparison steps with the stack in global memory (k_edt_cols_fh, k_edt_rows_fh).
+constexpr int kEdtExactSide = 4096;           // closed-form pass 1, shared-memory pass 2
+constexpr int kEdtIntSide = 16384;            // integer comparisons
+constexpr float kEdtExactKey = 536870912.0f;  // 2^29: finite keys are below it
 
 __host__ __device__ __forceinline__ float edt_fadd(float a, float b) {
 #ifdef __CUDA_ARCH__
@@ -156,7 +161,7 @@ __host__ __device__ __forceinline__ float edt_fmul(float a, float b) {
     return a * b;
 #endif
 }
-// f(v) + v*v in float (v*v < 2^24 converts exactly)
+// f(v) + v*v in float, as the reference sums it (v*v < 2^32)
 __host__ __device__ __forceinline__ float edt_key(float fv, unsigned v) { return edt_fadd(fv, (float)(v * v)); }
 // the reference's breakpoint ((double)kb - (double)ka) / ((double)(2 b) - (double)(2 a))
 __host__ __device__ __forceinline__ double edt_isect(float ka, unsigned a, float kb, unsigned b) {
@@ -213,47 +218,57 @@ __host__ __device__ inline void edt_col_exact(const uint64_t* col, int sh, int H
     }
 }
 
-// Pass 2 of one line (W, H <= 4096): the reference's F-H steps with the comparisons decided
-// exactly.  sv/sf hold n entries of stack (vertex, its input value).
+// One line (both sides <= 16384): the reference's F-H steps with the comparisons decided exactly.
+// The stack's entry k is (sv[k * ld], sf[k * ld]) -- vertex and its input value -- with room for
+// n entries; the top two entries are also kept in registers.
 #pragma nv_exec_check_disable
 template <class In, class Out>
-__host__ __device__ void fh_line_exact(const In& f, const Out& out, unsigned n, uint16_t* sv, float* sf) {
+__host__ __device__ void fh_line_exact(const In& f, const Out& out, unsigned n, uint16_t* sv, float* sf,
+                                       size_t ld) {
     if (n == 0) return;
     if (n == 1) { out(0, f(0)); return; }
-    unsigned top = 0, vt = 0;
+    unsigned top = 0, vt = 0, vs = 0;   // (vt, kt) entry top, (vs, ks) entry top - 1
+    const float f0 = f(0);
     sv[0] = 0;
-    sf[0] = f(0);
-    float kt = edt_key(sf[0], 0), fnext = f(1);
+    sf[0] = f0;
+    float kt = edt_key(f0, 0), ks = 0.0f, fnext = f(1);
     for (unsigned q = 1; q < n; ++q) {
         const float fq = fnext;
         if (q + 1 < n) fnext = f(q + 1);
         const float kq = edt_key(fq, q);
         while (top > 0) {   // z[0] = -DBL_MAX: the bottom vertex is never popped
-            const unsigned vu = sv[top - 1];
-            const float ku = edt_key(sf[top - 1], vu);
             bool pop;
-            if (kq < kEdtExactKey && kt < kEdtExactKey && ku < kEdtExactKey)
-                pop = (long long)((int)kq - (int)kt) * (int)(vt - vu) <=
-                      (long long)((int)kt - (int)ku) * (int)(q - vt);
+            if (kq < kEdtExactKey && kt < kEdtExactKey && ks < kEdtExactKey)
+                pop = (long long)((int)kq - (int)kt) * (int)(vt - vs) <=
+                      (long long)((int)kt - (int)ks) * (int)(q - vt);
             else
-                pop = edt_isect(kt, vt, kq, q) <= edt_isect(ku, vu, kt, vt);
+                pop = edt_isect(kt, vt, kq, q) <= edt_isect(ks, vs, kt, vt);
             if (!pop) break;
             --top;
-            vt = vu;
-            kt = ku;
+            vt = vs;
+            kt = ks;
+            if (top > 0) {
+                vs = sv[(size_t)(top - 1) * ld];
+                ks = edt_key(sf[(size_t)(top - 1) * ld], vs);
+            }
         }
         ++top;
-        sv[top] = (uint16_t)q;
-        sf[top] = fq;
+        sv[(size_t)top * ld] = (uint16_t)q;
+        sf[(size_t)top * ld] = fq;
+        vs = vt;
+        ks = kt;
         vt = q;
         kt = kq;
     }
-    unsigned k = 0, vk = sv[0];
-    float fk = sf[0], kk = edt_key(fk, vk);
+    unsigned k = 0, vk = sv[0], vn = 0;
+    float fk = sf[0], kk = edt_key(fk, vk), fn = 0.0f;
+    if (top > 0) {
+        vn = sv[ld];
+        fn = sf[ld];
+    }
     for (unsigned q = 0; q < n; ++q) {
-        while (k < top) {   // z[top + 1] = DBL_MAX
-            const unsigned vn = sv[k + 1];
-            const float fn = sf[k + 1], kn = edt_key(fn, vn);
+        while (k < top) {   // z[top + 1] = DBL_MAX; (vn, fn) is entry k + 1
+            const float kn = edt_key(fn, vn);
             bool adv;
             if (kk < kEdtExactKey && kn < kEdtExactKey)
                 adv = (long long)((int)kn - (int)kk) < (long long)q * (long long)(2u * (vn - vk));
@@ -264,6 +279,10 @@ __host__ __device__ void fh_line_exact(const In& f, const Out& out, unsigned n, 
             vk = vn;
             fk = fn;
             kk = kn;
+            if (k < top) {
+                vn = sv[(size_t)(k + 1) * ld];
+                fn = sf[(size_t)(k + 1) * ld];
+            }
         }
         const float dq = edt_fsub((float)q, (float)vk);
         out(q, edt_fadd(fk, edt_fmul(dq, dq)));
@@ -287,7 +306,22 @@ __global__ void k_edt_rows_exact(const float* __restrict__ g, int W, int H, floa
     float* sf = reinterpret_cast<float*>(s_stack) + (size_t)threadIdx.x * W;
     uint16_t* sv = reinterpret_cast<uint16_t*>(reinterpret_cast<float*>(s_stack) + (size_t)blockDim.x * W) +
                    (size_t)threadIdx.x * W;
-    fh_line_exact(RowInput{g, H, y}, RowSqrtOutput{dt, H, y}, (unsigned)W, sv, sf);
+    fh_line_exact(RowInput{g, H, y}, RowSqrtOutput{dt, H, y}, (unsigned)W, sv, sf, 1);
+}
+
+// a side above 4096: one thread per line, the lines' stacks interleaved in global memory
+// (entry k of line l at k * lines + l)
+__global__ void k_edt_cols_fh(const uint64_t* __restrict__ bits, int W, int H, int TY, float* g, uint16_t* sv,
+                              float* sf) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    fh_line_exact(OccInput{bits, TY, x}, ColOutput{g, (size_t)x * H}, (unsigned)H, sv + x, sf + x, (size_t)W);
+}
+
+__global__ void k_edt_rows_fh(const float* g, int W, int H, float* dt, uint16_t* sv, float* sf) {
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= H) return;
+    fh_line_exact(RowInput{g, H, y}, RowSqrtOutput{dt, H, y}, (unsigned)W, sv + y, sf + y, (size_t)H);
 }
 
 __global__ void k_dt_to_tiled(const float* __restrict__ lin, int W, int H, int TY, float* __restrict__ tiled) {
@@ -420,6 +454,15 @@ cudaError_t launch_edt(const uint64_t* d_bits, int W, int H, int TY, float* d_dt
         return cudaGetLastError();
     }
     size_t goff = ((size_t)W * H * sizeof(float) + 255) & ~(size_t)255;
+    if (W <= kEdtIntSide && H <= kEdtIntSide) {   // stacks: W * H floats, then W * H uint16 (either pass)
+        float* sf = reinterpret_cast<float*>(base + goff);
+        uint16_t* sv = reinterpret_cast<uint16_t*>(base + goff + (size_t)W * H * sizeof(float));
+        k_edt_cols_fh<<<blocks_for(W, 32), 32, 0, s>>>(d_bits, W, H, TY, g, sv, sf);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_edt_rows_fh<<<blocks_for(H, 32), 32, 0, s>>>(g, W, H, d_dt, sv, sf);
+        return cudaGetLastError();
+    }
     // per pass: z (n+1 doubles per line) first, then v (n uint32 per line)
     double* z1 = reinterpret_cast<double*>(base + goff);
     uint32_t* v1 = reinterpret_cast<uint32_t*>(base + goff + (size_t)W * (H + 1) * sizeof(double));

@@ -1,11 +1,13 @@
 // Host check of the distance transform's exact-comparison passes (rlc_map.cu: edt_col_exact,
-// fh_line_exact) against the oracle's Felzenszwalb-Huttenlocher transform, bit for bit.
+// fh_line_exact, as launch_edt picks them for maps up to 16384 per side) against the oracle's
+// Felzenszwalb-Huttenlocher transform, bit for bit.
 //
 //   edt_exact_check [--quick] [occupancy.u8 W H]...
 //
 // Each file holds W * H bytes (x-major, 1 = occupied).  Built-in cases: seeded random maps of
 // many shapes and densities, sparse maps with full columns, maps whose pass 2 meets mostly
-// FLT_MAX inputs, and 4096 x 4096 maps whose squared distances approach 2 * 4095^2.  Prints
+// FLT_MAX inputs, 4096 x 4096 maps whose squared distances approach 2 * 4095^2, and maps with a
+// side above 4096 (up to 16384), whose sums f + q*q round in float.  Prints
 // "<cases> cases, <n> mismatches" and exits non-zero on a mismatch.
 #include "rlc_map.cu"
 
@@ -27,6 +29,14 @@ struct HostIn {
     size_t stride;
     float operator()(unsigned q) const { return g[q * stride]; }
 };
+struct HostOcc {   // pass 1 input: 0 on occupied cells, FLT_MAX elsewhere
+    const uint8_t* occ;
+    float operator()(unsigned q) const { return occ[q] ? 0.0f : FLT_MAX; }
+};
+struct HostOut {
+    float* d;
+    void operator()(unsigned q, float v) const { d[q] = v; }
+};
 struct HostSqrtOut {
     float* d;
     size_t stride;
@@ -40,13 +50,19 @@ bool check(const std::vector<uint8_t>& occ, int W, int H, const char* what) {
         for (int y = 0; y < H; ++y)
             if (occ[(size_t)x * H + y]) bits[(size_t)(x >> 3) * TY + (y >> 3)] |= 1ull << (((x & 7) << 3) | (y & 7));
     std::vector<float> g((size_t)W * H), dt((size_t)W * H), ref((size_t)W * H);
-    std::vector<uint16_t> nx(TY + 1), sv(W);
-    std::vector<float> sf(W);
-    for (int x = 0; x < W; ++x)
-        rlc::edt_col_exact(bits.data() + (size_t)(x >> 3) * TY, (x & 7) << 3, H, TY, nx.data(), g.data() + (size_t)x * H);
+    std::vector<uint16_t> nx(TY + 1), sv(W > H ? W : H);
+    std::vector<float> sf(W > H ? W : H);
+    const bool closed_form = W <= rlc::kEdtExactSide && H <= rlc::kEdtExactSide;   // as launch_edt chooses
+    for (int x = 0; x < W; ++x) {
+        if (closed_form)
+            rlc::edt_col_exact(bits.data() + (size_t)(x >> 3) * TY, (x & 7) << 3, H, TY, nx.data(), g.data() + (size_t)x * H);
+        else
+            rlc::fh_line_exact(HostOcc{occ.data() + (size_t)x * H}, HostOut{g.data() + (size_t)x * H}, (unsigned)H,
+                               sv.data(), sf.data(), 1);
+    }
     for (int y = 0; y < H; ++y)
         rlc::fh_line_exact(HostIn{g.data() + y, (size_t)H}, HostSqrtOut{dt.data() + y, (size_t)H}, (unsigned)W,
-                           sv.data(), sf.data());
+                           sv.data(), sf.data(), 1);
     orc_edt(occ.data(), W, H, ref.data());
     size_t bad = 0, first = 0;
     for (size_t i = 0; i < dt.size(); ++i)
@@ -64,7 +80,7 @@ int main(int argc, char** argv) {
     if (a < argc && strcmp(argv[a], "--quick") == 0) { quick = true; ++a; }
     for (; a + 2 < argc; a += 3) {
         const int W = atoi(argv[a + 1]), H = atoi(argv[a + 2]);
-        if (W <= 0 || H <= 0 || W > rlc::kEdtExactSide || H > rlc::kEdtExactSide) { printf("bad size\n"); return 2; }
+        if (W <= 0 || H <= 0 || W > rlc::kEdtIntSide || H > rlc::kEdtIntSide) { printf("bad size\n"); return 2; }
         std::vector<uint8_t> occ((size_t)W * H);
         FILE* f = fopen(argv[a], "rb");
         if (!f) { printf("cannot open %s\n", argv[a]); return 2; }
@@ -133,6 +149,27 @@ int main(int argc, char** argv) {
                 }
                 ++cases;
                 fails += !check(occ, W, H, "flt_max_columns");
+            }
+    }
+    {   // a side above 4096: both passes run the stack with integer comparisons (keys up to 2^29)
+        const int dims[][2] = {{4097, 40}, {40, 4100}, {16384, 9}, {9, 16384}, {10976, 64}, {64, 10976}, {6000, 5000}};
+        for (auto& dd : dims)
+            for (int pat = 0; pat < 3; ++pat) {
+                const int W = dd[0], H = dd[1];
+                if (quick && (size_t)W * H > 1000000 && pat) continue;
+                std::vector<uint8_t> occ((size_t)W * H, 0);
+                if (pat == 0) {
+                    std::bernoulli_distribution b(0.001);
+                    for (auto& o : occ) o = b(rng);
+                }
+                if (pat == 1) occ[0] = 1;   // one corner: distances up to the diagonal
+                if (pat == 2)
+                    for (int c = 0; c < 3; ++c) {   // mostly empty columns
+                        const int x = (int)(rng() % W);
+                        for (int i = 0; i < 5; ++i) occ[(size_t)x * H + rng() % H] = 1;
+                    }
+                ++cases;
+                fails += !check(occ, W, H, "large_side");
             }
     }
     printf("%d cases, %d mismatches\n", cases, fails);

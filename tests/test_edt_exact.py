@@ -1,12 +1,13 @@
 """The distance transform's exact-comparison passes, run on the host against the oracle.
 
 Maps with both sides <= 4096 take a closed form of the column pass and a row pass whose
-breakpoint comparisons are decided with integer cross-multiplication (rlc_map.cu:
-edt_col_exact, fh_line_exact).  Both functions are __host__ __device__: this test compiles
-them for the host with nvcc, beside the oracle's C restatement of the reference's
-Felzenszwalb-Huttenlocher transform, and compares every cell bit for bit on seeded maps (all
-densities, 1x1 to 4096x4096, FLT_MAX-heavy rows), on the reference's benchmark map from the
-golden fixture and on the generated workload maps.  The GPU tests check the kernels themselves.
+breakpoint comparisons are decided with integer cross-multiplication; maps with a side up to
+16384 run both passes with those comparisons (rlc_map.cu: edt_col_exact, fh_line_exact).  Both
+functions are __host__ __device__: this test compiles them for the host with nvcc, beside the
+oracle's C restatement of the reference's Felzenszwalb-Huttenlocher transform, and compares
+every cell bit for bit on seeded maps (all densities, 1x1 to 16384 per side, FLT_MAX-heavy
+rows), on the reference's benchmark map from the golden fixture and on the generated workload
+maps.  The GPU tests check the kernels themselves.
 """
 import os
 import shutil

@@ -93,10 +93,15 @@ def test_distance_transform_large_map(rl, oracle_mod):
 def _edt_cases():
     rng = np.random.default_rng(91)
     cases = []
-    # both sides <= 4096 take the exact-comparison kernels, a side above 4096 the F-H kernels
-    for w, h in ((4096, 40), (40, 4096), (4097, 40), (40, 4100)):
+    # both sides <= 4096: closed-form columns and shared-memory rows; a side in (4096, 16384]:
+    # integer comparisons with the stacks in global memory; a side above 16384: the double F-H
+    for w, h in ((4096, 40), (40, 4096), (4097, 40), (40, 4100), (16384, 9), (16385, 8), (8, 16390)):
         occ = (rng.random((w, h)) < 0.002).astype(np.uint8)
         cases.append((f"{w}x{h}", occ))
+    occ = np.zeros((10976, 64), np.uint8)   # keys up to ~2^27 that round in float
+    occ[0, 0] = 1
+    occ[rng.integers(0, 10976, 5), rng.integers(0, 64, 5)] = 1
+    cases.append(("10976x64_sparse", occ))
     # the limit: one corner obstacle, squared distances up to 2 * 4095^2 and keys near 2^25
     occ = np.zeros((4096, 4096), np.uint8)
     occ[0, 0] = 1
