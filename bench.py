@@ -253,7 +253,8 @@ def run_reference(args):
     v1, d1, e1 = cpu_reference_pf(wl, world, 1000, 1, budget_s=5.0, nthreads=1)
     n, na = len(wl.ins), len(wl.angles)
     line = {
-        "impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": ws,
+        "gpus_used": 0, "devices": "host CPU cores of rank 0 (the reference's path has no GPU code here)",
         "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * el / done, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
         "config": dict(pf_config(args.workload if args.workload in ("fused", "plain") else "fused", n, na),

@@ -21,3 +21,4 @@ def test_reference_arm_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert "workload" in d["config"]
+    assert d["n_gpus"] == 1 and d["gpus_used"] == 0   # the launch's N; the arm itself runs on host cores
