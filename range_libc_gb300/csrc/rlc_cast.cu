@@ -134,11 +134,11 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
 // ---------------------------------------------------- Bresenham's line (BL)
 // RangeLib.h:696-769.  The occupancy word of the current 8x8 tile stays in a
 // register; a new word is read only when the line leaves the tile.
-struct BitCache {
-    long long tile = -1;
+struct BitCache {   // x, y in the grid; maps hold at most 2^31 cells (rlc_map_create), so < 2^26 tiles
+    unsigned tile = 0xFFFFFFFFu;
     uint64_t word = 0;
     __device__ __forceinline__ bool test(const MapDev& m, int x, int y) {
-        long long t = (long long)(x >> 3) * m.tiles_y + (y >> 3);
+        const unsigned t = (unsigned)(x >> 3) * (unsigned)m.tiles_y + (unsigned)(y >> 3);
         if (t != tile) { tile = t; word = __ldg(m.bits + t); }
         return (word >> (((x & 7) << 3) | (y & 7))) & 1ull;
     }
