@@ -82,7 +82,8 @@ enum rlc_flags {
 
 /* kernel-reported conditions, read with rlc_method_device_flags */
 enum rlc_device_flag {
-    RLC_FLAG_BL_BOUND = 1u,       /* Bresenham loop bound hit (|coordinate| > 2^24) */
+    RLC_FLAG_BL_BOUND = 1u,       /* Bresenham loop bound hit: |coordinate| > 2^24, or a walk that skips
+                                     its end cell where float +-1 rounds up across a power of two */
     RLC_FLAG_WRAP_BOUND = 2u,     /* CDDT heading wrap bound hit (|heading| > ~6e5 rad) */
     RLC_FLAG_CDDT_PAST_END = 4u,  /* query equal to a bin's last zero point (reference reads past the bin) */
     RLC_FLAG_NAN_INDEX = 8u       /* NaN range or observation mapped to sensor bin 0 */

@@ -206,8 +206,11 @@ float orc_bl_calc_range_trig(const uint8_t* occ, int width, int height, float ma
         int xstep = (x0 < x1) ? 1 : -1;
         int ystep = (y0 < y1) ? 1 : -1;
         float fw = (float)width, fh = (float)height;
-        /* the reference loop ends after |x1-x0|+2 steps; the bound only
-         * guards coordinates where float +-1 no longer moves _x */
+        /* the reference loop ends after |x1-x0|+2 steps unless (int)_x never
+         * equals the end: above 2^24 float +-1 no longer moves _x, and a start
+         * whose fraction is 1 - ulp rounds up across a power of two and skips
+         * that integer (999.99994 + 24 -> 1025.0); the reference then never
+         * terminates, the bound returns max_range */
         long bound = (long)(deltax < 1e9f ? deltax : 1e9f) + 4;
         while (f2i(_x) != f2i(x1 + (float)xstep)) {
             if (n > bound) { out = max_range; goto done; }

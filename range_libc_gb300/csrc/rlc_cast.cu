@@ -163,10 +163,11 @@ __device__ float bl_cast(const MapDev& m, float mr, float x, float y, float c, f
     float _x = x0, _y = y0;
     const float xstep = (x0 < x1) ? 1.0f : -1.0f;
     const float ystep = (y0 < y1) ? 1.0f : -1.0f;
-    const float fw = __int2float_rn(m.W), fh = __int2float_rn(m.H);
     const int end = __float2int_rz(__fadd_rn(x1, xstep));
-    // the reference loop ends after at most |x1 - x0| + 3 steps; the bound
-    // only fires where float +-1 no longer moves _x (|coordinates| > 2^24)
+    // the reference loop ends after at most |x1 - x0| + 3 steps unless the integer part of _x
+    // never equals `end`: above 2^24 float +-1 no longer moves _x, and a start whose fraction is
+    // 1 - ulp rounds up where the walk crosses a power of two (999.99994 + 24 -> 1025.0) and
+    // skips that integer; the reference then never terminates, here the bound returns max_range
     const int bound = (int)(deltax < 1e9f ? deltax : 1e9f) + 4;
     int n = 0;
     BitCache cache;
@@ -184,8 +185,11 @@ __device__ float bl_cast(const MapDev& m, float mr, float x, float y, float c, f
         }
         const float gx = steep ? _x : _y;   // isOccupied(_y, _x) when not steep
         const float gy = steep ? _y : _x;
-        if (0.0f <= gx && gx < fw && 0.0f <= gy && gy < fh &&
-            cache.test(m, __float2int_rz(gx), __float2int_rz(gy))) {
+        // the reference's `0 <= g && g < W` then (int)g: for an integer W, floor(g) < W exactly
+        // when g < W and floor(g) >= 0 exactly when g >= 0 (-0.0 included), and inside the grid
+        // floor equals truncation; g is never NaN here (NaN inputs end in the setup above)
+        const int fx = __float2int_rd(gx), fy = __float2int_rd(gy);
+        if ((unsigned)fx < (unsigned)m.W && (unsigned)fy < (unsigned)m.H && cache.test(m, fx, fy)) {
             float xd = __fsub_rn(_x, x0), yd = __fsub_rn(_y, y0);
             return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
         }

@@ -552,6 +552,29 @@ def test_edge_cases(rl, oracle_mod):
     assert np.array_equal(_bits(out), _bits(ref.calc_range_many(q)))
 
 
+def test_bresenham_walk_that_skips_its_end(rl, oracle_mod):
+    """A walk whose start has the fraction 1 - ulp rounds up where it crosses a power of two
+    (999.99994 + 24 -> 1025.0) and never reaches its end cell 1024, so the reference's loop never
+    ends.  The loop bound returns max_range and raises RLC_FLAG_BL_BOUND (1), on the GPU as in
+    the oracle; a neighbouring ray that reaches its end is unaffected."""
+    occ = np.zeros((64, 1100), np.uint8)
+    m = _pymap(rl, occ)
+    b = rl.PyBresenhamsLine(m, 23.5)
+    y = float(np.float32(1000.0) - np.float32(2.0 ** -14))
+    q = np.array([[5.5, y, np.pi / 2], [5.5, 999.5, np.pi / 2]], np.float32)
+    trig = np.array([[np.cos(np.pi / 2), np.sin(np.pi / 2)]] * 2, np.float32)
+    b.set_trig_override(trig)
+    b.device_flags()   # clears
+    out = np.empty(2, np.float32)
+    rl._lib.call("rlc_calc_range_many", b.handle, q.ctypes.data, out.ctypes.data, 2, rl._lib.RLC_NO_WORLD, None)
+    ref = oracle_mod.OracleMethod(occ, "bl", 23.5)
+    exp = np.array([ref.calc_range_trig(float(a), float(bb), float(c), float(s))
+                    for (a, bb, _), (c, s) in zip(q, trig)], np.float32)
+    assert np.array_equal(_bits(out), _bits(exp))
+    assert out[0] == np.float32(23.5) and out[1] == np.float32(23.5)
+    assert b.device_flags() & 1
+
+
 def test_argument_errors(rl):
     occ = _map("rect_128")
     m = _pymap(rl, occ)
