@@ -169,6 +169,11 @@ __device__ float bl_cast(const MapDev& m, float mr, float x, float y, float c, f
     // 1 - ulp rounds up where the walk crosses a power of two (999.99994 + 24 -> 1025.0) and
     // skips that integer; the reference then never terminates, here the bound returns max_range
     const int bound = (int)(deltax < 1e9f ? deltax : 1e9f) + 4;
+    // the reference's in-grid test is `0 <= g && g < (float)W`; (float)W rounds above 2^24, and the
+    // floats below it are exactly the floats below min(W, (float)W) (none lies between W and a
+    // (float)W rounded up)
+    const unsigned bx = min((unsigned)m.W, __float2uint_rz(__int2float_rn(m.W)));
+    const unsigned by = min((unsigned)m.H, __float2uint_rz(__int2float_rn(m.H)));
     int n = 0;
     BitCache cache;
     while (__float2int_rz(_x) != end) {
@@ -185,11 +190,11 @@ __device__ float bl_cast(const MapDev& m, float mr, float x, float y, float c, f
         }
         const float gx = steep ? _x : _y;   // isOccupied(_y, _x) when not steep
         const float gy = steep ? _y : _x;
-        // the reference's `0 <= g && g < W` then (int)g: for an integer W, floor(g) < W exactly
-        // when g < W and floor(g) >= 0 exactly when g >= 0 (-0.0 included), and inside the grid
-        // floor equals truncation; g is never NaN here (NaN inputs end in the setup above)
+        // `0 <= g && g < B` then (int)g: for an integer B, floor(g) < B exactly when g < B and
+        // floor(g) >= 0 exactly when g >= 0 (-0.0 included; saturation keeps |g| >= 2^31 out),
+        // and inside the grid floor equals truncation; g is never NaN here (NaN inputs end above)
         const int fx = __float2int_rd(gx), fy = __float2int_rd(gy);
-        if ((unsigned)fx < (unsigned)m.W && (unsigned)fy < (unsigned)m.H && cache.test(m, fx, fy)) {
+        if ((unsigned)fx < bx && (unsigned)fy < by && cache.test(m, fx, fy)) {
             float xd = __fsub_rn(_x, x0), yd = __fsub_rn(_y, y0);
             return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
         }

@@ -575,6 +575,29 @@ def test_bresenham_walk_that_skips_its_end(rl, oracle_mod):
     assert b.device_flags() & 1
 
 
+def test_bresenham_map_wider_than_2_pow_24(rl, oracle_mod):
+    """The reference's in-grid test compares with (float)width, which rounds down for a width of
+    2^24 + 1: the last column (x = 2^24) is never tested, and walks there stall (float +1 no
+    longer moves them) until the loop bound.  The GPU must agree with the oracle."""
+    w, h = (1 << 24) + 1, 2
+    occ = np.zeros((w, h), np.uint8)
+    occ[w - 1, :] = 1
+    m = _pymap(rl, occ)
+    b = rl.PyBresenhamsLine(m, 40.0)
+    q = np.array([[16777190.0, 0.5, 0.0], [16777200.0, 1.5, 0.0], [16777212.0, 0.5, 0.0],
+                  [16777215.0, 0.5, 0.01], [16777216.0, 0.5, np.pi], [16777100.0, 1.0, 0.02]], np.float32)
+    trig = np.stack([np.cos(q[:, 2].astype(np.float64)), np.sin(q[:, 2].astype(np.float64))], 1).astype(np.float32)
+    b.set_trig_override(trig)
+    out = np.empty(len(q), np.float32)
+    rl._lib.call("rlc_calc_range_many", b.handle, q.ctypes.data, out.ctypes.data, len(q), rl._lib.RLC_NO_WORLD,
+                 None)
+    ref = oracle_mod.OracleMethod(occ, "bl", 40.0)
+    exp = np.array([ref.calc_range_trig(float(x), float(y), float(c), float(s))
+                    for (x, y, _), (c, s) in zip(q, trig)], np.float32)
+    assert np.array_equal(_bits(out), _bits(exp))
+    b.device_flags()
+
+
 def test_argument_errors(rl):
     occ = _map("rect_128")
     m = _pymap(rl, occ)
