@@ -82,8 +82,11 @@ enum rlc_flags {
 
 /* kernel-reported conditions, read with rlc_method_device_flags */
 enum rlc_device_flag {
-    RLC_FLAG_BL_BOUND = 1u,       /* Bresenham loop bound hit: |coordinate| > 2^24, or a walk that skips
-                                     its end cell where float +-1 rounds up across a power of two */
+    RLC_FLAG_BL_BOUND = 1u,       /* Bresenham loop bound hit by a walk that has not yet passed the
+                                     grid's far edge: a start beyond 2^24 where float +-1 no longer
+                                     moves it, or a walk that skips its end cell where float +-1
+                                     rounds up across a power of two.  (A walk past the grid's edge in
+                                     its direction of motion ends there with max_range, unflagged.) */
     RLC_FLAG_WRAP_BOUND = 2u,     /* CDDT heading wrap bound hit (|heading| > ~6e5 rad) */
     RLC_FLAG_CDDT_PAST_END = 4u,  /* query equal to a bin's last zero point (reference reads past the bin) */
     RLC_FLAG_NAN_INDEX = 8u       /* NaN range or observation mapped to sensor bin 0 */
@@ -230,9 +233,11 @@ RLC_API int rlc_method_autotune(rlc_method* m, const float* d_ins, const float* 
  * d_dt[x * height + y] (float), asynchronously on `stream`, allocating nothing.  Its
  * scratch is a fixed device array of RLC_NOALLOC_SCRATCH_BYTES that every GPU loading this
  * library holds until exit; maps beyond RLC_NOALLOC_MAX_CELLS cells or RLC_NOALLOC_MAX_SIDE
- * per side are rejected with RLC_ERR_ARG.  The first call on a device looks up the array's
- * address there (make it before any stream capture).  Calls share the array: calls that
- * overlap on the GPU race and corrupt each other's results. */
+ * per side are rejected with RLC_ERR_ARG, and so are pointers that are not device memory of the
+ * current device (or managed memory).  The first call on a device looks up the array's
+ * address there and keeps it (make it before any stream capture; after cudaDeviceReset,
+ * reload the library before calling again).  Calls share the array: calls that overlap on the
+ * GPU race and corrupt each other's results. */
 #define RLC_NOALLOC_MAX_CELLS 1048576
 #define RLC_NOALLOC_MAX_SIDE 4096
 #define RLC_NOALLOC_SCRATCH_BYTES 16949760

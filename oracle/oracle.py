@@ -25,7 +25,20 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", platform.machine(), "librlc_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "librlc_ref.so")
 REF_FAST_SO = os.path.join(HERE, "_ref", "librlc_ref_fast.so")
-REF_SRC = os.environ.get("RLC_REFERENCE_DIR", "/root/reference")
+
+
+def _reference_dir() -> str:
+    """Where the reference's sources lie: RLC_REFERENCE_DIR, else the oracle Makefile's REF."""
+    env = os.environ.get("RLC_REFERENCE_DIR")
+    if env:
+        return env
+    try:
+        return subprocess.check_output(["make", "-s", "-C", HERE, "refdir"], text=True).strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+
+
+REF_SRC = _reference_dir()
 
 BL, RM, CDDT, GLT = 0, 1, 2, 3
 KINDS = {"bl": BL, "rm": RM, "cddt": CDDT, "pcddt": CDDT, "glt": GLT}
@@ -41,7 +54,7 @@ def build(reference: bool | None = None) -> None:
     """Compile the oracle (always) and the reference harness (when its sources exist)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
     if reference is None:
-        reference = os.path.isdir(os.path.join(REF_SRC, "includes"))
+        reference = bool(REF_SRC) and os.path.isdir(os.path.join(REF_SRC, "includes"))
     if reference:
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"])
 

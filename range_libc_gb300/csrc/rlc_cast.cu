@@ -174,6 +174,10 @@ __device__ float bl_cast(const MapDev& m, float mr, float x, float y, float c, f
     // (float)W rounded up)
     const unsigned bx = min((unsigned)m.W, __float2uint_rz(__int2float_rn(m.W)));
     const unsigned by = min((unsigned)m.H, __float2uint_rz(__int2float_rn(m.H)));
+    // both walk coordinates move monotonically (_x by xstep, _y by ystep), so once a grid axis
+    // has left [0, b) in its direction of motion no later cell is inside the grid: the walk
+    // returns max_range there, as the reference's does when it ends (it walks on to its end cell)
+    const bool gx_up = (steep ? xstep : ystep) > 0.0f, gy_up = (steep ? ystep : xstep) > 0.0f;
     int n = 0;
     BitCache cache;
     while (__float2int_rz(_x) != end) {
@@ -194,9 +198,13 @@ __device__ float bl_cast(const MapDev& m, float mr, float x, float y, float c, f
         // floor(g) >= 0 exactly when g >= 0 (-0.0 included; saturation keeps |g| >= 2^31 out),
         // and inside the grid floor equals truncation; g is never NaN here (NaN inputs end above)
         const int fx = __float2int_rd(gx), fy = __float2int_rd(gy);
-        if ((unsigned)fx < bx && (unsigned)fy < by && cache.test(m, fx, fy)) {
-            float xd = __fsub_rn(_x, x0), yd = __fsub_rn(_y, y0);
-            return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+        if ((unsigned)fx < bx && (unsigned)fy < by) {
+            if (cache.test(m, fx, fy)) {
+                float xd = __fsub_rn(_x, x0), yd = __fsub_rn(_y, y0);
+                return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+            }
+        } else if ((gx_up ? fx >= (int)bx : fx < 0) || (gy_up ? fy >= (int)by : fy < 0)) {
+            return mr;   // past the grid's edge: no occupied cell is left on the walk
         }
     }
     return mr;

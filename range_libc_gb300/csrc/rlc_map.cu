@@ -542,7 +542,9 @@ cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int TY, uin
 //   RLC_NOALLOC_MAX_SIDE; larger maps are rejected with RLC_ERR_ARG.
 // * The first call on a device looks up the array's device address there
 //   (cudaGetSymbolAddress, with that device current) and caches it; make
-//   that first call before any stream capture.
+//   that first call before any stream capture.  The cached address lives as
+//   long as the device's primary context: after cudaDeviceReset the library
+//   has to be unloaded and loaded again before this entry point is used.
 // * All calls share the array and it keeps the last call's contents.  No
 //   word of it needs to start at zero (each is written before it is read),
 //   but calls that overlap on the GPU -- on different streams, or from
@@ -590,13 +592,22 @@ int noalloc_scratch(void** out) {
     return RLC_OK;
 }
 
+// device memory of the current device, or managed memory; memory of another device is refused
+// (without peer access the kernels here would fault on it)
 bool is_device_pointer(const void* p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    if (a.type != cudaMemoryTypeDevice) return false;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.device == dev;
 }
 
 }  // namespace
@@ -617,7 +628,7 @@ extern "C" int rlc_distance_transform_noalloc(const uint8_t* d_occ, int width, i
         return set_last_error(RLC_ERR_ARG, msg);
     }
     if (!is_device_pointer(d_occ) || !is_device_pointer(d_dt))
-        return set_last_error(RLC_ERR_ARG, "rlc_distance_transform_noalloc: d_occ and d_dt must be device memory");
+        return set_last_error(RLC_ERR_ARG, "rlc_distance_transform_noalloc: d_occ and d_dt must be device memory of the current device");
     void* base = nullptr;
     if (int rc = noalloc_scratch(&base)) return rc;
     cudaStream_t s = (cudaStream_t)stream;

@@ -1,7 +1,7 @@
 """Generate the golden vectors under tests/golden/ by running the reference.
 
-Run in a checkout where the reference sources exist (RLC_REFERENCE_DIR,
-default /root/reference): it builds the reference harness (oracle/Makefile,
+Run in a checkout where the reference sources exist (RLC_REFERENCE_DIR, or
+the oracle Makefile's REF): it builds the reference harness (oracle/Makefile,
 target `ref`, strict IEEE flags) and records, for a set of maps, poses and
 sensor tables, what the reference's own classes return:
 

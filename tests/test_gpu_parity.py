@@ -578,7 +578,10 @@ def test_bresenham_walk_that_skips_its_end(rl, oracle_mod):
 def test_bresenham_map_wider_than_2_pow_24(rl, oracle_mod):
     """The reference's in-grid test compares with (float)width, which rounds down for a width of
     2^24 + 1: the last column (x = 2^24) is never tested, and walks there stall (float +1 no
-    longer moves them) until the loop bound.  The GPU must agree with the oracle."""
+    longer moves them); the reference never ends them, the oracle's loop bound returns max_range.
+    The GPU must agree with the oracle.  A stalled walk at 2^24 has passed the grid's in-grid
+    bound min(W, (float)W) = 2^24 in its direction of motion, so the GPU ends it there without
+    running into the loop bound: no RLC_FLAG_BL_BOUND."""
     w, h = (1 << 24) + 1, 2
     occ = np.zeros((w, h), np.uint8)
     occ[w - 1, :] = 1
@@ -588,6 +591,7 @@ def test_bresenham_map_wider_than_2_pow_24(rl, oracle_mod):
                   [16777215.0, 0.5, 0.01], [16777216.0, 0.5, np.pi], [16777100.0, 1.0, 0.02]], np.float32)
     trig = np.stack([np.cos(q[:, 2].astype(np.float64)), np.sin(q[:, 2].astype(np.float64))], 1).astype(np.float32)
     b.set_trig_override(trig)
+    b.device_flags()   # clears
     out = np.empty(len(q), np.float32)
     rl._lib.call("rlc_calc_range_many", b.handle, q.ctypes.data, out.ctypes.data, len(q), rl._lib.RLC_NO_WORLD,
                  None)
@@ -595,7 +599,33 @@ def test_bresenham_map_wider_than_2_pow_24(rl, oracle_mod):
     exp = np.array([ref.calc_range_trig(float(x), float(y), float(c), float(s))
                     for (x, y, _), (c, s) in zip(q, trig)], np.float32)
     assert np.array_equal(_bits(out), _bits(exp))
+    assert b.device_flags() & 1 == 0
+
+
+def test_bresenham_walk_past_the_grid_edge_ends_there(rl, oracle_mod):
+    """A walk that has left the grid in its direction of motion meets no occupied cell again, so
+    the GPU ends it there with max_range (the reference walks on to its end cell and returns
+    max_range too): a huge max_range costs no more than the map's size, and the results equal
+    the oracle's, whose loop walks to the end.  A walk that starts off the grid and moves into it
+    is not cut short."""
+    occ = np.zeros((64, 48), np.uint8)
+    occ[30:34, 20:24] = 1
+    m = _pymap(rl, occ)
+    b = rl.PyBresenhamsLine(m, 1.0e7)
+    q = np.array([[10.5, 10.5, 0.0], [10.5, 10.5, np.pi / 2], [10.5, 10.5, np.pi], [10.5, 10.5, -np.pi / 2],
+                  [10.5, 10.5, 0.7], [-50.5, 21.5, np.pi / 2], [31.5, -40.5, 0.0], [31.5, 90.5, np.pi],
+                  [-5.0, -5.0, 0.8], [70.5, 21.5, np.pi / 2]], np.float32)
+    trig = np.stack([np.cos(q[:, 2].astype(np.float64)), np.sin(q[:, 2].astype(np.float64))], 1).astype(np.float32)
+    b.set_trig_override(trig)
     b.device_flags()
+    out = np.empty(len(q), np.float32)
+    rl._lib.call("rlc_calc_range_many", b.handle, q.ctypes.data, out.ctypes.data, len(q), rl._lib.RLC_NO_WORLD,
+                 None)
+    ref = oracle_mod.OracleMethod(occ, "bl", 1.0e7)
+    exp = np.array([ref.calc_range_trig(float(x), float(y), float(c), float(s))
+                    for (x, y, _), (c, s) in zip(q, trig)], np.float32)
+    assert np.array_equal(_bits(out), _bits(exp))
+    assert b.device_flags() & 1 == 0
 
 
 def test_argument_errors(rl):

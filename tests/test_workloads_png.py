@@ -210,7 +210,8 @@ def test_png_save_round_trip(tmp_path):
 
 def test_png_occupancy_matches_reference_loader():
     """The reference's own small fixture maps, loaded by the reference (golden) and by us."""
-    ref_maps = os.path.join(os.environ.get("RLC_REFERENCE_DIR", "/root/reference"), "maps")
+    import oracle as O
+    ref_maps = os.path.join(O.REF_SRC, "maps")
     gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.npz"))
     if not os.path.isdir(ref_maps):
         pytest.skip("reference maps not present")

@@ -47,6 +47,8 @@ def test_noalloc_matches_allocating_entry_point(rl):
     maps = [
         W.rect_disk_map(1024, 77),                                   # the largest allowed map
         np.ascontiguousarray(W.corridor_map(512, 78)[:300, :410]),   # smaller, non-square, after it
+        np.ascontiguousarray(W.rect_disk_map(4096, 79)[:, :256]),    # the side limit with few rows
+        np.ascontiguousarray(W.rect_disk_map(4096, 80)[:256, :]),    # and with few columns
     ]
     for occ in maps:   # two calls in a row share the scratch
         got = _noalloc_dt(rl, torch, occ)
@@ -66,3 +68,20 @@ def test_noalloc_rejects_oversized_maps(rl):
     rc = rl._lib.lib().rlc_distance_transform_noalloc(C.c_void_p(buf.data_ptr()), 5000, 10,
                                                       C.c_void_p(out.data_ptr()), None)
     assert rc == rl._lib.RLC_ERR_ARG
+
+
+def test_noalloc_rejects_host_memory(rl):
+    """Host buffers are refused before anything is launched (the kernels would read them as
+    device addresses)."""
+    torch = pytest.importorskip("torch")
+    occ = np.zeros((16, 16), np.uint8)
+    dt = np.zeros((16, 16), np.float32)
+    dev = torch.device("cuda:0")
+    d_occ = torch.zeros(256, dtype=torch.uint8, device=dev)
+    d_dt = torch.zeros(256, dtype=torch.float32, device=dev)
+    L = rl._lib.lib()
+    for a, b in ((occ.ctypes.data, d_dt.data_ptr()), (d_occ.data_ptr(), dt.ctypes.data)):
+        rc = L.rlc_distance_transform_noalloc(C.c_void_p(a), 16, 16, C.c_void_p(b), None)
+        assert rc == rl._lib.RLC_ERR_ARG
+        assert b"device memory of the current device" in L.rlc_last_error()
+    torch.cuda.synchronize()
