@@ -197,9 +197,17 @@ RLC_API int rlc_calc_range_repeat_angles_eval_sensor_model(rlc_method* m, const 
                                                            unsigned flags, void* stream);
 
 /* Parity mode (testing): per-ray (cos, sin) pairs, ray-indexed like the outputs of the
- * next query calls (BL and RM).  trig = NULL restores device sincosf.  `count` rays,
+ * next query calls (BL and RM).  trig = NULL restores the device's own (rlc_trig_eval).  `count` rays,
  * host pointer; the array is copied. */
 RLC_API int rlc_method_set_trig_override(rlc_method* m, const float* trig, int64_t count);
+
+/* The cos/sin the BL and RM casts use for a ray heading x when no trig override is set: the
+ * floats nearest to the exact sin(x) and cos(x) (the reference calls the host libm's sinf/cosf,
+ * RangeLib.h:700-702, 930-931, which glibc rounds to nearest on all but ~0.1 % of arguments).
+ * sincos[2 i] = sin(x[i]), sincos[2 i + 1] = cos(x[i]), computed by the device; with
+ * RLC_DEVICE_PTRS both arrays are device memory and the call is queued on `stream`.  Lets a
+ * checker reproduce the production casts bit for bit. */
+RLC_API int rlc_trig_eval(const float* x, float* sincos, int64_t n, unsigned flags, void* stream);
 
 /* Measurement: total march steps of the rays of a repeat-angle call (RM: distance-transform
  * reads; BL: cells tested), for stating algorithmic bytes.  Synchronous; RM and BL only. */
@@ -259,7 +267,8 @@ typedef struct rlc_filter_desc {
     int n_angles;
 } rlc_filter_desc;
 
-/* The methods must outlive the batch.  block = threads per block (0 = 256). */
+/* The methods must outlive the batch.  block = threads per block (0 = 256).  A method's trig
+ * override set or cleared after the batch was created is taken up by the next rlc_batch_run. */
 RLC_API int rlc_batch_create(const rlc_filter_desc* filters, int n_filters, int block, rlc_batch** out);
 RLC_API int rlc_batch_run(rlc_batch* b, void* stream);
 /* Schedule of the persistent launch: distance-transform layout (0 linear, 1 tiled, 2 compact

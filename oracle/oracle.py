@@ -72,7 +72,7 @@ class _Method(C.Structure):
         ("kind", C.c_int), ("width", C.c_int), ("height", C.c_int),
         ("occ", _u8p), ("dt", _f32p), ("cddt", C.c_void_p),
         ("max_range", C.c_float), ("world", _World),
-        ("table", _f64p), ("K", C.c_int), ("glt", C.c_void_p),
+        ("table", _f64p), ("K", C.c_int), ("glt", C.c_void_p), ("trig", _f32p),
     ]
 
 
@@ -214,6 +214,7 @@ class OracleMethod:
             if kind == "pcddt":
                 self.prune()
         self.table = None
+        self.trig = None
         self._m = _Method()
         self._sync()
 
@@ -229,6 +230,13 @@ class OracleMethod:
         m.table = _ptr(self.table, _f64p) if self.table is not None else None
         m.K = 0 if self.table is None else self.table.shape[0]
         m.glt = C.cast(self.glt, C.c_void_p) if self.glt is not None else None
+        m.trig = _ptr(self.trig, _f32p) if self.trig is not None else None
+
+    def set_trig_override(self, trig):
+        """Per-ray (cos, sin) for the batched BL/RM calls, ray-indexed like their outputs
+        (None: the libm's cosf/sinf, as the reference)."""
+        self.trig = None if trig is None else np.ascontiguousarray(trig, np.float32).reshape(-1, 2)
+        self._sync()
 
     def __del__(self):
         if getattr(self, "cddt", None) is not None:

@@ -629,6 +629,17 @@ float orc_method_calc_range(const orc_method* m, float x, float y, float heading
     }
 }
 
+/* one ray of a batched call: the method's own cos/sin, or the per-ray override (BL and RM) */
+static inline float ray_range(const orc_method* m, float x, float y, float heading, size_t ray) {
+    if (m->trig && m->kind == ORC_RM)
+        return orc_rm_calc_range_trig(m->dt, m->width, m->height, m->max_range, x, y, m->trig[2 * ray],
+                                      m->trig[2 * ray + 1], NULL);
+    if (m->trig && m->kind == ORC_BL)
+        return orc_bl_calc_range_trig(m->occ, m->width, m->height, m->max_range, x, y, m->trig[2 * ray],
+                                      m->trig[2 * ray + 1], NULL);
+    return orc_method_calc_range(m, x, y, heading, NULL);
+}
+
 typedef struct { float inv_s, s, rc; } world_consts;
 
 static world_consts make_world(const orc_world* w) {
@@ -662,7 +673,7 @@ static void numpy_range_body(void* p, int lo, int hi) {
     for (int i = lo; i < hi; ++i) {
         float ax, ay, th;
         world_to_grid(&b->m->world, &b->k, b->ins + 3 * (size_t)i, &ax, &ay, &th);
-        b->outs[i] = orc_method_calc_range(b->m, ax, ay, th, NULL) * b->k.s;
+        b->outs[i] = ray_range(b->m, ax, ay, th, (size_t)i) * b->k.s;
     }
 }
 
@@ -706,7 +717,7 @@ static void raw_range_body(void* p, int lo, int hi) {
     batch_ctx* b = (batch_ctx*)p;
     for (int i = lo; i < hi; ++i) {
         const float* q = b->ins + 3 * (size_t)i;
-        b->outs[i] = orc_method_calc_range(b->m, q[0], q[1], q[2], NULL);
+        b->outs[i] = ray_range(b->m, q[0], q[1], q[2], (size_t)i);
     }
 }
 
@@ -721,7 +732,7 @@ static void angles_body(void* p, int lo, int hi) {
         float ax, ay, th;
         world_to_grid(&b->m->world, &b->k, b->ins + 3 * (size_t)i, &ax, &ay, &th);
         for (int a = 0; a < b->na; ++a)
-            b->outs[(size_t)i * b->na + a] = orc_method_calc_range(b->m, ax, ay, th - b->angles[a], NULL) * b->k.s;
+            b->outs[(size_t)i * b->na + a] = ray_range(b->m, ax, ay, th - b->angles[a], (size_t)i * b->na + a) * b->k.s;
     }
 }
 
@@ -770,7 +781,7 @@ static void fused_body(void* p, int lo, int hi) {
         world_to_grid(&m->world, &b->k, b->ins + 3 * (size_t)i, &ax, &ay, &th);
         double weight = 1.0;
         for (int a = 0; a < b->na; ++a) {
-            float d = orc_method_calc_range(m, ax, ay, th - b->angles[a], NULL);
+            float d = ray_range(m, ax, ay, th - b->angles[a], (size_t)i * b->na + a);
             int di = sensor_bin(d, K);
             int ri = sensor_bin(b->obs[a] * b->k.inv_s, K);
             weight *= m->table[(size_t)ri * K + di];

@@ -76,6 +76,8 @@ typedef struct orc_method {
     const double* table;     /* sensor model, K x K row-major (borrowed) */
     int K;
     orc_glt* glt;            /* GLT: borrowed table */
+    const float* trig;       /* BL/RM: per-ray (cos, sin) used instead of the libm's by the batched
+                                calls, ray-indexed like their outputs (NULL: cosf/sinf) */
 } orc_method;
 
 /* ---- map preprocessing ---- */

@@ -81,6 +81,7 @@ SIGNATURES = {
         C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_uint, _vp]),
     "rlc_method_set_trig_override": (C.c_int, [_vp, _f32p, C.c_int64]),
     "rlc_count_steps": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_uint, _i64p]),
+    "rlc_trig_eval": (C.c_int, [_vp, _vp, C.c_int64, C.c_uint, _vp]),
     "rlc_method_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
     "rlc_method_get_schedule": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p]),
     "rlc_method_autotune": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),

@@ -904,6 +904,26 @@ static int fused_device(rlc_method* m, const float* ins, const float* angles, co
                          "fused sensor model");
 }
 
+int rlc_trig_eval(const float* x, float* sincos, int64_t n, unsigned flags, void* stream) {
+    if (n < 0) return fail(RLC_ERR_ARG, "negative size");
+    if (n == 0) return RLC_OK;
+    if (!x || !sincos) return fail(RLC_ERR_ARG, "null array");
+    if (flags & RLC_DEVICE_PTRS) {
+        CUDA_OR_FAIL(launch_trig_eval(x, sincos, (long long)n, (cudaStream_t)stream), "trig eval");
+        return RLC_OK;
+    }
+    float* d = nullptr;
+    const size_t bx = align256((size_t)n * sizeof(float));
+    CUDA_OR_FAIL(cudaMalloc(&d, bx + (size_t)n * 2 * sizeof(float)), "trig eval allocation");
+    float* d_sc = (float*)((char*)d + bx);
+    cudaError_t e = cudaMemcpy(d, x, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_trig_eval(d, d_sc, (long long)n, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(sincos, d_sc, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    CUDA_OR_FAIL(e, "trig eval");
+    return RLC_OK;
+}
+
 int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n, int na, unsigned flags,
                     int64_t* total_steps) {
     if (int rc = check_method(m)) return rc;
@@ -1080,6 +1100,7 @@ struct rlc_batch {
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    std::vector<const float*> trig_seen;   // each method's trig override when the table was built
 
     void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -1144,6 +1165,8 @@ struct rlc_batch {
             it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
             items.push_back(it);
         }
+        trig_seen.clear();
+        for (const rlc_filter_desc& d : descs) trig_seen.push_back(d.method->d_trig);
         std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.cost > b.cost; });
         unsigned long long tiles = 0, parts = 0;
         std::vector<FilterDev> hf;
@@ -1180,6 +1203,16 @@ struct rlc_batch {
     // queue reset + persistent kernel, captured once as a CUDA graph
     int launch(cudaStream_t stream) {
         if (total_tiles == 0) return RLC_OK;
+        // a method whose trig override was set or cleared since the build: the device table holds
+        // the old (freed) override, so rebuild it (and the graph) first
+        for (size_t i = 0; i < descs.size(); ++i) {
+            const rlc_method* m = descs[i].method;
+            if (i < trig_seen.size() && m->d_trig == trig_seen[i]) continue;
+            if (m->d_trig && m->trig_count < (long long)descs[i].n_particles * descs[i].n_angles)
+                return fail(RLC_ERR_ARG, "filter %d: trig override too short", (int)i);
+            if (int rc = build()) return rc;
+            break;
+        }
         if (!exec) {
             CUDA_OR_FAIL(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "batch capture");
             cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(unsigned), cap);

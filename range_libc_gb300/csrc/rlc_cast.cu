@@ -8,9 +8,11 @@
 // (RangeLib.h), and its results are reproduced bit for bit.  Mixed
 // float/double expressions of the reference are evaluated in double here
 // too, except where the float evaluation is provably identical (noted).
-// The only source of difference is the per-ray cosf/sinf of RM and BL (the
-// host libm and CUDA's sincosf are not both correctly rounded); the optional
-// per-ray trig override removes it for parity tests.
+// The only source of difference is the per-ray cosf/sinf of RM and BL: here
+// they are the correctly rounded values (rlc_trig.cuh), which a host libm
+// matches on all but ~0.1 % of arguments (glibc's float sine and cosine are
+// not correctly rounded); the optional per-ray trig override takes the
+// host's values instead, for parity tests.
 #include "rlc_internal.cuh"
 
 #include <climits>
@@ -507,7 +509,7 @@ __device__ __forceinline__ float cast_one(const CastParams& p, float x, float y,
         c = p.trig[2 * ray];
         s = p.trig[2 * ray + 1];
     } else {
-        sincosf(h, &s, &c);
+        rlc_trig::sincos_cr(h, &s, &c);
     }
     if (KIND == K_RM) return rm_cast<LAYOUT, PF>(p.map, p.mr, x, y, c, s);
     return bl_cast(p.map, p.mr, x, y, c, s, p.err);
@@ -956,7 +958,7 @@ __global__ void __launch_bounds__(kStagedThreads, 1) k_bm_cast(CastParams p, Sen
         world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1),
                       __ldg(ins + 3 * (size_t)i + 2), ax, ay, th);
         float c, s;
-        sincosf(__fsub_rn(th, ang), &s, &c);
+        rlc_trig::sincos_cr(__fsub_rn(th, ang), &s, &c);
         const float ex = ax + p.mr * c, ey = ay + p.mr * s;
         if (!(isfinite(ax) && isfinite(ay) && isfinite(ex) && isfinite(ey))) continue;
         const float lx = fminf(fmaxf(fminf(ax, ex), -1e6f), 1e6f), hx = fminf(fmaxf(fmaxf(ax, ex), -1e6f), 1e6f);
@@ -1009,7 +1011,7 @@ __global__ void __launch_bounds__(kStagedThreads, 1) k_bm_cast(CastParams p, Sen
                       __ldg(ins + 3 * (size_t)i + 2), x0, y0, th);
         const long long ray = (long long)i * na + a;
         float c, s;
-        if (p.trig) { c = p.trig[2 * ray]; s = p.trig[2 * ray + 1]; } else sincosf(__fsub_rn(th, ang), &s, &c);
+        if (p.trig) { c = p.trig[2 * ray]; s = p.trig[2 * ray + 1]; } else rlc_trig::sincos_cr(__fsub_rn(th, ang), &s, &c);
         float out = p.mr;
         if (!(isnan(x0) || isnan(y0) || isnan(c) || isnan(s))) {
             float t = 0.0f;
@@ -1102,7 +1104,7 @@ __global__ void __launch_bounds__(256) k_count_steps(CastParams p, const float* 
         world_to_grid(p.world, ins[3 * (size_t)i], ins[3 * (size_t)i + 1], ins[3 * (size_t)i + 2], ax, ay, th);
         float h = __fsub_rn(th, angles[a]);
         float c, s;
-        if (p.trig) { c = p.trig[2 * g]; s = p.trig[2 * g + 1]; } else sincosf(h, &s, &c);
+        if (p.trig) { c = p.trig[2 * g]; s = p.trig[2 * g + 1]; } else rlc_trig::sincos_cr(h, &s, &c);
         if (KIND == K_RM) rm_cast<DT_LINEAR>(p.map, p.mr, ax, ay, c, s, &steps);
         else bl_cast(p.map, p.mr, ax, ay, c, s, p.err, &steps);
     }
@@ -1235,6 +1237,22 @@ cudaError_t launch_count_steps(const CastParams& p, const float* ins, const floa
     if (p.kind == K_RM) k_count_steps<K_RM><<<blocks_for(rays, 256), 256, 0, s>>>(p, ins, angles, n, na, total);
     else if (p.kind == K_BL) k_count_steps<K_BL><<<blocks_for(rays, 256), 256, 0, s>>>(p, ins, angles, n, na, total);
     else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+// the per-ray cos/sin of the casts (rlc_trig::sincos_cr) for given arguments
+__global__ void __launch_bounds__(256) k_trig_eval(const float* __restrict__ x, float2* __restrict__ sc, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float s, c;
+        rlc_trig::sincos_cr(__ldg(x + i), &s, &c);
+        sc[i] = make_float2(s, c);
+    }
+}
+
+cudaError_t launch_trig_eval(const float* x, float* sincos, long long n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const long long blocks = (n + 255) / 256;
+    k_trig_eval<<<(unsigned)(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, s>>>(x, reinterpret_cast<float2*>(sincos), n);
     return cudaGetLastError();
 }
 

@@ -17,6 +17,8 @@
 
 #include <cuda_runtime.h>
 
+#include "rlc_trig.cuh"
+
 #include <atomic>
 #include <stdint.h>
 
@@ -143,6 +145,9 @@ cudaError_t launch_cddt_radial(const CastParams& p, const float* ins, const floa
 // march steps of world-frame repeat-angle rays (RM and BL), summed into *total
 cudaError_t launch_count_steps(const CastParams& p, const float* ins, const float* angles, int n, int na,
                                unsigned long long* total, cudaStream_t s);
+
+// sincos[2i], sincos[2i + 1] = the casts' sin and cos of x[i] (rlc_trig::sincos_cr)
+cudaError_t launch_trig_eval(const float* x, float* sincos, long long n, cudaStream_t s);
 
 // ---- batched multi-filter update (rlc_cast.cu) ----
 struct FilterDev {

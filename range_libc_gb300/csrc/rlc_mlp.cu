@@ -638,7 +638,7 @@ __global__ void k_sample_rays(MapDev m, float mr, const uint32_t* __restrict__ f
     xyt[3 * (size_t)r + 1] = y;
     xyt[3 * (size_t)r + 2] = th;
     float s, c, rg;
-    sincosf(th, &s, &c);
+    rlc_trig::sincos_cr(th, &s, &c);   // the exact path's cos/sin
     t[r] = march_t(m, mr, x, y, c, s, &rg);
     if (range) range[r] = rg;
 }
@@ -677,7 +677,7 @@ __global__ void k_accept(MapDev m, float mr, const float* __restrict__ xyt, cons
     float rg = 0.0f;
     if (t > 1.0f && t < 0.999f * mr && isfinite(t)) {
         float s, c;
-        sincosf(th, &s, &c);
+        rlc_trig::sincos_cr(th, &s, &c);
         const int hx = __float2int_rz(x0 + c * t), hy = __float2int_rz(y0 + s * t);
         const int bx = __float2int_rz(x0 + c * (t - 1.0f)), by = __float2int_rz(y0 + s * (t - 1.0f));
         if (occ_cell(m, hx, hy) && !occ_cell(m, bx, by)) {
@@ -702,7 +702,7 @@ __global__ void k_recast(MapDev m, float mr, const float* __restrict__ xyt, cons
     const int r = list[j];
     const float x0 = xyt[3 * (size_t)r], y0 = xyt[3 * (size_t)r + 1], th = xyt[3 * (size_t)r + 2];
     float s, c, rg;
-    sincosf(th, &s, &c);
+    rlc_trig::sincos_cr(th, &s, &c);
     march_t(m, mr, x0, y0, c, s, &rg);
     outs[r] = __fmul_rn(rg, scale);
 }

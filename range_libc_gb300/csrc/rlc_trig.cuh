@@ -1,0 +1,211 @@
+// Correctly rounded float sine and cosine for the per-ray headings of ray
+// marching and Bresenham's line.
+//
+// The reference computes each ray's cosf/sinf with the host C library
+// (RangeLib.h:700-702, 930-931), and a ray's hit cell can change with the
+// last bit of either.  No fixed rule reproduces every libm (glibc's float
+// sine and cosine are themselves not correctly rounded on about 0.1 % of
+// arguments); the rule here is the one every accurate libm agrees with
+// almost everywhere: the float nearest to the exact sin(x) and cos(x).
+//
+// Method (written for this library):
+//  1. |x| < 2^-12: sin = x and cos = 1 are the correctly rounded values.
+//  2. |x| < 4096: j = rint(x * 2/pi) and r = x - j * pi/2 as a float pair,
+//     with pi/2 split into four floats (Cody-Waite): j * C0 and j * C1 are
+//     formed exactly (two-product by FMA), x - fl(j * C0) is exact
+//     (Sterbenz), and the tail terms are summed in float.  |r| <= pi/4 + 2^-11.
+//  3. k = rint(256 r), u = r - k/256 (|u| <= 2^-9, renormalised float pair);
+//     sin(r) = S_k cos(u) + C_k sin(u), cos(r) = C_k cos(u) - S_k sin(u),
+//     with S_k, C_k = sin, cos(k/256) as float pairs (rlc_trig_table.h,
+//     computed with mpmath) and short Taylor series for sin(u) and cos(u)
+//     (the first omitted terms are below 2^-54 relative).  The largest
+//     products are formed exactly, the small corrections in float.
+//  4. The result is a float pair (h, l) within 2^-42 of the exact value
+//     (relative), so h is the correctly rounded value unless the exact value
+//     may lie across a rounding midpoint of h: the code checks
+//     |l| + 2^-40 |h| < (half the spacing of floats at h), and
+//  5. otherwise (about 1 argument in 2^15, |x| >= 4096, a reduced argument
+//     below 2^-16 after a reduction, NaN, infinities) rounds the double
+//     precision sin and cos, whose error (a few units in the 53rd bit) can
+//     misround only arguments within ~2^-50 of a midpoint.
+//
+// Every operation is written out (no contraction: the library is compiled
+// with -fmad=false and host checks with -ffp-contract=off), so the host and
+// the device compute the same bits; tests/cpp/trig_check.cpp compares the
+// host build against the exact values and the device kernels against it.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "rlc_trig_table.h"
+
+#if defined(__CUDACC__)
+#define RLC_TRIG_HD __host__ __device__ __forceinline__
+#else
+#define RLC_TRIG_HD static inline
+#endif
+
+namespace rlc_trig {
+
+struct F2 {
+    float h, l;
+};
+
+struct Row {
+    float sh, sl, ch, cl;
+};
+
+#if defined(__CUDACC__)
+__device__ __align__(16) const Row kTableDev[RLC_TRIG_KMAX + 1] = {RLC_TRIG_TABLE_ROWS};
+#endif
+static const Row kTableHost[RLC_TRIG_KMAX + 1] = {RLC_TRIG_TABLE_ROWS};
+
+RLC_TRIG_HD uint32_t bits_of(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+
+RLC_TRIG_HD float float_of(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+
+RLC_TRIG_HD Row row(int k) {
+#if defined(__CUDA_ARCH__)
+    const float4 v = __ldg(reinterpret_cast<const float4*>(kTableDev) + k);
+    return Row{v.x, v.y, v.z, v.w};
+#else
+    return kTableHost[k];
+#endif
+}
+
+// s + e = a + b exactly
+RLC_TRIG_HD F2 two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return F2{s, e};
+}
+
+// s + e = a + b exactly, given a == 0 or exponent(a) >= exponent(b)
+RLC_TRIG_HD F2 fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return F2{s, b - (s - a)};
+}
+
+// p + e = a * b exactly (no underflow here)
+RLC_TRIG_HD F2 two_prod(float a, float b) {
+    const float p = a * b;
+    return F2{p, fmaf(a, b, -p)};
+}
+
+// true when h is the correctly rounded value of every number within 2^-40 |h| of h + l
+// (h normal, |l| <= half an ulp of h)
+RLC_TRIG_HD bool rounds_safely(F2 v) {
+    const float ah = fabsf(v.h);
+    const uint32_t b = bits_of(ah);
+    const float ulp = float_of(b & 0x7f800000u) * 0x1p-23f;
+    const float half = (b & 0x007fffffu) ? ulp * 0.5f : ulp * 0.25f;   // below a power of two: a quarter
+    return fabsf(v.l) + ah * 0x1p-40f < half;
+}
+
+// Fast path: returns false where the double-precision fallback must decide.
+RLC_TRIG_HD bool sincos_fast(float x, float* sp, float* cp) {
+    const float ax = fabsf(x);
+    if (!(ax < 4096.0f)) return false;   // also NaN and infinities
+    if (ax < 0x1p-12f) {
+        *sp = x;
+        *cp = 1.0f;
+        return true;
+    }
+    // 2. reduction
+    const float j = rintf(x * RLC_TRIG_TWO_OVER_PI);
+    const F2 p0 = two_prod(j, RLC_TRIG_C0);
+    const float t = x - p0.h;   // exact
+    const F2 p1 = two_prod(j, RLC_TRIG_C1);
+    const F2 a = two_sum(t, -p0.l);
+    const F2 b = two_sum(a.h, -p1.h);
+    const float tail = fmaf(j, RLC_TRIG_C3, fmaf(j, RLC_TRIG_C2, p1.l));
+    const float rest = (a.l + b.l) - tail;
+    const F2 r = fast_two_sum(b.h, rest);
+    if (j != 0.0f && fabsf(r.h) < 0x1p-16f) return false;   // the reduction's relative error grows
+    // 3. r = k/256 + u
+    const float kf = rintf(r.h * 256.0f);
+    const int k = (int)kf;
+    const float uh = r.h - kf * 0x1p-8f;   // exact
+    const F2 u = fast_two_sum(uh, r.l);
+    const F2 u2 = two_prod(u.h, u.h);
+    const float u2t = fmaf(2.0f * u.h, u.l, u2.l);                    // u^2 = u2.h + u2t (+ u.l^2)
+    const float q1 = -0.5f * u2.h;                                     // cos u = 1 + q1 + q2
+    const float q2 = fmaf(u2.h * u2.h, 1.0f / 24.0f, -0.5f * u2t);
+    const float P = u2.h * fmaf(u2.h, 1.0f / 120.0f, -1.0f / 6.0f);   // sin u = u + u P
+    const float su_l = fmaf(u.h, P, u.l);                              // sin u = u.h + su_l
+    Row T = row(k < 0 ? -k : k);
+    if (k < 0) {
+        T.sh = -T.sh;
+        T.sl = -T.sl;
+    }
+    // sin r = S + S q1 + S q2 + C u.h + C su_l
+    const F2 ms = two_prod(T.ch, u.h);
+    const F2 as = two_sum(T.sh, ms.h);
+    float cs = T.sl + as.l + ms.l;
+    cs = fmaf(T.cl, u.h, cs);
+    cs = fmaf(T.ch, su_l, cs);
+    cs = fmaf(T.sh, q2, cs);
+    cs = fmaf(T.sl, q1, cs);
+    cs = fmaf(T.sh, q1, cs);
+    const F2 sr = fast_two_sum(as.h, cs);
+    // cos r = C + C q1 + C q2 - S u.h - S su_l
+    const F2 mc = two_prod(T.sh, u.h);
+    const F2 ac = two_sum(T.ch, -mc.h);
+    float cc = T.cl + ac.l - mc.l;
+    cc = fmaf(-T.sl, u.h, cc);
+    cc = fmaf(-T.sh, su_l, cc);
+    cc = fmaf(T.ch, q2, cc);
+    cc = fmaf(T.cl, q1, cc);
+    cc = fmaf(T.ch, q1, cc);
+    const F2 cr = fast_two_sum(ac.h, cc);
+    if (!rounds_safely(sr) || !rounds_safely(cr)) return false;
+    const int q = (int)j & 3;
+    const float s = sr.h, c = cr.h;
+    *sp = (q == 0) ? s : (q == 1) ? c : (q == 2) ? -s : -c;
+    *cp = (q == 0) ? c : (q == 1) ? -s : (q == 2) ? -c : s;
+    return true;
+}
+
+// the double-precision fallback, kept out of line on the device (it is rarely taken)
+#if defined(__CUDACC__)
+static __device__ __noinline__ float2 sincos_slow_dev(float x) {
+    double sd, cd;
+    sincos((double)x, &sd, &cd);
+    return make_float2((float)sd, (float)cd);
+}
+#endif
+
+// The float nearest to sin(x) and to cos(x).
+RLC_TRIG_HD void sincos_cr(float x, float* sp, float* cp) {
+    if (sincos_fast(x, sp, cp)) return;
+#if defined(__CUDA_ARCH__)
+    const float2 v = sincos_slow_dev(x);
+    *sp = v.x;
+    *cp = v.y;
+#else
+    const double xd = (double)x;
+    *sp = (float)sin(xd);
+    *cp = (float)cos(xd);
+#endif
+}
+
+}  // namespace rlc_trig

@@ -182,8 +182,49 @@ def cddt_json_loads(text: str) -> dict:
 
 
 def _quaternion_yaw(q) -> float:
-    x, y, z, w = q.x, q.y, q.z, q.w
-    return float(np.arctan2(2.0 * (w * z + x * y), 1.0 - 2.0 * (y * y + z * z)))
+    """Yaw of a geometry_msgs/Quaternion-shaped object, as the reference's quaternion_to_angle
+    (RangeLibc.pyx:122-128) gets it from ROS tf.transformations.euler_from_quaternion with its
+    default axes 'sxyz': the quaternion (x, y, z, w) is scaled by sqrt(2 / |q|^2), the rotation
+    matrix's entries M[0][0] = 1 - q_y^2 - q_z^2 and M[1][0] = q_x q_y + q_z q_w are formed from
+    the scaled components, and the yaw is atan2(M[1][0], M[0][0]) -- 0 for a near-zero quaternion
+    (identity matrix) and at gimbal lock (sqrt(M[0][0]^2 + M[1][0]^2) <= 4 eps)."""
+    eps = float(np.finfo(np.float64).eps) * 4.0
+    v = np.array([q.x, q.y, q.z, q.w], np.float64)
+    n = float(np.dot(v, v))
+    if n < eps:
+        return 0.0
+    v *= np.sqrt(2.0 / n)
+    m00 = 1.0 - v[1] * v[1] - v[2] * v[2]
+    m10 = v[0] * v[1] + v[2] * v[3]
+    if not np.sqrt(m00 * m00 + m10 * m10) > eps:
+        return 0.0
+    return float(np.arctan2(m10, m00))
+
+
+def occupancy_grid_parts(msg):
+    """Grid and world parameters of a nav_msgs/OccupancyGrid-shaped message, as PyOMap's ROS
+    branch builds them (RangeLibc.pyx:146-167): ``data`` reshaped to (height, width) rows, a cell
+    occupied when its value is > 10 (-1 unknown and 0..10 free), OMap(height, width) so that
+    grid[x][y] = data[x, y] (x the row); world scale = resolution, angle = -yaw of the origin's
+    orientation, origin = the origin's position, and the angle's sine and cosine.  Returns
+    (occ[x, y] uint8 of shape (height, width), world tuple)."""
+    info = msg.info
+    width, height = int(info.width), int(info.height)
+    arr = np.asarray(msg.data, dtype=np.int64).reshape((height, width))
+    occ = np.ascontiguousarray(arr > 10, dtype=np.uint8)
+    angle = -1.0 * _quaternion_yaw(info.origin.orientation)
+    world = (float(info.resolution), angle, float(info.origin.position.x), float(info.origin.position.y),
+             float(np.sin(angle)), float(np.cos(angle)))
+    return occ, world
+
+
+def trig_eval(x) -> np.ndarray:
+    """(sin, cos) pairs [n, 2] that the BL and RM casts use for headings x when no trig override
+    is set: the floats nearest to the exact values, computed on the device (rlc_trig_eval)."""
+    x = np.ascontiguousarray(x, np.float32).reshape(-1)
+    out = np.empty((x.size, 2), np.float32)
+    call("rlc_trig_eval", x.ctypes.data, out.ctypes.data, x.size, 0, None)
+    return out
 
 
 # ---------------------------------------------------------------- PyOMap
@@ -210,13 +251,7 @@ class PyOMap:
         elif isinstance(arg1, np.ndarray):
             occ = np.ascontiguousarray((arg1 != 0).T, dtype=np.uint8)
         elif hasattr(arg1, "info") and hasattr(arg1, "data"):
-            info = arg1.info
-            width, height = int(info.width), int(info.height)
-            arr = np.asarray(arg1.data, dtype=np.int64).reshape((height, width))
-            occ = np.ascontiguousarray(arr > 10, dtype=np.uint8)
-            angle = -1.0 * _quaternion_yaw(info.origin.orientation)
-            world = (float(info.resolution), angle, float(info.origin.position.x), float(info.origin.position.y),
-                     float(np.sin(angle)), float(np.cos(angle)))
+            occ, world = occupancy_grid_parts(arg1)
         elif isinstance(arg1, str):
             self.fn = arg1
             occ = self._from_png(arg1, 128.0)
