@@ -55,7 +55,7 @@ def _host_eval(exe, x):
 
 def _sample():
     rng = np.random.default_rng(17)
-    bits = np.arange(np.float32(-16).view(np.uint32) & 0x7FFFFFFF, 0, -509, dtype=np.int64)
+    bits = np.arange(int(np.float32(16).view(np.uint32)), 0, -509, dtype=np.int64)
     xs = [np.concatenate([bits, bits | 0x80000000]).astype(np.uint32).view(np.float32),
           rng.uniform(-4096, 4096, 500_000).astype(np.float32),
           rng.uniform(-11.0, 0.0, 500_000).astype(np.float32),
