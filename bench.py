@@ -171,7 +171,18 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------- distributed
+_DIST = None
+
+
 def dist_init():
+    """(rank, world size, torch.distributed or None); the process group is set up once."""
+    global _DIST
+    if _DIST is None:
+        _DIST = _dist_setup()
+    return _DIST
+
+
+def _dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, None
@@ -274,9 +285,10 @@ def run_reference(args):
 # of the same workload (the k_fused and k_batch summaries under profiles/)
 FUSED_NCU_TRAFFIC = 512_256
 FUSED_NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"
-BATCH6_NCU_TRAFFIC = 539_045_376 + 38_185_216
-BATCH6_NCU_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 filters "
-                     "(--filters 6); the 32-filter launch is not captured")
+BATCH_NCU_TRAFFIC = {
+    6: (539_045_376 + 38_185_216, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
+                                   "filters (--filters 6)"),
+}
 
 
 # The reference's published single-call figures (Jetson TX1; CPU methods on one thread, RMGPU on
@@ -401,6 +413,9 @@ def main():
     ap.add_argument("--prune", action="store_true", help="cddt workload: pruned table (PCDDT)")
     ap.add_argument("--filters", type=int, default=32, help="batch workload: number of filters")
     ap.add_argument("--no-plain", action="store_true", help="batch workload: skip the per-call comparisons")
+    ap.add_argument("--oracle-check", action="store_true", help="batch workload: check the weights against the oracle")
+    ap.add_argument("--no-north-star", action="store_true",
+                    help="fused workload: skip the batched and learned figures added to its line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", default=None,
                     help="fixed schedule instead of the autotuner (for profiling): fused 'layout,block,prefetch,tile', "
@@ -412,11 +427,13 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
-        return run_batch(args)
+        run_batch(args, oracle_check=args.oracle_check)
+        return 0
     if args.workload == "cddt":
         return run_cddt(args)
     if args.workload == "learned":
-        return run_learned(args)
+        run_learned(args)
+        return 0
     if args.workload == "glt":
         return run_glt(args)
     if args.workload == "radial":
@@ -452,11 +469,16 @@ def main():
         return 2
 
     # autotune the schedule on this workload (or take the given one), then warm up
+    tune_table = None
     if args.workload == "fused":
         if args.schedule:
             method.set_schedule(*[int(v) for v in args.schedule.split(",")])
         else:
-            method.autotune(ins, angles, obs, weights)
+            # the timed steps run after an L2 flush, so the candidates are timed the same way
+            method.autotune(ins, angles, obs, weights, flush_l2=True)
+            res = sorted(method.autotune_results(), key=lambda r: r[2] if r[2] is not None else 1e9 + r[1])
+            tune_table = [{"schedule": list(sc), "median_ms": round(m1, 5),
+                           "final_median_ms": None if m2 is None else round(m2, 5)} for sc, m1, m2 in res[:6]]
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -549,7 +571,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 ranges / f64 weights", "data": "synthetic",
             "config": dict(pf_config(args.workload, n, na), l2="flushed before every step (256 MiB write)"),
-            "schedule": dict(zip(("dt_layout", "block", "prefetch", "tile"), method.schedule())),
+            "schedule": dict(zip(("dt_layout", "block", "prefetch", "tile"), method.schedule()),
+                             autotune_candidates=tune_table,
+                             autotune="median of 5 launches per candidate, then of 31 for the best 3, "
+                                      "L2 flushed before each"),
             "particle_updates_per_s": value / na,
             "e2e": {"value": e2e, "unit": "rays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "particle_updates_per_s": e2e / na},
@@ -558,6 +583,11 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
         }
+    if args.workload == "fused" and not args.no_north_star:
+        line_ns = north_star_figures(args, value)
+        if rank == 0:
+            line["north_star"] = line_ns
+    if rank == 0:
         s = json.dumps(line)
         print(s)
         if args.out:
@@ -566,6 +596,28 @@ def main():
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def north_star_figures(args, fused_value):
+    """The ratios the metric names, measured in the same run as the particle-filter step: the
+    32-filter batch against plain per-call GPU casts (weights checked against the oracle), and the
+    learned surrogate against the exact path."""
+    out = {}
+    b = run_batch(args, emit=False, oracle_check=True)
+    out["batched"] = {k: b.get(k) for k in (
+        "value", "unit", "ms_per_step", "particle_updates_per_s", "plain_per_call_rays_per_s",
+        "per_filter_fused_rays_per_s", "batched_over_plain", "weights_equal_plain", "weights_vs_oracle",
+        "roofline", "clocks", "gpu_launches")}
+    out["batched"]["config"] = b.get("config")
+    ln = run_learned(args, emit=False)
+    out["learned"] = {k: ln.get(k) for k in (
+        "value", "unit", "ms_per_step", "exact_repeat_angles_rays_per_s", "exact_fused_rays_per_s",
+        "learned_over_exact", "fallback_rate", "heldout_t_error_px", "range_error_px_all",
+        "range_error_px_accepted", "weight_error")}
+    out["learned"]["config"] = ln.get("config")
+    out["learned"]["learned_over_batched_exact"] = ln["value"] / b["value"] if b.get("value") else None
+    out["batched_over_particle_filter_step"] = b["value"] / fused_value if fused_value else None
+    return out
 
 
 def _event_steps(torch, stream, steps, flush, step_fn):
@@ -583,11 +635,52 @@ def _event_steps(torch, stream, steps, flush, step_fn):
     return [a.elapsed_time(b) for a, b in zip(starts, ends)], launches
 
 
-def run_batch(args):
+def oracle_check_batch(rl, filters, host):
+    """The batch's production weights (and ranges when kept) against the oracle on the host cores:
+    bit for bit given the device's own per-ray cos/sin, and against the oracle with the host libm
+    (the reference's own result here) the rays and particles that differ, all of them ones whose
+    cos/sin differ."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build(reference=False)
+    nt = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    res = {"filters": len(filters), "particles": 0, "bit_exact_given_same_trig": True, "trig_differs_rays": 0,
+           "weights_differ_from_host_libm": 0, "weights_rel_diff_above_1e-6": 0, "explained_by_trig": True}
+    for f, wl in zip(filters, host):
+        meth, w = f[0], f[4].cpu().numpy()
+        n, na = len(wl.ins), len(wl.angles)
+        world = tuple(float(np.float32(v)) for v in wl.world)
+        ref = O.OracleMethod(wl.occ, "rm", wl.max_range, world=world)
+        ref.set_sensor_model(wl.table)
+        xyh, trig_libm = O.world_rays(world, wl.ins, wl.angles)
+        trig_cr = np.ascontiguousarray(rl.trig_eval(xyh[:, 2])[:, ::-1])
+        del xyh
+        tdiff = np.any(trig_cr.view(np.uint32) != trig_libm.view(np.uint32), axis=1)
+        ref.set_trig_override(trig_cr)
+        w_cr = ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=nt)
+        ref.set_trig_override(None)
+        w_libm = ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=nt)
+        res["particles"] += n
+        res["trig_differs_rays"] += int(tdiff.sum())
+        res["bit_exact_given_same_trig"] &= bool(np.array_equal(w.view(np.uint64), w_cr.view(np.uint64)))
+        wd = w.view(np.uint64) != w_libm.view(np.uint64)
+        res["weights_differ_from_host_libm"] += int(wd.sum())
+        res["explained_by_trig"] &= not bool(np.any(wd & ~tdiff.reshape(n, na).any(axis=1)))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            rel = np.where(w_libm != 0, np.abs(w - w_libm) / np.abs(w_libm), np.where(w == 0, 0.0, np.inf))
+        res["weights_rel_diff_above_1e-6"] += int(np.sum(rel > 1e-6))
+    res["oracle_s"] = time.perf_counter() - t0
+    res["oracle_threads"] = nt
+    return res
+
+
+def run_batch(args, emit=True, oracle_check=False):
     """32 uneven particle filters (maps 512-4096 px, 500-20,000 particles, 30-1,081 beams,
     max_range 100-400 px) updated by one persistent launch replayed as a CUDA graph, against
     per-filter plain calls (cast to ranges, then the sensor model, host buffers -- the
-    reference's per-call pattern) and per-filter fused device calls."""
+    reference's per-call pattern) and per-filter fused device calls.  Returns the JSON line
+    (printed when `emit`); `oracle_check` adds the weights' check against the oracle."""
     import torch
     import range_libc_gb300.range_libc as rl
     from range_libc_gb300 import workloads as W
@@ -646,11 +739,12 @@ def run_batch(args):
     ref_w = [f[4].cpu().numpy().copy() for f in filters]
     if args.no_plain:
         total_b = max_over_ranks(dist, sum(tb))
-        if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": ws * rays * args.steps / (total_b / 1e3), "unit": "rays/s",
-                              "ms_per_step": total_b / args.steps, "filters": len(filters), "rays_per_step": rays,
-                              "gpu_launches": launches}))
-        return 0
+        short = {"metric": METRIC, "value": ws * rays * args.steps / (total_b / 1e3), "unit": "rays/s",
+                 "ms_per_step": total_b / args.steps, "filters": len(filters), "rays_per_step": rays,
+                 "gpu_launches": launches}
+        if rank == 0 and emit:
+            print(json.dumps(short))
+        return short
     for _ in range(args.warmup):
         per_filter_fused()
     tf, _ = _event_steps(torch, stream, args.steps, flush, per_filter_fused)
@@ -684,8 +778,9 @@ def run_batch(args):
     alg_bytes = particles * (12 + 8) + rays * (8 + 4) + 4 * steps_total
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (total_b / args.steps / 1e3) / 1e9
+    traffic, traffic_src = BATCH_NCU_TRAFFIC.get(len(filters), (None, None))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": BATCH6_NCU_TRAFFIC if len(filters) == 6 else None, "traffic_source": BATCH6_NCU_SOURCE,
+                "traffic": traffic, "traffic_source": traffic_src,
                 "peak_source": f"hbm_gbs burst ({peak_kind})", "algorithmic_bytes_per_launch": alg_bytes,
                 "mean_march_steps_per_ray": steps_total / rays, "kernel": "k_batch (persistent cast + products)"}
     line = {
@@ -704,12 +799,14 @@ def run_batch(args):
         "weights_equal_per_filter_fused": same, "weights_equal_plain": same_plain,
         "gpu_launches": launches, "setup_s": setup_s, "roofline": roofline, "clocks": clk,
     }
-    if rank == 0:
+    if oracle_check and rank == 0:
+        line["weights_vs_oracle"] = oracle_check_batch(rl, filters, host)
+    if rank == 0 and emit:
         print(json.dumps(line))
         if args.out:
             with open(args.out, "w") as f:
                 f.write(json.dumps(line) + "\n")
-    return 0
+    return line
 
 
 def run_cddt(args):
@@ -911,10 +1008,11 @@ def run_radial(args):
     return 0
 
 
-def run_learned(args):
+def run_learned(args, emit=True):
     """Learned range surrogate on a 4096^2 rectangles-and-disks map: train on rays from the
     exact marcher, then 10,000 particles x 108 beams through the learned query (accept check +
-    exact recast) against the exact path; range and weight errors on the same queries."""
+    exact recast) against the exact path; range and weight errors on the same queries.  Returns
+    the JSON line (printed when `emit`)."""
     import torch
     import range_libc_gb300.range_libc as rl
     from range_libc_gb300 import workloads as W
@@ -1010,12 +1108,12 @@ def run_learned(args):
                          "median_abs_log": float(np.median(logw)) if len(logw) else None},
         "gpu_launches": None,
     }
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line))
         if args.out:
             with open(args.out, "w") as f:
                 f.write(json.dumps(line) + "\n")
-    return 0
+    return line
 
 
 if __name__ == "__main__":

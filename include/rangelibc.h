@@ -220,7 +220,8 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
  * max(d * 0.999, 1) (0 on occupied cells), 3 = beam-major fused update that stages each bundle's
  * window of 8-bit squared distances in shared memory (RM only; tile = particle chunks per beam,
  * 0 = one block per SM) (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
- * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray; for CDDT
+ * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray, 2 = RM
+ * speculative unit runs (after a one-pixel step the next 8 cells are read together); for CDDT
  * methods prefetch selects the bin search: 0 binary, 1 warp-cooperative (32 zero points per
  * step, ballot; calc_range_many and calc_range_repeat_angles), 2 by 32-byte sectors for bins of
  * more than 32 zero points (fewer dependent reads; pays when queries spread over the map); tile =
@@ -229,9 +230,20 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
 RLC_API int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile);
 RLC_API int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_block, int* prefetch,
                                     int* tile);
-/* Time the schedule candidates on a workload (device pointers) and keep the fastest. */
+/* Time the schedule candidates on a workload (device pointers) and keep the fastest: the median
+ * of 5 single launches for every candidate, then the median of 31 for the three fastest, taken
+ * round-robin.  rlc_method_autotune_ex with RLC_TUNE_FLUSH_L2 writes twice the L2 size before
+ * every timed launch (for callers whose maps leave L2 between updates; it holds that buffer for
+ * the call), and rlc_method_autotune_results returns the candidates of the last autotune:
+ * schedules[4 i .. 4 i + 3] = (dt_layout, fused_block, prefetch, tile) and times_ms[2 i],
+ * times_ms[2 i + 1] = first-stage and final medians (0 when not a finalist); at most `max`
+ * entries are written, *count gets the number of candidates. */
+enum rlc_tune_flags { RLC_TUNE_FLUSH_L2 = 1u };
 RLC_API int rlc_method_autotune(rlc_method* m, const float* d_ins, const float* d_angles, const float* d_obs,
                                 double* d_weights, int n, int num_angles, void* stream);
+RLC_API int rlc_method_autotune_ex(rlc_method* m, const float* d_ins, const float* d_angles, const float* d_obs,
+                                   double* d_weights, int n, int num_angles, unsigned flags, void* stream);
+RLC_API int rlc_method_autotune_results(const rlc_method* m, int max, int* count, int* schedules, float* times_ms);
 
 /* ---- distance transform without device allocation ----------------------------
  * No counterpart in the reference.  For callers that may not call cudaMalloc (real-time
@@ -272,8 +284,9 @@ typedef struct rlc_filter_desc {
 RLC_API int rlc_batch_create(const rlc_filter_desc* filters, int n_filters, int block, rlc_batch** out);
 RLC_API int rlc_batch_run(rlc_batch* b, void* stream);
 /* Schedule of the persistent launch: distance-transform layout (0 linear, 1 tiled, 2 compact
- * 16-bit, 4 step map) and prefetch of every ray-marching filter, threads per block, particles per tile
- * (0 = 32).  Results are identical under every schedule. */
+ * 16-bit, 4 step map) and march variant of every ray-marching filter (prefetch 0 plain, 1 L1
+ * prefetch, 2 speculative unit runs), threads per block, particles per tile (0 = 32).  Results
+ * are identical under every schedule. */
 RLC_API int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile);
 RLC_API int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, int* block, int* tile);
 /* Where the per-particle products run: RLC_PRODUCTS_OVERLAPPED -- inside the persistent kernel,

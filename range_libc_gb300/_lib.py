@@ -17,6 +17,7 @@ RLC_BL, RLC_RM, RLC_CDDT, RLC_PCDDT, RLC_RMGPU, RLC_GLT = range(6)
 RLC_DEVICE_PTRS = 1
 RLC_HOST_AUTO, RLC_HOST_STAGED = 0, 1
 RLC_NO_WORLD = 2
+RLC_TUNE_FLUSH_L2 = 1
 ABI_VERSION = 1
 
 _f32p = C.POINTER(C.c_float)
@@ -85,6 +86,8 @@ SIGNATURES = {
     "rlc_method_set_schedule": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
     "rlc_method_get_schedule": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p]),
     "rlc_method_autotune": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "rlc_method_autotune_ex": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_uint, _vp]),
+    "rlc_method_autotune_results": (C.c_int, [_vp, C.c_int, _i32p, _vp, _vp]),
     "rlc_distance_transform_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "rlc_learned_create": (C.c_int, [_vp, C.c_uint, C.POINTER(_vp)]),
     "rlc_learned_destroy": (C.c_int, [_vp]),

@@ -167,6 +167,9 @@ struct rlc_method {
     int fused_block = 256;
     int tile = 0;             // particles per tile of the fused kernels (0 = auto)
     bool autotune_pending = false;
+    // the last autotune: every candidate's schedule and median times (ms) of both stages
+    struct TuneResult { int layout, block, prefetch, tile; float first_ms, final_ms; };
+    std::vector<TuneResult> tune_results;
 
     ~rlc_method() {
         cudaFree(d_widths);
@@ -961,8 +964,7 @@ int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int p
     if (dt_layout < -1 || dt_layout > 4) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2, 3 or 4");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
-    if (prefetch < 0 || prefetch > (m->dkind == K_CDDT ? 2 : 1))
-        return fail(RLC_ERR_ARG, m->dkind == K_CDDT ? "prefetch must be 0, 1 or 2" : "prefetch must be 0 or 1");
+    if (prefetch < 0 || prefetch > 2) return fail(RLC_ERR_ARG, "prefetch must be 0, 1 or 2");
     if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
     if (dt_layout == -1) {
         m->autotune_pending = true;
@@ -984,95 +986,150 @@ int rlc_method_get_schedule(const rlc_method* m, int* dt_layout, int* fused_bloc
     return RLC_OK;
 }
 
-constexpr int kTuneReps = 8;   // per candidate: one warm-up launch pair, then 7 timed launches
+constexpr int kTuneFirst = 5;       // stage 1: timed launches per candidate (median)
+constexpr int kTuneFinal = 31;      // stage 2: timed launches per finalist, round-robin (median)
+constexpr int kTuneFinalists = 3;
 
-// Times every schedule candidate (distance-transform layout x RM prefetch or CDDT bin search x
-// block size x particles per tile, and the staged update) on the caller's workload with CUDA
-// events and keeps the fastest.
-int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
-                        int na, void* stream) {
+static float median_of(std::vector<float> v) {
+    if (v.empty()) return 1e30f;
+    std::sort(v.begin(), v.end());
+    return v[v.size() / 2];
+}
+
+// Times every schedule candidate (distance-transform layout x RM march variant or CDDT bin search
+// x block size x particles per tile, and the staged update) on the caller's workload with CUDA
+// events around single launches: the median of kTuneFirst launches for every candidate, then the
+// median of kTuneFinal launches for the kTuneFinalists fastest, taken round-robin so that clock
+// and neighbour drift falls on all of them alike.  With RLC_TUNE_FLUSH_L2 a write of twice the
+// L2 size precedes every timed launch (a device buffer held for the duration of the call).
+int rlc_method_autotune_ex(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
+                           int na, unsigned flags, void* stream) {
     if (int rc = check_method(m)) return rc;
     if (!m->d_table) return fail(RLC_ERR_STATE, "set_sensor_model has not been called");
     if (n <= 0) return RLC_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    cudaEvent_t e0, e1;
-    CUDA_OR_FAIL(cudaEventCreate(&e0), "autotune");
-    CUDA_OR_FAIL(cudaEventCreate(&e1), "autotune");
+    using Cand = rlc_method::TuneResult;
+    std::vector<Cand> cands;
     const int blocks[3] = {128, 256, 512};
     const int tiles[3] = {0, 16, 32};
-    float best = 1e30f;
-    int best_layout = m->layout, best_block = m->fused_block, best_pf = m->prefetch, best_tile = m->tile;
-    SensorDev sm{m->d_table, m->K};
-    cudaError_t err = cudaSuccess;
     const bool rm = m->dkind == K_RM;
     static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
-    for (int lk = 0; lk < (rm ? 4 : 1) && err == cudaSuccess; ++lk) {
-        const int li = kLayouts[lk];
-        // march variants: RM plain / prefetching; CDDT binary / sector search
-        for (int pk = 0; pk < (rm || m->dkind == K_CDDT ? 2 : 1) && err == cudaSuccess; ++pk) {
-            const int pf = (m->dkind == K_CDDT && pk) ? 2 : pk;
-            for (int bi = 0; bi < 3 && err == cudaSuccess; ++bi) {
-                for (int ti = 0; ti < 3 && err == cudaSuccess; ++ti) {
+    for (int lk = 0; lk < (rm ? 4 : 1); ++lk)
+        // march variants: RM plain / prefetching / unit runs; CDDT binary / sector search
+        for (int pk = 0; pk < (rm ? 3 : m->dkind == K_CDDT ? 2 : 1); ++pk)
+            for (int bi = 0; bi < 3; ++bi)
+                for (int ti = 0; ti < 3; ++ti) {
                     if (ti > 0 && tile_particles(na, blocks[bi], tiles[ti]) == tile_particles(na, blocks[bi], 0))
                         continue;   // same tile as the automatic choice
-                    m->layout = li;
-                    CastParams p = m->params();
-                    float total = 0.0f;
-                    for (int rep = 0; rep < kTuneReps && err == cudaSuccess; ++rep) {
-                        err = launch_fused(p, li, pf, sm, ins, angles, obs, w, n, na, blocks[bi], tiles[ti], s);
-                        if (err == cudaSuccess) err = cudaEventRecord(e0, s);
-                        if (err == cudaSuccess)
-                            err = launch_fused(p, li, pf, sm, ins, angles, obs, w, n, na, blocks[bi], tiles[ti], s);
-                        if (err == cudaSuccess) err = cudaEventRecord(e1, s);
-                        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-                        float ms = 0.0f;
-                        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-                        if (rep > 0) total += ms;
-                    }
-                    if (err == cudaSuccess && total < best) {
-                        best = total;
-                        best_layout = li;
-                        best_block = blocks[bi];
-                        best_pf = pf;
-                        best_tile = tiles[ti];
-                    }
+                    const int pf = (m->dkind == K_CDDT && pk) ? 2 : pk;
+                    cands.push_back(Cand{kLayouts[lk], blocks[bi], pf, tiles[ti], 0.0f, 0.0f});
                 }
-            }
+    if (rm) {   // beam-major update with staged windows
+        if (int rc = ensure_bins(m, (size_t)n * na)) return rc;
+        cands.push_back(Cand{DT_STAGED, 0, 0, 0, 0.0f, 0.0f});
+    }
+    void* flush = nullptr;
+    size_t flush_bytes = 0;
+    if (flags & RLC_TUNE_FLUSH_L2) {
+        int dev = 0, l2 = 0;
+        CUDA_OR_FAIL(cudaGetDevice(&dev), "autotune");
+        CUDA_OR_FAIL(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev), "autotune");
+        flush_bytes = 2 * (size_t)(l2 > 0 ? l2 : (64 << 20));
+        if (cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(RLC_ERR_NOMEM, "autotune: no room for the %zu-byte L2 flush buffer", flush_bytes);
         }
     }
-    if (rm && err == cudaSuccess) {   // beam-major update with staged windows
-        if (int rc = ensure_bins(m, (size_t)n * na)) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return rc;
-        }
-        m->layout = DT_STAGED;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    SensorDev sm{m->d_table, m->K};
+    const int saved_layout = m->layout;
+    auto launch = [&](const Cand& c) -> cudaError_t {
+        m->layout = c.layout;
         CastParams p = m->params();
-        float total = 0.0f;
-        for (int rep = 0; rep < kTuneReps && err == cudaSuccess; ++rep) {
-            err = launch_fused_staged(p, sm, ins, angles, obs, w, n, na, 0, m->d_bins, s);
-            if (err == cudaSuccess) err = cudaEventRecord(e0, s);
-            if (err == cudaSuccess) err = launch_fused_staged(p, sm, ins, angles, obs, w, n, na, 0, m->d_bins, s);
-            if (err == cudaSuccess) err = cudaEventRecord(e1, s);
-            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        if (c.layout == DT_STAGED) return launch_fused_staged(p, sm, ins, angles, obs, w, n, na, 0, m->d_bins, s);
+        return launch_fused(p, c.layout, c.prefetch, sm, ins, angles, obs, w, n, na, c.block, c.tile, s);
+    };
+    unsigned flush_round = 0;
+    auto time_once = [&](const Cand& c, float* ms) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        if (flush) e = cudaMemsetAsync(flush, (int)(++flush_round & 0xFF), flush_bytes, s);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+        if (e == cudaSuccess) e = launch(c);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+        return e;
+    };
+    for (size_t i = 0; i < cands.size() && err == cudaSuccess; ++i) {
+        err = launch(cands[i]);   // warm-up (first use of the variant)
+        std::vector<float> t;
+        for (int r = 0; r < kTuneFirst && err == cudaSuccess; ++r) {
             float ms = 0.0f;
-            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-            if (rep > 0) total += ms;
+            err = time_once(cands[i], &ms);
+            t.push_back(ms);
         }
-        if (err == cudaSuccess && total < best) {
-            best = total;
-            best_layout = DT_STAGED;
-            best_tile = 0;
-            best_pf = 0;
+        cands[i].first_ms = median_of(t);
+    }
+    std::vector<int> order(cands.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return cands[a].first_ms < cands[b].first_ms; });
+    const int nf = (int)std::min<size_t>(kTuneFinalists, order.size());
+    std::vector<std::vector<float>> fin(nf);
+    for (int r = 0; r < kTuneFinal && err == cudaSuccess; ++r)
+        for (int k = 0; k < nf && err == cudaSuccess; ++k) {
+            float ms = 0.0f;
+            err = time_once(cands[order[k]], &ms);
+            fin[k].push_back(ms);
+        }
+    int best = order.empty() ? -1 : order[0];
+    float best_ms = 1e30f;
+    for (int k = 0; k < nf; ++k) {
+        cands[order[k]].final_ms = median_of(fin[k]);
+        if (cands[order[k]].final_ms < best_ms) {
+            best_ms = cands[order[k]].final_ms;
+            best = order[k];
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    m->layout = best_layout;
-    m->fused_block = best_block;
-    m->prefetch = best_pf;
-    m->tile = best_tile;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (flush) cudaFree(flush);
+    m->layout = saved_layout;
     if (err != cudaSuccess) return cuda_fail(err, "autotune");
+    if (best >= 0) {
+        const Cand& b = cands[best];
+        m->layout = b.layout;
+        if (b.block) m->fused_block = b.block;
+        m->prefetch = b.prefetch;
+        m->tile = b.tile;
+    }
+    m->tune_results = cands;
+    return RLC_OK;
+}
+
+int rlc_method_autotune(rlc_method* m, const float* ins, const float* angles, const float* obs, double* w, int n,
+                        int na, void* stream) {
+    return rlc_method_autotune_ex(m, ins, angles, obs, w, n, na, 0, stream);
+}
+
+int rlc_method_autotune_results(const rlc_method* m, int max, int* count, int* schedules, float* times_ms) {
+    if (int rc = check_method(m)) return rc;
+    if (!count) return fail(RLC_ERR_ARG, "null output");
+    *count = (int)m->tune_results.size();
+    for (int i = 0; i < max && i < *count; ++i) {
+        const auto& r = m->tune_results[i];
+        if (schedules) {
+            schedules[4 * i] = r.layout;
+            schedules[4 * i + 1] = r.block;
+            schedules[4 * i + 2] = r.prefetch;
+            schedules[4 * i + 3] = r.tile;
+        }
+        if (times_ms) {
+            times_ms[2 * i] = r.first_ms;
+            times_ms[2 * i + 1] = r.final_ms;
+        }
+    }
     return RLC_OK;
 }
 
@@ -1277,7 +1334,7 @@ int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block,
     if (!b) return fail(RLC_ERR_ARG, "null batch handle");
     if (dt_layout < 0 || dt_layout > 4 || dt_layout == DT_STAGED)
         return fail(RLC_ERR_ARG, "dt_layout must be 0, 1, 2 or 4");
-    if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
+    if (prefetch < 0 || prefetch > 2) return fail(RLC_ERR_ARG, "prefetch must be 0, 1 or 2");
     if (block != 0 && (block < 32 || block > 512 || block % 32)) return fail(RLC_ERR_ARG, "block must be a multiple of 32 in [32, 512]");
     if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
     b->layout = dt_layout;
@@ -1311,55 +1368,86 @@ int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, in
 
 // Runs the batch under each schedule candidate (outputs are overwritten with
 // identical values), keeps the fastest.
+// Runs the batch under each schedule candidate (outputs are overwritten with identical values):
+// every candidate timed over two launches after a warm-up, then the three fastest re-timed
+// round-robin over 9 launches each (median); keeps the fastest.
 int rlc_batch_autotune(rlc_batch* b, void* stream) {
     if (!b) return fail(RLC_ERR_ARG, "null batch handle");
     cudaStream_t s = (cudaStream_t)stream;
-    cudaEvent_t e0, e1;
-    CUDA_OR_FAIL(cudaEventCreate(&e0), "batch autotune");
-    CUDA_OR_FAIL(cudaEventCreate(&e1), "batch autotune");
+    struct Cand { bool sep; int layout, pf, block, tile; float ms; };
+    std::vector<Cand> cands;
     const int blocks[2] = {256, 512};
     const int tiles[3] = {8, 16, 32};
-    float best = 1e30f;
-    int bl = b->layout, bp = b->prefetch, bb = b->block, bt = b->tile;
-    bool bs = b->separate;
-    int rc = RLC_OK;
     static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
-    for (int sp = 0; sp < 2 && !rc; ++sp)
-    for (int lk = 0; lk < 4 && !rc; ++lk)
-        for (int pf = 0, li = kLayouts[lk]; pf < 2 && !rc; ++pf)
-            for (int bi = 0; bi < 2 && !rc; ++bi)
-                for (int ti = 0; ti < 3 && !rc; ++ti) {
-                    if (!b->rm_only && (li != 0 || pf != 0)) continue;
-                    b->separate = sp != 0;
-                    b->layout = li;
-                    b->prefetch = pf;
-                    b->block = blocks[bi];
-                    b->tile = tiles[ti];
-                    if ((rc = b->build())) break;
-                    if ((rc = b->launch(s))) break;   // warm (and graph capture)
-                    cudaEventRecord(e0, s);
-                    for (int rep = 0; rep < 2 && !rc; ++rep) rc = b->launch(s);
-                    cudaEventRecord(e1, s);
-                    cudaError_t e = cudaEventSynchronize(e1);
-                    float ms = 0.0f;
-                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-                    if (e != cudaSuccess) rc = cuda_fail(e, "batch autotune");
-                    if (!rc && ms < best) {
-                        best = ms;
-                        bs = sp != 0;
-                        bl = li;
-                        bp = pf;
-                        bb = blocks[bi];
-                        bt = tiles[ti];
+    for (int sp = 0; sp < 2; ++sp)
+        for (int lk = 0; lk < 4; ++lk)
+            for (int pf = 0; pf < 3; ++pf)
+                for (int bi = 0; bi < 2; ++bi)
+                    for (int ti = 0; ti < 3; ++ti) {
+                        if (!b->rm_only && (kLayouts[lk] != 0 || pf != 0)) continue;
+                        cands.push_back(Cand{sp != 0, kLayouts[lk], pf, blocks[bi], tiles[ti], 0.0f});
                     }
-                }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    b->separate = bs;
-    b->layout = bl;
-    b->prefetch = bp;
-    b->block = bb;
-    b->tile = bt;
+    const bool s0 = b->separate;
+    const int l0 = b->layout, p0 = b->prefetch, b0 = b->block, t0 = b->tile;
+    auto apply = [&](const Cand& c) {
+        b->separate = c.sep;
+        b->layout = c.layout;
+        b->prefetch = c.pf;
+        b->block = c.block;
+        b->tile = c.tile;
+        return b->build();
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = RLC_OK;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = cuda_fail(cudaGetLastError(), "batch autotune");
+    auto time_launches = [&](int reps, float* ms) -> int {
+        if (int r = b->launch(s)) return r;   // warm (and graph capture)
+        cudaEventRecord(e0, s);
+        for (int rep = 0; rep < reps; ++rep)
+            if (int r = b->launch(s)) return r;
+        cudaEventRecord(e1, s);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+        if (e != cudaSuccess) return cuda_fail(e, "batch autotune");
+        *ms /= (float)reps;
+        return RLC_OK;
+    };
+    for (size_t i = 0; i < cands.size() && !rc; ++i) {
+        if ((rc = apply(cands[i]))) break;
+        rc = time_launches(2, &cands[i].ms);
+    }
+    std::vector<int> order(cands.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int c) { return cands[a].ms < cands[c].ms; });
+    const int nf = (int)std::min<size_t>(3, order.size());
+    std::vector<std::vector<float>> fin(nf);
+    for (int r = 0; r < 9 && !rc; ++r)
+        for (int k = 0; k < nf && !rc; ++k) {
+            float ms = 0.0f;
+            if ((rc = apply(cands[order[k]]))) break;
+            rc = time_launches(1, &ms);
+            fin[k].push_back(ms);
+        }
+    int best = -1;
+    float best_ms = 1e30f;
+    for (int k = 0; k < nf && !rc; ++k) {
+        const float med = median_of(fin[k]);
+        if (med < best_ms) {
+            best_ms = med;
+            best = order[k];
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (best >= 0) {
+        int rc2 = apply(cands[best]);
+        return rc ? rc : rc2;
+    }
+    b->separate = s0;
+    b->layout = l0;
+    b->prefetch = p0;
+    b->block = b0;
+    b->tile = t0;
     int rc2 = b->build();
     return rc ? rc : rc2;
 }

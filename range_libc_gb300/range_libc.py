@@ -461,8 +461,8 @@ class _RangeMethod:
     def set_schedule(self, dt_layout: int = 0, fused_block: int = 0, prefetch: int = 0, tile: int = 0) -> None:
         """dt_layout 0 linear / 1 tiled / 2 compact 16-bit / 4 per-cell step map / 3 beam-major
         update with staged 8-bit windows (-1: autotune on the next fused call), threads per block of the fused kernel
-        (0 keeps it), prefetch (RM: 0 plain / 1 prefetching march; CDDT: 0 binary / 1 warp-cooperative /
-        2 sector bin search), particles per tile (0 automatic; for layout 3 the particle
+        (0 keeps it), prefetch (RM: 0 plain / 1 prefetching march / 2 speculative unit runs; CDDT: 0
+        binary / 1 warp-cooperative / 2 sector bin search), particles per tile (0 automatic; for layout 3 the particle
         chunks per beam).  Results do not depend on the schedule."""
         call("rlc_method_set_schedule", self._h, int(dt_layout), int(fused_block), int(prefetch), int(tile))
 
@@ -472,13 +472,27 @@ class _RangeMethod:
         call("rlc_method_get_schedule", self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d))
         return a.value, b.value, c.value, d.value
 
-    def autotune(self, ins, angles, obs, weights) -> None:
-        """Time the schedule candidates on this workload (CUDA tensors) and keep the fastest."""
+    def autotune(self, ins, angles, obs, weights, flush_l2: bool = False) -> None:
+        """Time the schedule candidates on this workload (CUDA tensors) and keep the fastest;
+        flush_l2 writes twice the L2 size before every timed launch (maps that leave L2 between
+        updates)."""
         ptrs = [_arg(a, dt, nd, nm) for a, dt, nd, nm in ((ins, np.float32, 2, "ins"), (angles, np.float32, 1, "angles"),
                                                           (obs, np.float32, 1, "obs"), (weights, np.float64, 1, "weights"))]
         if not all(d for _, d in ptrs):
             raise ValueError("autotune takes CUDA tensors")
-        call("rlc_method_autotune", self._h, *[p for p, _ in ptrs], ins.shape[0], angles.shape[0], _stream_of(ins))
+        call("rlc_method_autotune_ex", self._h, *[p for p, _ in ptrs], ins.shape[0], angles.shape[0],
+             _lib.RLC_TUNE_FLUSH_L2 if flush_l2 else 0, _stream_of(ins))
+
+    def autotune_results(self):
+        """Candidates of the last autotune: list of ((dt_layout, fused_block, prefetch, tile),
+        first-stage median ms, final median ms or None)."""
+        n = C.c_int()
+        call("rlc_method_autotune_results", self._h, 0, C.byref(n), None, None)
+        sched = np.zeros((max(n.value, 1), 4), np.int32)
+        ms = np.zeros((max(n.value, 1), 2), np.float32)
+        call("rlc_method_autotune_results", self._h, n.value, C.byref(n), sched.ctypes.data, ms.ctypes.data)
+        return [(tuple(int(v) for v in sched[i]), float(ms[i, 0]), float(ms[i, 1]) if ms[i, 1] > 0 else None)
+                for i in range(n.value)]
 
 
 class PyBresenhamsLine(_RangeMethod):

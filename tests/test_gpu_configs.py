@@ -141,12 +141,15 @@ def test_particle_filter_step_2048_4000x61(rl, oracle_mod, pf_full):
     dev = torch.device("cuda:0")
     t = [torch.from_numpy(a).to(dev) for a in (wl.ins, wl.angles, wl.obs)]
     tw = torch.empty(n, dtype=torch.float64, device=dev)
-    meth.autotune(t[0], t[1], t[2], tw)
+    meth.autotune(t[0], t[1], t[2], tw, flush_l2=True)
     tuned = meth.schedule()
+    table = meth.autotune_results()
+    finalists = [sched for sched, _, final in table if final is not None]
+    assert len(finalists) == 3 and any(f[0] == tuned[0] and f[2:] == tuned[2:] for f in finalists)
     w = np.empty(n, np.float64)
     r = np.empty(n * na, np.float32)
     we = np.empty(n, np.float64)
-    for sched in (tuned, (0, 0, 0, 0), (4, 0, 0, 0)):
+    for sched in (tuned, (0, 0, 0, 0), (4, 0, 0, 0), (4, 0, 2, 0), (1, 0, 2, 0)):
         meth.set_schedule(*sched)
         meth.set_trig_override(trig_libm)                     # parity mode
         meth.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, w)
