@@ -220,8 +220,7 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
  * max(d * 0.999, 1) (0 on occupied cells), 3 = beam-major fused update that stages each bundle's
  * window of 8-bit squared distances in shared memory (RM only; tile = particle chunks per beam,
  * 0 = one block per SM) (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
- * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray, 2 = RM
- * speculative unit runs (after a one-pixel step the next 8 cells are read together); for CDDT
+ * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray; for CDDT
  * methods prefetch selects the bin search: 0 binary, 1 warp-cooperative (32 zero points per
  * step, ballot; calc_range_many and calc_range_repeat_angles), 2 by 32-byte sectors for bins of
  * more than 32 zero points (fewer dependent reads; pays when queries spread over the map); tile =
@@ -284,9 +283,8 @@ typedef struct rlc_filter_desc {
 RLC_API int rlc_batch_create(const rlc_filter_desc* filters, int n_filters, int block, rlc_batch** out);
 RLC_API int rlc_batch_run(rlc_batch* b, void* stream);
 /* Schedule of the persistent launch: distance-transform layout (0 linear, 1 tiled, 2 compact
- * 16-bit, 4 step map) and march variant of every ray-marching filter (prefetch 0 plain, 1 L1
- * prefetch, 2 speculative unit runs), threads per block, particles per tile (0 = 32).  Results
- * are identical under every schedule. */
+ * 16-bit, 4 step map) and prefetch of every ray-marching filter, threads per block, particles per tile
+ * (0 = 32).  Results are identical under every schedule. */
 RLC_API int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile);
 RLC_API int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, int* block, int* tile);
 /* Where the per-particle products run: RLC_PRODUCTS_OVERLAPPED -- inside the persistent kernel,

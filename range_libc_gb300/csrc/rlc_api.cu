@@ -964,7 +964,8 @@ int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int p
     if (dt_layout < -1 || dt_layout > 4) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2, 3 or 4");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
-    if (prefetch < 0 || prefetch > 2) return fail(RLC_ERR_ARG, "prefetch must be 0, 1 or 2");
+    if (prefetch < 0 || prefetch > (m->dkind == K_CDDT ? 2 : 1))
+        return fail(RLC_ERR_ARG, m->dkind == K_CDDT ? "prefetch must be 0, 1 or 2" : "prefetch must be 0 or 1");
     if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
     if (dt_layout == -1) {
         m->autotune_pending = true;
@@ -1015,8 +1016,8 @@ int rlc_method_autotune_ex(rlc_method* m, const float* ins, const float* angles,
     const bool rm = m->dkind == K_RM;
     static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
     for (int lk = 0; lk < (rm ? 4 : 1); ++lk)
-        // march variants: RM plain / prefetching / unit runs; CDDT binary / sector search
-        for (int pk = 0; pk < (rm ? 3 : m->dkind == K_CDDT ? 2 : 1); ++pk)
+        // march variants: RM plain / prefetching; CDDT binary / sector search
+        for (int pk = 0; pk < (rm || m->dkind == K_CDDT ? 2 : 1); ++pk)
             for (int bi = 0; bi < 3; ++bi)
                 for (int ti = 0; ti < 3; ++ti) {
                     if (ti > 0 && tile_particles(na, blocks[bi], tiles[ti]) == tile_particles(na, blocks[bi], 0))
@@ -1334,7 +1335,7 @@ int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block,
     if (!b) return fail(RLC_ERR_ARG, "null batch handle");
     if (dt_layout < 0 || dt_layout > 4 || dt_layout == DT_STAGED)
         return fail(RLC_ERR_ARG, "dt_layout must be 0, 1, 2 or 4");
-    if (prefetch < 0 || prefetch > 2) return fail(RLC_ERR_ARG, "prefetch must be 0, 1 or 2");
+    if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
     if (block != 0 && (block < 32 || block > 512 || block % 32)) return fail(RLC_ERR_ARG, "block must be a multiple of 32 in [32, 512]");
     if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
     b->layout = dt_layout;
@@ -1381,7 +1382,7 @@ int rlc_batch_autotune(rlc_batch* b, void* stream) {
     static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
     for (int sp = 0; sp < 2; ++sp)
         for (int lk = 0; lk < 4; ++lk)
-            for (int pf = 0; pf < 3; ++pf)
+            for (int pf = 0; pf < 2; ++pf)
                 for (int bi = 0; bi < 2; ++bi)
                     for (int ti = 0; ti < 3; ++ti) {
                         if (!b->rm_only && (kLayouts[lk] != 0 || pf != 0)) continue;

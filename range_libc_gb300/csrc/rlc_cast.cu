@@ -36,7 +36,6 @@ constexpr float kMPiUpF = 0x1.921fb6p+1f;
 constexpr float kMPiHiF = 0x1.921fb6p+1f;     // (float)M_PI
 constexpr float kMPiLoF = -0x1.777a5cp-24f;   // (float)(M_PI - kMPiHiF)
 constexpr int kPrefetch = 8;                        // RM prefetch distance (px) of the prefetching schedule
-constexpr int kUnitRun = -8;                        // RM schedule with speculative unit runs of 8 steps
 constexpr int kAnyKind = -1;                        // fused_tile: kind, layout and prefetch chosen per filter
 constexpr int kRmOnly = -2;                         // fused_tile: every filter ray-marches (LAYOUT, PF given)
 
@@ -90,84 +89,6 @@ __device__ __forceinline__ bool occ_at(const MapDev& m, int x, int y) {
 }
 
 // ------------------------------------------------------- ray marching (RM)
-// one march step's distance-transform read (cell (0, 0) when off the grid) and its step
-template <int LAYOUT>
-__device__ __forceinline__ float rm_read(const MapDev& m, bool out, int px, int py) {
-    if (LAYOUT == DT_LINEAR || LAYOUT == DT_STEP) {
-        const unsigned cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
-        return __ldg((LAYOUT == DT_STEP ? m.step : m.dt) + cell);
-    }
-    return dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
-}
-
-template <int LAYOUT>
-__device__ __forceinline__ float rm_step(float d) {
-    return LAYOUT == DT_STEP ? d : ref_maxf(__fmul_rn(d, 0.999f), 1.0f);
-}
-
-__device__ __forceinline__ float corner_range(int px, int py, float x0, float y0) {
-    const float xd = __fsub_rn(__int2float_rn(px), x0);
-    const float yd = __fsub_rn(__int2float_rn(py), y0);
-    return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
-}
-
-// RangeLib.h:927-962 with speculative unit runs.  Next to a wall the march advances exactly one
-// pixel per step (max(d * 0.999, 1) = 1 while d * 0.999 <= 1), and such runs are what make the
-// longest rays long (147 one-pixel steps along a wall in the 2048^2 corridor workload).  After a
-// unit step the next K parameters are known before any cell is read -- t_j+1 = t_j + 1, rounded
-// as the reference's own addition -- so their K cells are requested together and then checked in
-// order: the first hit, position off the grid, t reaching max_range or step that is not a unit
-// step ends the run exactly where the reference's loop is.  Results and step counts equal
-// rm_cast's; K reads overlap where the plain loop waits on each in turn.
-template <int LAYOUT, int K>
-__device__ float rm_cast_unit_runs(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps) {
-    if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
-    float t = 0.0f;
-    if (!(t < mr)) return mr;
-    for (;;) {
-        const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
-        const int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
-        const bool out = (unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H;
-        const float d = rm_read<LAYOUT>(m, out, px, py);
-        if (steps && !out) ++*steps;
-        float st = rm_step<LAYOUT>(d);
-        float tn = __fadd_rn(t, st);
-        if (out | (d <= 0.0f) | !(tn < mr)) return (out || !(d <= 0.0f)) ? mr : corner_range(px, py, x0, y0);
-        t = tn;
-        while (st == 1.0f) {
-            // the run's parameters t, t + 1, ... are formed twice (for the reads, then for the
-            // checks) rather than kept, to hold only the K cell values in registers
-            float dk[K];
-            float tj = t;
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                if (j) tj = __fadd_rn(tj, 1.0f);
-                const int qx = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, tj)));
-                const int qy = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, tj)));
-                const bool qo = (unsigned)qx >= (unsigned)m.W || (unsigned)qy >= (unsigned)m.H;
-                dk[j] = qo ? -1.0f : rm_read<LAYOUT>(m, false, qx, qy);   // -1: off the grid (no read)
-            }
-            tj = t;
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                if (j) tj = __fadd_rn(tj, 1.0f);
-                const bool qo = dk[j] < 0.0f;   // distance-transform values are >= 0
-                if (steps && !qo) ++*steps;
-                st = rm_step<LAYOUT>(dk[j]);
-                tn = __fadd_rn(tj, st);
-                if (qo | (dk[j] <= 0.0f) | !(tn < mr)) {
-                    if (qo || !(dk[j] <= 0.0f)) return mr;
-                    const int qx = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, tj)));
-                    const int qy = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, tj)));
-                    return corner_range(qx, qy, x0, y0);
-                }
-                t = tn;
-                if (st != 1.0f) break;
-            }
-        }
-    }
-}
-
 // RangeLib.h:927-962 (RayMarching::calc_range).  t grows by >= 1 per step,
 // so the loop runs at most ceil(max_range) + 1 times.
 //
@@ -177,7 +98,6 @@ __device__ float rm_cast_unit_runs(const MapDev& m, float mr, float x0, float y0
 // the prefetch is a hint and never changes a result.
 template <int LAYOUT, int PF = 0>
 __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps = nullptr) {
-    if constexpr (PF < 0) return rm_cast_unit_runs<LAYOUT, -PF>(m, mr, x0, y0, c, s, steps);
     if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
     float t = 0.0f;
     if (!(t < mr)) return mr;
@@ -833,12 +753,6 @@ __device__ __forceinline__ float cast_ray(const CastParams& p, const float* __re
     if (KIND == kRmOnly) return cast_one<K_RM, LAYOUT, PF>(p, ax, ay, h, ray);   // every filter ray-marches
     // mixed kinds: dispatch at run time
     if (p.kind == K_RM) {
-        if (pf == 2) {
-            if (layout == DT_STEP) return cast_one<K_RM, DT_STEP, kUnitRun>(p, ax, ay, h, ray);
-            if (layout == DT_U16) return cast_one<K_RM, DT_U16, kUnitRun>(p, ax, ay, h, ray);
-            if (layout == DT_TILED) return cast_one<K_RM, DT_TILED, kUnitRun>(p, ax, ay, h, ray);
-            return cast_one<K_RM, DT_LINEAR, kUnitRun>(p, ax, ay, h, ray);
-        }
         if (layout == DT_STEP)
             return pf ? cast_one<K_RM, DT_STEP, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_STEP, 0>(p, ax, ay, h, ray);
         if (layout == DT_U16)
@@ -1203,12 +1117,6 @@ inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) /
 template <template <int, int, int> class F, class... Args>
 cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
     if (kind == K_RM) {
-        if (pf == 2) {   // speculative unit runs
-            if (layout == DT_STEP) return F<K_RM, DT_STEP, kUnitRun>::run(args...);
-            if (layout == DT_U16) return F<K_RM, DT_U16, kUnitRun>::run(args...);
-            if (layout == DT_TILED) return F<K_RM, DT_TILED, kUnitRun>::run(args...);
-            return F<K_RM, DT_LINEAR, kUnitRun>::run(args...);
-        }
         if (pf) {
             if (layout == DT_STEP) return F<K_RM, DT_STEP, kPrefetch>::run(args...);
             if (layout == DT_U16) return F<K_RM, DT_U16, kPrefetch>::run(args...);
@@ -1353,12 +1261,6 @@ typedef void (*BatchKernel)(const FilterDev*, int, unsigned, unsigned*);
 template <bool SEP>
 static BatchKernel batch_kernel_t(bool rm_only, int layout, int pf) {
     if (!rm_only) return k_batch<kAnyKind, 0, 0, SEP>;
-    if (pf == 2) {
-        if (layout == DT_STEP) return k_batch<kRmOnly, DT_STEP, kUnitRun, SEP>;
-        if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, kUnitRun, SEP>;
-        if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, kUnitRun, SEP>;
-        return k_batch<kRmOnly, DT_LINEAR, kUnitRun, SEP>;
-    }
     if (pf) {
         if (layout == DT_STEP) return k_batch<kRmOnly, DT_STEP, kPrefetch, SEP>;
         if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, kPrefetch, SEP>;

@@ -202,9 +202,9 @@ def test_repeat_angles_parity(rl, oracle_mod, kind):
         g.set_schedule(0, 0, 1, 0)
         g.calc_range_repeat_angles(ins, angles, out)
         assert np.array_equal(_bits(out), _bits(exp))
-    if kind == "rm":     # every distance-transform layout and march variant
+    if kind == "rm":     # every distance-transform layout, with and without prefetch
         for layout in (0, 1, 2, 4):
-            for pf in (0, 1, 2):
+            for pf in (0, 1):
                 g.set_schedule(layout, 0, pf, 0)
                 g.calc_range_repeat_angles(ins, angles, out)
                 assert np.array_equal(_bits(out), _bits(exp)), (layout, pf)
@@ -253,7 +253,7 @@ def test_narrow_corridor_parity(rl, oracle_mod, mr):
     obs = (np.linspace(1, 30, 31) % mr).astype(np.float32)
     exp_w = ref.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs)
     for layout in (0, 1, 2, 4):
-        for pf in (0, 1, 2):   # plain, prefetching, speculative unit runs
+        for pf in (0, 1):
             g.set_schedule(layout, 0, pf, 0)
             g.set_trig_override(trig)
             out = np.empty(len(q), np.float32)
@@ -696,7 +696,7 @@ def test_batch_matches_per_filter_calls(rl, oracle_mod):
 
 
 def test_batch_of_ray_marchers_schedules(rl):
-    """The ray-marching-only persistent kernel: every layout and march variant gives the per-filter weights."""
+    """The ray-marching-only persistent kernel: every layout and prefetch gives the per-filter weights."""
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda:0")
     filters, expect, keep = [], [], []
@@ -714,7 +714,7 @@ def test_batch_of_ray_marchers_schedules(rl):
         keep.append(m)
     batch = rl.PyFilterBatch(filters)
     for layout in (0, 1, 2, 4):
-        for pf in (0, 1, 2):
+        for pf in (0, 1):
             batch.set_schedule(layout, pf, 256, 16)
             batch.run()
             torch.cuda.synchronize()
@@ -723,7 +723,7 @@ def test_batch_of_ray_marchers_schedules(rl):
 
 
 def test_results_do_not_depend_on_the_schedule(rl):
-    """Every schedule (DT layout x march variant x block size x tile) gives bit-identical ranges and weights."""
+    """Every schedule (DT layout x prefetch x block size x tile) gives bit-identical ranges and weights."""
     torch = pytest.importorskip("torch")
     wl = _pf(n=700, side=1024)
     m = _pymap(rl, wl.occ, wl.world)
@@ -735,7 +735,7 @@ def test_results_do_not_depend_on_the_schedule(rl):
     g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, base_w)
     g.calc_range_repeat_angles(wl.ins, wl.angles, base_r)
     for layout in (0, 1, 2, 3, 4):
-        for pf in (0, 1, 2):
+        for pf in (0, 1):
             for block in (64, 128, 512):
                 for tile in (0, 1, 7, 32):
                     g.set_schedule(layout, block, pf, tile)
