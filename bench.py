@@ -283,11 +283,17 @@ def run_reference(args):
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one `ncu --set full` capture
 # of the same workload (the k_fused and k_batch summaries under profiles/)
-FUSED_NCU_TRAFFIC = 512_256
-FUSED_NCU_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"
+# per distance-transform layout of the fused kernel (the schedules the autotuner picks here)
+FUSED_NCU_TRAFFIC = {
+    0: (512_256, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"),
+    4: (522_112, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, step map>, this workload "
+                 "(mean of 2 launches: 521,984 and 522,240 B read, 0 written)"),
+}
 BATCH_NCU_TRAFFIC = {
     6: (539_045_376 + 38_185_216, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
                                    "filters (--filters 6)"),
+    32: (2_615_891_200 + 407_052_544, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch, all 32 filters, "
+                                      "schedule step map / 256 threads / 8 particles per tile / separate products"),
 }
 
 
@@ -550,8 +556,9 @@ def main():
     kern_s = (sum(per_step_ms) / args.steps) / 1e3
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / kern_s / 1e9
+    traffic, traffic_src = FUSED_NCU_TRAFFIC.get(method.schedule()[0], (None, "no capture of this layout"))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": FUSED_NCU_TRAFFIC, "traffic_source": FUSED_NCU_SOURCE,
+                "traffic": traffic, "traffic_source": traffic_src,
                 "peak_source": f"hbm_gbs burst ({peak_kind})",
                 "algorithmic_bytes_per_launch": alg_bytes, "mean_march_steps_per_ray": total_steps / rays_per_step,
                 "kernel": "k_fused (cast + sensor model)"}
