@@ -222,13 +222,18 @@ def build_pf(rl, W, args):
     return wl, omap, method
 
 
-def cpu_reference_pf(wl, world, steps, warmup, budget_s, nthreads):
+SHIPPED_BUILD = ("oracle/ C restatement built with the reference's shipped flags (-O3 -ffast-math "
+                 "-fno-math-errno, -march=native spelled -mcpu=neoverse-v2 on Grace)")
+
+
+def cpu_reference_pf(wl, world, steps, warmup, budget_s, nthreads, fast=True):
     """The reference algorithm (C restatement, oracle/) on the host cores: full
-    particle-filter steps until `budget_s` seconds or `steps` steps."""
+    particle-filter steps until `budget_s` seconds or `steps` steps.  fast: the build with the
+    reference's shipped optimisation flags (the speed baseline); else the strict parity build."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build(reference=False)
-    ref = O.OracleMethod(wl.occ, "rm", wl.max_range, world=world)
+    ref = O.OracleMethod(wl.occ, "rm", wl.max_range, world=world, fast=fast)
     ref.set_sensor_model(wl.table)
     for _ in range(max(warmup, 0)):
         ref.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, nthreads=nthreads)
@@ -262,6 +267,7 @@ def run_reference(args):
     nthreads = os.cpu_count() or 1
     val, done, el = cpu_reference_pf(wl, world, args.steps, args.warmup, budget_s=60.0, nthreads=nthreads)
     v1, d1, e1 = cpu_reference_pf(wl, world, 1000, 1, budget_s=5.0, nthreads=1)
+    vs, ds, es = cpu_reference_pf(wl, world, 1000, 1, budget_s=5.0, nthreads=nthreads, fast=False)
     n, na = len(wl.ins), len(wl.angles)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": ws,
@@ -272,9 +278,11 @@ def run_reference(args):
                        l2="no device cache to flush: host CPU run"),
         "particle_updates_per_s": val / na,
         "cpu_baseline": {"value": val, "unit": "rays/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{done} full steps ({n}x{na} rays each), oracle/ C restatement, "
-                                   f"{nthreads} threads",
-                         "single_thread": {"value": v1, "sample": f"{d1} full steps in {e1:.1f} s, 1 thread"}},
+                         "build": "shipped flags",
+                         "sample": f"{done} full steps ({n}x{na} rays each), {SHIPPED_BUILD}, {nthreads} threads",
+                         "single_thread": {"value": v1, "sample": f"{d1} full steps in {e1:.1f} s, 1 thread"},
+                         "strict_build": {"value": vs, "sample": f"{ds} full steps in {es:.1f} s, the parity build "
+                                                                 f"(-O3 -ffp-contract=off), {nthreads} threads"}},
         "e2e": {"value": val, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -568,10 +576,13 @@ def main():
         nthreads = os.cpu_count() or 1
         v1, d1, e1 = cpu_reference_pf(wl, omap.world, steps=100000, warmup=1, budget_s=10.0, nthreads=nthreads)
         s1, sd, se = cpu_reference_pf(wl, omap.world, steps=100000, warmup=1, budget_s=3.0, nthreads=1)
-        cpu = {"value": v1, "unit": "rays/s", "cores": nthreads, "kind": "port",
-               "sample": f"{d1} full steps ({n}x{na} rays each) in {e1:.1f} s, oracle/ C restatement, "
-                         f"{nthreads} threads",
-               "single_thread": {"value": s1, "sample": f"{sd} full steps in {se:.1f} s, 1 thread"}}
+        vs, ds, es = cpu_reference_pf(wl, omap.world, steps=100000, warmup=1, budget_s=3.0, nthreads=nthreads,
+                                      fast=False)
+        cpu = {"value": v1, "unit": "rays/s", "cores": nthreads, "kind": "port", "build": "shipped flags",
+               "sample": f"{d1} full steps ({n}x{na} rays each) in {e1:.1f} s, {SHIPPED_BUILD}, {nthreads} threads",
+               "single_thread": {"value": s1, "sample": f"{sd} full steps in {se:.1f} s, 1 thread"},
+               "strict_build": {"value": vs, "sample": f"{ds} full steps in {es:.1f} s, the parity build "
+                                                       f"(-O3 -ffp-contract=off), {nthreads} threads"}}
 
     if rank == 0:
         line = {

@@ -23,6 +23,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", platform.machine(), "librlc_oracle.so")
+ORACLE_FAST_SO = os.path.join(HERE, "_build", platform.machine(), "librlc_oracle_fast.so")
 REF_SO = os.path.join(HERE, "_ref", "librlc_ref.so")
 REF_FAST_SO = os.path.join(HERE, "_ref", "librlc_ref_fast.so")
 
@@ -93,56 +94,63 @@ class _Cddt(C.Structure):
     ]
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(ORACLE_SO):
+def lib(fast: bool = False):
+    """The strict oracle build, or (fast=True) the same code built with the reference's shipped
+    flags -- a speed baseline whose results are not the oracle's."""
+    key = bool(fast)
+    if key not in _libs:
+        path = ORACLE_FAST_SO if fast else ORACLE_SO
+        if not os.path.exists(path):
             build(reference=False)
-        L = C.CDLL(ORACLE_SO)
-        L.orc_edt.argtypes = [_u8p, C.c_int, C.c_int, _f32p]
-        L.orc_edge_map.argtypes = [_u8p, C.c_int, C.c_int, _u8p]
-        for fn in ("orc_rm_calc_range", "orc_bl_calc_range"):
-            getattr(L, fn).restype = C.c_float
-        L.orc_rm_calc_range.argtypes = [_f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
-        L.orc_rm_calc_range_trig.argtypes = [_f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
-        L.orc_rm_calc_range_trig.restype = C.c_float
-        L.orc_bl_calc_range.argtypes = [_u8p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
-        L.orc_bl_calc_range_trig.argtypes = [_u8p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
-        L.orc_bl_calc_range_trig.restype = C.c_float
-        L.orc_cddt_build.argtypes = [_u8p, C.c_int, C.c_int, C.c_float, C.c_uint]
-        L.orc_cddt_build.restype = C.POINTER(_Cddt)
-        L.orc_cddt_prune.argtypes = [C.POINTER(_Cddt), C.c_float]
-        L.orc_cddt_free.argtypes = [C.POINTER(_Cddt)]
-        L.orc_cddt_calc_range.argtypes = [C.POINTER(_Cddt), C.c_float, C.c_float, C.c_float, _i32p]
-        L.orc_cddt_calc_range.restype = C.c_float
-        L.orc_cddt_num_zeros.argtypes = [C.POINTER(_Cddt)]
-        L.orc_cddt_num_zeros.restype = C.c_int64
-        L.orc_cddt_load.argtypes = [C.POINTER(_Cddt), _i32p, _f32p, _i64p, _f32p, C.c_int64]
-        L.orc_cddt_discretize.argtypes = [C.POINTER(_Cddt), C.c_float, _i32p, _f32p, _i32p]
-        mp = C.POINTER(_Method)
-        L.orc_numpy_calc_range.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int]
-        L.orc_calc_range_many_raw.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int]
-        L.orc_numpy_calc_range_angles.argtypes = [mp, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int]
-        L.orc_eval_sensor_model.argtypes = [mp, _f32p, _f32p, _f64p, C.c_int, C.c_int, C.c_int]
-        L.orc_calc_range_repeat_angles_eval_sensor_model.argtypes = [mp, _f32p, _f32p, _f32p, _f64p, C.c_int, C.c_int, C.c_int]
-        L.orc_method_calc_range.argtypes = [mp, C.c_float, C.c_float, C.c_float, _i32p]
-        L.orc_method_calc_range.restype = C.c_float
-        L.orc_world_rays.argtypes = [C.POINTER(_World), _f32p, _f32p, C.c_int, C.c_int, _f32p, _f32p]
-        L.orc_mean_steps.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int]
-        L.orc_mean_steps.restype = C.c_double
-        L.orc_cddt_calc_range_pair.argtypes = [C.POINTER(_Cddt), C.c_float, C.c_float, C.c_float, _f32p, _f32p]
-        L.orc_cddt_radial.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int, C.c_float, C.c_float]
-        L.orc_glt_build.argtypes = [_f32p, C.c_int, C.c_int, C.c_float, C.c_uint, C.c_int]
-        L.orc_glt_build.restype = C.POINTER(_Glt)
-        L.orc_glt_free.argtypes = [C.POINTER(_Glt)]
-        L.orc_glt_calc_range.argtypes = [C.POINTER(_Glt), C.c_float, C.c_float, C.c_float]
-        L.orc_glt_calc_range.restype = C.c_float
-        L.orc_glt_discretize.argtypes = [C.POINTER(_Glt), C.c_float]
-        _lib = L
-    return _lib
+        _libs[key] = _bind(C.CDLL(path))
+    return _libs[key]
+
+
+def _bind(L):
+    """Argument and result types of the oracle's C functions on the loaded library L."""
+    L.orc_edt.argtypes = [_u8p, C.c_int, C.c_int, _f32p]
+    L.orc_edge_map.argtypes = [_u8p, C.c_int, C.c_int, _u8p]
+    for fn in ("orc_rm_calc_range", "orc_bl_calc_range"):
+        getattr(L, fn).restype = C.c_float
+    L.orc_rm_calc_range.argtypes = [_f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
+    L.orc_rm_calc_range_trig.argtypes = [_f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
+    L.orc_rm_calc_range_trig.restype = C.c_float
+    L.orc_bl_calc_range.argtypes = [_u8p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
+    L.orc_bl_calc_range_trig.argtypes = [_u8p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, _i32p]
+    L.orc_bl_calc_range_trig.restype = C.c_float
+    L.orc_cddt_build.argtypes = [_u8p, C.c_int, C.c_int, C.c_float, C.c_uint]
+    L.orc_cddt_build.restype = C.POINTER(_Cddt)
+    L.orc_cddt_prune.argtypes = [C.POINTER(_Cddt), C.c_float]
+    L.orc_cddt_free.argtypes = [C.POINTER(_Cddt)]
+    L.orc_cddt_calc_range.argtypes = [C.POINTER(_Cddt), C.c_float, C.c_float, C.c_float, _i32p]
+    L.orc_cddt_calc_range.restype = C.c_float
+    L.orc_cddt_num_zeros.argtypes = [C.POINTER(_Cddt)]
+    L.orc_cddt_num_zeros.restype = C.c_int64
+    L.orc_cddt_load.argtypes = [C.POINTER(_Cddt), _i32p, _f32p, _i64p, _f32p, C.c_int64]
+    L.orc_cddt_discretize.argtypes = [C.POINTER(_Cddt), C.c_float, _i32p, _f32p, _i32p]
+    mp = C.POINTER(_Method)
+    L.orc_numpy_calc_range.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int]
+    L.orc_calc_range_many_raw.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int]
+    L.orc_numpy_calc_range_angles.argtypes = [mp, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int]
+    L.orc_eval_sensor_model.argtypes = [mp, _f32p, _f32p, _f64p, C.c_int, C.c_int, C.c_int]
+    L.orc_calc_range_repeat_angles_eval_sensor_model.argtypes = [mp, _f32p, _f32p, _f32p, _f64p, C.c_int, C.c_int, C.c_int]
+    L.orc_method_calc_range.argtypes = [mp, C.c_float, C.c_float, C.c_float, _i32p]
+    L.orc_method_calc_range.restype = C.c_float
+    L.orc_world_rays.argtypes = [C.POINTER(_World), _f32p, _f32p, C.c_int, C.c_int, _f32p, _f32p]
+    L.orc_mean_steps.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int]
+    L.orc_mean_steps.restype = C.c_double
+    L.orc_cddt_calc_range_pair.argtypes = [C.POINTER(_Cddt), C.c_float, C.c_float, C.c_float, _f32p, _f32p]
+    L.orc_cddt_radial.argtypes = [mp, _f32p, _f32p, C.c_int, C.c_int, C.c_float, C.c_float]
+    L.orc_glt_build.argtypes = [_f32p, C.c_int, C.c_int, C.c_float, C.c_uint, C.c_int]
+    L.orc_glt_build.restype = C.POINTER(_Glt)
+    L.orc_glt_free.argtypes = [C.POINTER(_Glt)]
+    L.orc_glt_calc_range.argtypes = [C.POINTER(_Glt), C.c_float, C.c_float, C.c_float]
+    L.orc_glt_calc_range.restype = C.c_float
+    L.orc_glt_discretize.argtypes = [C.POINTER(_Glt), C.c_float]
+    return L
 
 
 def _occ(occ) -> np.ndarray:
@@ -192,10 +200,14 @@ class OracleMethod:
     """One of the reference's range methods, restated on the CPU.
 
     kind: 'bl', 'rm', 'cddt', 'pcddt' (pruned at construction) or 'glt' (GiantLUTCast with td
-    angle bins, built from the distance transform with ``nthreads`` threads).
+    angle bins, built from the distance transform with ``nthreads`` threads).  fast=True runs the
+    queries on the same restatement built with the reference's shipped flags (a speed baseline:
+    fast-math changes some results, so it is never the checker).
     """
 
-    def __init__(self, occ, kind: str, max_range: float, td: int = 108, world=None, nthreads: int = 1):
+    def __init__(self, occ, kind: str, max_range: float, td: int = 108, world=None, nthreads: int = 1,
+                 fast: bool = False):
+        self._L = lib(fast)
         self.occ = _occ(occ)
         self.width, self.height = self.occ.shape
         self.kind_name = kind
@@ -205,11 +217,11 @@ class OracleMethod:
         self.dt = edt(self.occ) if self.kind in (RM, GLT) else None
         self.glt = None
         if self.kind == GLT:
-            self.glt = lib().orc_glt_build(_ptr(self.dt, _f32p), self.width, self.height,
+            self.glt = self._L.orc_glt_build(_ptr(self.dt, _f32p), self.width, self.height,
                                            C.c_float(self.max_range), td, nthreads)
         self.cddt = None
         if self.kind == CDDT:
-            self.cddt = lib().orc_cddt_build(_ptr(self.occ, _u8p), self.width, self.height,
+            self.cddt = self._L.orc_cddt_build(_ptr(self.occ, _u8p), self.width, self.height,
                                              C.c_float(self.max_range), td)
             if kind == "pcddt":
                 self.prune()
@@ -240,10 +252,10 @@ class OracleMethod:
 
     def __del__(self):
         if getattr(self, "cddt", None) is not None:
-            lib().orc_cddt_free(self.cddt)
+            self._L.orc_cddt_free(self.cddt)
             self.cddt = None
         if getattr(self, "glt", None) is not None:
-            lib().orc_glt_free(self.glt)
+            self._L.orc_glt_free(self.glt)
             self.glt = None
 
     # --- GiantLUTCast table ---
@@ -256,20 +268,20 @@ class OracleMethod:
     # --- CDDT radial pairs ---
     def calc_range_pair(self, x, y, heading):
         r, ri = C.c_float(), C.c_float()
-        lib().orc_cddt_calc_range_pair(self.cddt, x, y, heading, C.byref(r), C.byref(ri))
+        self._L.orc_cddt_calc_range_pair(self.cddt, x, y, heading, C.byref(r), C.byref(ri))
         return r.value, ri.value
 
     def calc_range_many_radial_optimized(self, num_rays, min_angle, max_angle, ins, outs):
         """Fills outs [n * num_rays] in place (positions the reference does not write keep their values)."""
         ins = np.ascontiguousarray(ins, np.float32)
         assert outs.dtype == np.float32 and outs.flags.c_contiguous and outs.size == ins.shape[0] * num_rays
-        lib().orc_cddt_radial(C.byref(self._m), _ptr(ins, _f32p), _ptr(outs, _f32p), ins.shape[0], num_rays,
+        self._L.orc_cddt_radial(C.byref(self._m), _ptr(ins, _f32p), _ptr(outs, _f32p), ins.shape[0], num_rays,
                               min_angle, max_angle)
         return outs
 
     # --- CDDT table ---
     def prune(self, max_range: float | None = None):
-        lib().orc_cddt_prune(self.cddt, C.c_float(self.max_range if max_range is None else max_range))
+        self._L.orc_cddt_prune(self.cddt, C.c_float(self.max_range if max_range is None else max_range))
 
     def cddt_table(self):
         """(widths, trans, bin_len, zeros) of the CSR table."""
@@ -288,46 +300,46 @@ class OracleMethod:
         trans = np.ascontiguousarray(trans, np.float32)
         bin_len = np.ascontiguousarray(bin_len, np.int64)
         zeros = np.ascontiguousarray(zeros, np.float32)
-        rc = lib().orc_cddt_load(self.cddt, _ptr(widths, _i32p), _ptr(trans, _f32p),
+        rc = self._L.orc_cddt_load(self.cddt, _ptr(widths, _i32p), _ptr(trans, _f32p),
                                  _ptr(bin_len, _i64p), _ptr(zeros, _f32p), len(zeros))
         if rc != 0:
             raise ValueError(f"table shape mismatch ({rc})")
 
     # --- queries ---
     def calc_range(self, x, y, heading):
-        return lib().orc_method_calc_range(C.byref(self._m), x, y, heading, None)
+        return self._L.orc_method_calc_range(C.byref(self._m), x, y, heading, None)
 
     def calc_range_steps(self, x, y, heading):
         s = C.c_int(0)
-        r = lib().orc_method_calc_range(C.byref(self._m), x, y, heading, C.byref(s))
+        r = self._L.orc_method_calc_range(C.byref(self._m), x, y, heading, C.byref(s))
         return r, s.value
 
     def calc_range_trig(self, x, y, c, s):
         if self.kind == RM:
-            return lib().orc_rm_calc_range_trig(_ptr(self.dt, _f32p), self.width, self.height,
+            return self._L.orc_rm_calc_range_trig(_ptr(self.dt, _f32p), self.width, self.height,
                                                 self.max_range, x, y, c, s, None)
         if self.kind == BL:
-            return lib().orc_bl_calc_range_trig(_ptr(self.occ, _u8p), self.width, self.height,
+            return self._L.orc_bl_calc_range_trig(_ptr(self.occ, _u8p), self.width, self.height,
                                                 self.max_range, x, y, c, s, None)
         raise ValueError("trig parity mode applies to BL and RM")
 
     def calc_range_many(self, ins, nthreads=1):
         ins = np.ascontiguousarray(ins, np.float32)
         out = np.empty(ins.shape[0], np.float32)
-        lib().orc_numpy_calc_range(C.byref(self._m), _ptr(ins, _f32p), _ptr(out, _f32p), len(out), nthreads)
+        self._L.orc_numpy_calc_range(C.byref(self._m), _ptr(ins, _f32p), _ptr(out, _f32p), len(out), nthreads)
         return out
 
     def calc_range_many_raw(self, ins, nthreads=1):
         ins = np.ascontiguousarray(ins, np.float32)
         out = np.empty(ins.shape[0], np.float32)
-        lib().orc_calc_range_many_raw(C.byref(self._m), _ptr(ins, _f32p), _ptr(out, _f32p), len(out), nthreads)
+        self._L.orc_calc_range_many_raw(C.byref(self._m), _ptr(ins, _f32p), _ptr(out, _f32p), len(out), nthreads)
         return out
 
     def calc_range_repeat_angles(self, ins, angles, nthreads=1):
         ins = np.ascontiguousarray(ins, np.float32)
         angles = np.ascontiguousarray(angles, np.float32)
         out = np.empty(ins.shape[0] * len(angles), np.float32)
-        lib().orc_numpy_calc_range_angles(C.byref(self._m), _ptr(ins, _f32p), _ptr(angles, _f32p),
+        self._L.orc_numpy_calc_range_angles(C.byref(self._m), _ptr(ins, _f32p), _ptr(angles, _f32p),
                                           _ptr(out, _f32p), ins.shape[0], len(angles), nthreads)
         return out
 
@@ -339,7 +351,7 @@ class OracleMethod:
         obs = np.ascontiguousarray(obs, np.float32)
         ranges = np.ascontiguousarray(ranges, np.float32)
         out = np.empty(num_particles, np.float64)
-        lib().orc_eval_sensor_model(C.byref(self._m), _ptr(obs, _f32p), _ptr(ranges, _f32p),
+        self._L.orc_eval_sensor_model(C.byref(self._m), _ptr(obs, _f32p), _ptr(ranges, _f32p),
                                     _ptr(out, _f64p), num_rays, num_particles, nthreads)
         return out
 
@@ -348,7 +360,7 @@ class OracleMethod:
         angles = np.ascontiguousarray(angles, np.float32)
         obs = np.ascontiguousarray(obs, np.float32)
         out = np.empty(ins.shape[0], np.float64)
-        lib().orc_calc_range_repeat_angles_eval_sensor_model(
+        self._L.orc_calc_range_repeat_angles_eval_sensor_model(
             C.byref(self._m), _ptr(ins, _f32p), _ptr(angles, _f32p), _ptr(obs, _f32p),
             _ptr(out, _f64p), ins.shape[0], len(angles), nthreads)
         return out
@@ -359,7 +371,7 @@ class OracleMethod:
         if angles is not None:
             angles = np.ascontiguousarray(angles, np.float32)
             ap = _ptr(angles, _f32p)
-        return lib().orc_mean_steps(C.byref(self._m), _ptr(ins, _f32p), ap, ins.shape[0],
+        return self._L.orc_mean_steps(C.byref(self._m), _ptr(ins, _f32p), ap, ins.shape[0],
                                     1 if angles is None else len(angles))
 
 
