@@ -596,7 +596,7 @@ def main():
                                       "L2 flushed before each"),
             "particle_updates_per_s": value / na,
             "step_us": {"min": 1e3 * min(per_step_ms), "median": 1e3 * statistics.median(per_step_ms),
-                        "max": 1e3 * max(per_step_ms)},
+                        "max": 1e3 * max(per_step_ms), "max_at_step": per_step_ms.index(max(per_step_ms))},
             "e2e": {"value": e2e, "unit": "rays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "particle_updates_per_s": e2e / na},
             "gpu_launches": launches,

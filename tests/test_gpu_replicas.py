@@ -63,9 +63,9 @@ def _replica(rank, world, port, out):
 
 def test_two_library_replicas_on_one_gpu():
     world, port = 2, _free_port()
-    with mp.Manager() as mgr:
+    ctx = mp.get_context("spawn")   # no fork of a process that may hold a CUDA context
+    with ctx.Manager() as mgr:
         out = mgr.dict()
-        ctx = mp.get_context("spawn")
         procs = [ctx.Process(target=_replica, args=(r, world, port, out)) for r in range(world)]
         for p in procs:
             p.start()

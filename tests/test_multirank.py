@@ -31,9 +31,9 @@ def _worker(rank, world, port, out):
 
 def test_two_gloo_ranks_take_the_max():
     world, port = 2, _free_port()
-    with mp.Manager() as m:
-        out = m.dict()
-        ctx = mp.get_context("spawn")
+    ctx = mp.get_context("spawn")   # no fork of a process that may hold a CUDA context
+    with ctx.Manager() as mgr:
+        out = mgr.dict()
         procs = [ctx.Process(target=_worker, args=(r, world, port, out)) for r in range(world)]
         for p in procs:
             p.start()
