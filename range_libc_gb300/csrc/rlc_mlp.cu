@@ -18,9 +18,12 @@
 #include "rlc_internal.cuh"
 #include "rlc_tc.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cmath>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -50,8 +53,8 @@ constexpr size_t kOutW = kW0 + kHidden + 3 * (kWh + kHidden);  // output weights
 enum Epi : int { EPI_F32 = 0, EPI_FWD = 1, EPI_BWD = 2, EPI_F32_ADD = 3 };
 
 struct GemmArgs {
-    const bf16* A;   // a_t ? A[k * lda + m] : A[m * lda + k]
-    const bf16* B;   // b_t ? B[k * ldb + n] : B[n * ldb + k]
+    const bf16* A;   // A[m * lda + k] (a_t and b_t must be 0: both operands K-major)
+    const bf16* B;   // B[n * ldb + k]
     int lda, ldb, a_t, b_t;
     int M, N, K;
     int ksplit;         // K range of blockIdx.z: [z * ksplit, (z + 1) * ksplit)
@@ -63,6 +66,9 @@ struct GemmArgs {
     bf16* Hout;         // EPI_FWD: GELU(z)
     const bf16* Zin;    // EPI_BWD: pre-activation of the layer below
     bf16* dZ;           // EPI_BWD: acc * GELU'(Zin)
+    bf16* HoutT;        // EPI_FWD (optional): GELU(z) transposed, [n * ldt + m]
+    bf16* dZT;          // EPI_BWD (optional): dZ transposed, [n * ldt + m]
+    int ldt;
     unsigned* err;
 };
 
@@ -87,137 +93,239 @@ __device__ __forceinline__ float gelu_grad(float z) {
     return 0.5f * (1.0f + th) + 0.5f * z * (1.0f - th * th) * k0 * (1.0f + 3.0f * k1 * z * z);
 }
 
-// load one K chunk (64) of `rows` rows of an operand into the core-matrix layout
-__device__ __forceinline__ void load_tile(uint8_t* dst, const bf16* src, int ld, int trans, int r0, int rows, int k0) {
-    const int nvec = rows * 8;   // 16-byte vectors of 8 elements
-    if (!trans) {
-        for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
-            const int row = v >> 3, kv = v & 7;
-            const uint4 val = *reinterpret_cast<const uint4*>(src + (size_t)(r0 + row) * ld + k0 + kv * 8);
-            *reinterpret_cast<uint4*>(dst + tc::core_offset(row, kv * 8)) = val;
-        }
-    } else {
-        const int rvecs = rows >> 3;
-        for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
-            const int k = v / rvecs, rv = v - k * rvecs;
-            const uint4 val = *reinterpret_cast<const uint4*>(src + (size_t)(k0 + k) * ld + r0 + rv * 8);
-            const bf16* e = reinterpret_cast<const bf16*>(&val);
-#pragma unroll
-            for (int i = 0; i < 8; ++i) *reinterpret_cast<bf16*>(dst + tc::core_offset(rv * 8 + i, k)) = e[i];
-        }
-    }
-}
+// --------------------------------------------------------------- TMA GEMM
+// C tile [128 x 256] at (blockIdx.y * 128, blockIdx.x * 256) of C = A . B^T, both operands
+// K-major in global memory (A[m * lda + k], B[n * ldb + k]), K range [z * ksplit, (z+1) * ksplit).
+//
+// Warp-specialised, one CTA per SM (192 threads, 4 pipeline stages of 48 KB):
+//   warp 0     TMA producer: per 64-wide K chunk, 8 + 8 tile loads (one per group of 8 K
+//              elements: a 128- or 256-row x 16-byte box) into stage s, completing on full[s];
+//              it reuses a stage once the MMAs that read it have committed to empty[s];
+//   warp 1     allocates 256 TMEM columns; one thread issues the chunk's four
+//              tcgen05.mma (K = 16 each) per stage and commits them to empty[s], and after the
+//              last chunk to `accum`;
+//   warps 2-5  epilogue: wait for `accum`, read the accumulator with tcgen05.ld (warp w reads
+//              TMEM lanes 32 (w % 4) .. + 31) and apply the epilogue.
+// Shared-memory operand layout (no swizzle, K-major): stage A holds 8 groups of 128 rows x
+// 16 bytes, group g (K elements 8g .. 8g + 7) at g * 2048; a core matrix (8 rows x 16 bytes) is
+// then 128 bytes, the next one along M 128 bytes on (SBO) and along K 2048 bytes on (LBO); B the
+// same with 256 rows (LBO 4096).  Every wait is bounded (about a second); a time-out sets bit 16 of
+// *err, the remaining roles stop at their next wait, and the CTA still frees its TMEM.
+constexpr int kStages = 4;
+constexpr uint32_t kStageA = kBM * tc::kKChunk * 2;   // 16 KB
+constexpr uint32_t kStageB = kBN * tc::kKChunk * 2;   // 32 KB
+constexpr size_t kTmaSmem = kStages * (size_t)(kStageA + kStageB) + 1024;   // + alignment slack
+constexpr int kGemmThreads = 192;
 
-// C tile [128 x 256] at (blockIdx.y * 128, blockIdx.x * 256): two smem stages of
-// A (16 KB) and B (32 KB), MMA issued by thread 0, accumulator in 256 TMEM columns.
-__global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+__global__ void __launch_bounds__(kGemmThreads, 1)
+k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accum;
     __shared__ uint32_t tmem_base;
-    uint8_t* sA[2] = {smem, smem + 16384};
-    uint8_t* sB[2] = {smem + 32768, smem + 65536};
-    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+    __shared__ int abort_flag, n_issued, n_consumed;
+    uint8_t* smem = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sbase = tc::smem_addr(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
+    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+    const int kbase = blockIdx.z * g.ksplit;
+    const int nchunks = g.ksplit / tc::kKChunk;
+    if (warp == 1) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
     if (threadIdx.x == 0) {
-        tc::mbar_init(tc::smem_addr(&mbar[0]), 1);
-        tc::mbar_init(tc::smem_addr(&mbar[1]), 1);
+        for (int i = 0; i < kStages; ++i) {
+            tc::mbar_init(tc::smem_addr(&full[i]), 1);
+            tc::mbar_init(tc::smem_addr(&empty[i]), 1);
+        }
+        tc::mbar_init(tc::smem_addr(&accum), 1);
+        abort_flag = 0;
+        n_issued = 0;
+        n_consumed = 0;
         tc::fence_mbar_init();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
-    const uint32_t idesc = tc::make_idesc(kBM, kBN);
-    const int kbase = blockIdx.z * g.ksplit;
-    const int nchunks = g.ksplit / tc::kKChunk;
-    bool ok = true;
-    for (int c = 0; c < nchunks && ok; ++c) {
-        const int s = c & 1;
-        if (c >= 2) {   // stage s is free once the MMAs of chunk c - 2 completed
-            const bool w = tc::mbar_wait(tc::smem_addr(&mbar[s]), ((c - 2) >> 1) & 1);
-            ok = __syncthreads_and(w) != 0;
-            if (!ok) break;
+    auto stage_a = [&](int st) { return sbase + (uint32_t)st * (kStageA + kStageB); };
+    auto stage_b = [&](int st) { return stage_a(st) + kStageA; };
+    if (warp == 0 && lane == 0) {
+        // ---- producer
+        tc::tma_prefetch_map(&tmA);
+        tc::tma_prefetch_map(&tmB);
+        for (int c = 0; c < nchunks; ++c) {
+            const int st = c % kStages;
+            if (c >= kStages && !tc::mbar_wait(tc::smem_addr(&empty[st]), ((c / kStages) - 1) & 1)) {
+                atomicOr(g.err, 16u);
+                atomicExch(&abort_flag, 1);
+                break;
+            }
+            if (*(volatile int*)&abort_flag) break;
+            const uint32_t fb = tc::smem_addr(&full[st]);
+            tc::mbar_arrive_expect_tx(fb, kStageA + kStageB);
+            const int k0 = kbase + c * tc::kKChunk;
+#pragma unroll
+            for (int gi = 0; gi < 8; ++gi) tc::tma_load_2d(stage_a(st) + gi * (kBM * 16), &tmA, k0 + gi * 8, m0, fb);
+#pragma unroll
+            for (int gi = 0; gi < 8; ++gi) tc::tma_load_2d(stage_b(st) + gi * (kBN * 16), &tmB, k0 + gi * 8, n0, fb);
+            n_issued = c + 1;
         }
-        load_tile(sA[s], g.A, g.lda, g.a_t, m0, kBM, kbase + c * tc::kKChunk);
-        load_tile(sB[s], g.B, g.ldb, g.b_t, n0, kBN, kbase + c * tc::kKChunk);
-        tc::fence_async_smem();
-        __syncthreads();
-        if (threadIdx.x == 0) {
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer
+        const uint32_t idesc = tc::make_idesc(kBM, kBN);
+        for (int c = 0; c < nchunks; ++c) {
+            const int st = c % kStages;
+            if (!tc::mbar_wait(tc::smem_addr(&full[st]), (c / kStages) & 1)) {
+                atomicOr(g.err, 16u);
+                atomicExch(&abort_flag, 1);
+                break;
+            }
             tc::fence_after_sync();
-            const uint32_t a0 = tc::smem_addr(sA[s]), b0 = tc::smem_addr(sB[s]);
 #pragma unroll
             for (int ks = 0; ks < tc::kKChunk / 16; ++ks) {
-                const uint64_t ad = tc::make_desc(a0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
-                const uint64_t bd = tc::make_desc(b0 + ks * 2 * tc::kCoreBytes, tc::kCoreBytes, tc::kRowBlockBytes);
+                const uint64_t ad = tc::make_desc(stage_a(st) + ks * 2 * (kBM * 16), kBM * 16, tc::kCoreBytes);
+                const uint64_t bd = tc::make_desc(stage_b(st) + ks * 2 * (kBN * 16), kBN * 16, tc::kCoreBytes);
                 tc::mma_bf16(tmem, ad, bd, idesc, (c > 0 || ks > 0) ? 1u : 0u);
             }
-            tc::mma_commit(tc::smem_addr(&mbar[s]));
+            tc::mma_commit(tc::smem_addr(&empty[st]));
+            n_consumed = c + 1;
         }
-    }
-    if (ok && nchunks > 0) {
-        const int cl = nchunks - 1;
-        const bool w = tc::mbar_wait(tc::smem_addr(&mbar[cl & 1]), (cl >> 1) & 1);
-        ok = __syncthreads_and(w) != 0;
-    }
-    tc::fence_after_sync();
-    if (!ok) {
-        if (threadIdx.x == 0) atomicOr(g.err, 16u);
-    } else {
-        // epilogue: warp w owns TMEM lanes (rows) 32w..32w+31
-        const int row = m0 + warp * 32 + lane;
-        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int cb = 0; cb < kBN; cb += 32) {
-            float v[32];
-            tc::tmem_ld32(lane_addr + cb, v);
-            const int col0 = n0 + cb;
-            if (g.epi == EPI_F32) {
-                float* out = g.C32 + (size_t)row * g.ldc + col0;
+        // `accum` completes once every MMA issued above has (also with none issued)
+        tc::mma_commit(tc::smem_addr(&accum));
+    } else if (warp >= 2) {
+        // ---- epilogue
+        const bool ok = tc::mbar_wait(tc::smem_addr(&accum), 0);
+        tc::fence_after_sync();
+        if (!ok) {
+            if (lane == 0) atomicOr(g.err, 16u);
+        } else if (!*(volatile int*)&abort_flag && nchunks > 0) {
+            const int lq = warp & 3;   // TMEM lane quarter this warp may read
+            const int row = m0 + lq * 32 + lane;
+            const uint32_t lane_addr = tmem + ((uint32_t)(lq * 32) << 16);
+            for (int cb = 0; cb < kBN; cb += 32) {
+                float v[32];
+                tc::tmem_ld32(lane_addr + cb, v);
+                const int col0 = n0 + cb;
+                if (g.epi == EPI_F32) {
+                    float* out = g.C32 + (size_t)row * g.ldc + col0;
 #pragma unroll
-                for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-            } else if (g.epi == EPI_F32_ADD) {
-                float* out = g.C32 + (size_t)row * g.ldc + col0;
+                    for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                } else if (g.epi == EPI_F32_ADD) {
+                    float* out = g.C32 + (size_t)row * g.ldc + col0;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) atomicAdd(out + i, v[i]);
-            } else if (g.epi == EPI_FWD) {
-                bf16* zo = g.Zout + (size_t)row * g.ldc + col0;
-                bf16* ho = g.Hout + (size_t)row * g.ldc + col0;
+                    for (int i = 0; i < 32; ++i) atomicAdd(out + i, v[i]);
+                } else if (g.epi == EPI_FWD) {
+                    bf16* zo = g.Zout + (size_t)row * g.ldc + col0;
+                    bf16* ho = g.Hout + (size_t)row * g.ldc + col0;
 #pragma unroll
-                for (int i = 0; i < 32; i += 2) {
-                    const float z0 = v[i] + __ldg(g.bias + col0 + i), z1 = v[i + 1] + __ldg(g.bias + col0 + i + 1);
-                    const __nv_bfloat162 zb = __floats2bfloat162_rn(z0, z1);
-                    *reinterpret_cast<__nv_bfloat162*>(zo + i) = zb;
-                    const float2 zf = __bfloat1622float2(zb);   // GELU of the stored (rounded) pre-activation
-                    *reinterpret_cast<__nv_bfloat162*>(ho + i) = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
-                }
-            } else {
-                const bf16* zi = g.Zin + (size_t)row * g.ldc + col0;
-                bf16* dz = g.dZ + (size_t)row * g.ldc + col0;
+                    for (int i = 0; i < 32; i += 2) {
+                        const float z0 = v[i] + __ldg(g.bias + col0 + i), z1 = v[i + 1] + __ldg(g.bias + col0 + i + 1);
+                        const __nv_bfloat162 zb = __floats2bfloat162_rn(z0, z1);
+                        *reinterpret_cast<__nv_bfloat162*>(zo + i) = zb;
+                        const float2 zf = __bfloat1622float2(zb);   // GELU of the stored (rounded) pre-activation
+                        const __nv_bfloat162 hb = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
+                        *reinterpret_cast<__nv_bfloat162*>(ho + i) = hb;
+                        if (g.HoutT) {   // transposed copy [column][row] for the weight-gradient GEMMs
+                            g.HoutT[(size_t)(col0 + i) * g.ldt + row] = __low2bfloat16(hb);
+                            g.HoutT[(size_t)(col0 + i + 1) * g.ldt + row] = __high2bfloat16(hb);
+                        }
+                    }
+                } else {
+                    const bf16* zi = g.Zin + (size_t)row * g.ldc + col0;
+                    bf16* dz = g.dZ + (size_t)row * g.ldc + col0;
 #pragma unroll
-                for (int i = 0; i < 32; i += 2) {
-                    const float2 z = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(zi + i));
-                    *reinterpret_cast<__nv_bfloat162*>(dz + i) =
-                        __floats2bfloat162_rn(v[i] * gelu_grad(z.x), v[i + 1] * gelu_grad(z.y));
+                    for (int i = 0; i < 32; i += 2) {
+                        const float2 z = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(zi + i));
+                        const __nv_bfloat162 db = __floats2bfloat162_rn(v[i] * gelu_grad(z.x), v[i + 1] * gelu_grad(z.y));
+                        *reinterpret_cast<__nv_bfloat162*>(dz + i) = db;
+                        if (g.dZT) {
+                            g.dZT[(size_t)(col0 + i) * g.ldt + row] = __low2bfloat16(db);
+                            g.dZT[(size_t)(col0 + i + 1) * g.ldt + row] = __high2bfloat16(db);
+                        }
+                    }
                 }
             }
         }
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    if (abort_flag && threadIdx.x == 0) {
+        // tile loads issued but never waited for are still landing in this CTA's shared memory:
+        // wait for them (bounded) before the CTA exits
+        for (int c = n_consumed; c < n_issued; ++c) (void)tc::mbar_wait(tc::smem_addr(&full[c % kStages]), (c / kStages) & 1);
+    }
+    __syncthreads();
+    if (warp == 1) tc::tmem_dealloc(tmem, 256);
 }
 
-constexpr size_t kGemmSmem = 2 * (16384 + 32768);
+// [rows x cols] -> [cols x rows] (bf16), 32 x 32 tiles through shared memory
+__global__ void k_transpose_bf16(const bf16* __restrict__ src, int rows, int cols, int lds, bf16* __restrict__ dst,
+                                 int ldd) {
+    __shared__ bf16 t[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) t[i][threadIdx.x] = src[(size_t)r * lds + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) dst[(size_t)c * ldd + r] = t[threadIdx.x][i];
+    }
+}
+
+cudaError_t transpose_bf16(const bf16* src, int rows, int cols, int lds, bf16* dst, int ldd, cudaStream_t s) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    k_transpose_bf16<<<dim3((cols + 31) / 32, (rows + 31) / 32), dim3(32, 8), 0, s>>>(src, rows, cols, lds, dst, ldd);
+    return cudaGetLastError();
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// tensor map of a K-major bf16 operand [rows x K] (row stride ld elements), box 8 K x box_rows
+cudaError_t operand_map(CUtensorMap* map, const bf16* base, int rows, int K, int ld, int box_rows) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return cudaErrorNotSupported;
+    if (((uintptr_t)base & 15) || (ld * 2) % 16) return cudaErrorInvalidValue;
+    const cuuint64_t dim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t stride[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(base), dim, stride, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
 
 cudaError_t gemm(GemmArgs g, cudaStream_t s) {
     if (g.M % kBM || g.N % kBN || g.K % tc::kKChunk || g.K <= 0) return cudaErrorInvalidValue;
+    if (g.a_t || g.b_t) return cudaErrorInvalidValue;   // operands are K-major (transposed copies are made)
     if (g.ksplit <= 0) g.ksplit = g.K;
     if (g.K % g.ksplit || g.ksplit % tc::kKChunk) return cudaErrorInvalidValue;
     if (g.ksplit != g.K && g.epi != EPI_F32_ADD) return cudaErrorInvalidValue;
+    CUtensorMap ta, tb;
+    if (cudaError_t e = operand_map(&ta, g.A, g.M, g.K, g.lda, kBM)) return e;
+    if (cudaError_t e = operand_map(&tb, g.B, g.N, g.K, g.ldb, kBN)) return e;
     static std::atomic<unsigned long long> attr{0};
-    if (cudaError_t e = ensure_smem_attr(k_gemm, (int)kGemmSmem, attr)) return e;
+    if (cudaError_t e = ensure_smem_attr(k_gemm_tma, (int)kTmaSmem, attr)) return e;
     dim3 grid(g.N / kBN, g.M / kBM, g.K / g.ksplit);
-    k_gemm<<<grid, 128, kGemmSmem, s>>>(g);
+    k_gemm_tma<<<grid, kGemmThreads, kTmaSmem, s>>>(ta, tb, g);
     return cudaGetLastError();
 }
 
@@ -749,6 +857,11 @@ struct LearnedModel {
     bf16* Z[kLayers] = {};             // pre-activations [cap x 256]
     bf16* Hh[kLayers] = {};            // activations
     bf16* dZ[2] = {};                  // ping-pong gradients
+    // transposed copies, [column x cap]: the K-major operands of the weight-gradient GEMMs
+    bf16* XT = nullptr;                // features [512 x cap]
+    bf16* HT[kLayers - 1] = {};        // activations of layers 0-2 [256 x cap]
+    bf16* dZT = nullptr;               // the current layer's gradient [256 x cap]
+    bf16* wbfT = nullptr;              // weights of layers 1-3 transposed [in x out] (input gradients)
     float* y = nullptr;
     float* dy = nullptr;
     float* loss = nullptr;
@@ -777,8 +890,11 @@ struct LearnedModel {
         cudaFree(X);
         for (int l = 0; l < kLayers; ++l) { cudaFree(Z[l]); cudaFree(Hh[l]); Z[l] = Hh[l] = nullptr; }
         cudaFree(dZ[0]); cudaFree(dZ[1]);
+        cudaFree(XT); cudaFree(dZT); cudaFree(wbfT);
+        for (int l = 0; l < kLayers - 1; ++l) { cudaFree(HT[l]); HT[l] = nullptr; }
         cudaFree(y); cudaFree(dy); cudaFree(loss);
         X = nullptr; dZ[0] = dZ[1] = nullptr; y = dy = loss = nullptr;
+        XT = dZT = wbfT = nullptr;
         cap = 0;
     }
     ~LearnedModel() {
@@ -798,6 +914,10 @@ struct LearnedModel {
         }
         TRY(cudaMalloc(&dZ[0], (size_t)rows * kHidden * sizeof(bf16)));
         TRY(cudaMalloc(&dZ[1], (size_t)rows * kHidden * sizeof(bf16)));
+        TRY(cudaMalloc(&XT, (size_t)rows * kFeat * sizeof(bf16)));
+        for (int l = 0; l < kLayers - 1; ++l) TRY(cudaMalloc(&HT[l], (size_t)rows * kHidden * sizeof(bf16)));
+        TRY(cudaMalloc(&dZT, (size_t)rows * kHidden * sizeof(bf16)));
+        TRY(cudaMalloc(&wbfT, (size_t)(kLayers - 1) * kWh * sizeof(bf16)));
         TRY(cudaMalloc(&y, (size_t)rows * sizeof(float)));
         TRY(cudaMalloc(&dy, (size_t)rows * sizeof(float)));
         TRY(cudaMalloc(&loss, sizeof(float)));
@@ -830,6 +950,7 @@ struct LearnedModel {
             g.epi = EPI_FWD; g.ldc = kHidden;
             g.bias = params + b_offset(l);
             g.Zout = Z[l]; g.Hout = Hh[l];
+            if (l < kLayers - 1) { g.HoutT = HT[l]; g.ldt = cap; }
             TRY(gemm(g, s));
             in = Hh[l];
         }
@@ -844,13 +965,18 @@ struct LearnedModel {
         TRY(cudaGetLastError());
         k_out_wgrad<<<256, 256, 0, s>>>(dy, Hh[kLayers - 1], rows, grads);
         TRY(cudaGetLastError());
+        // K-major operands of the weight and input gradients: features and the top gradient
+        // transposed here, the hidden activations by the forward epilogue, the weights of layers 1-3
+        TRY(transpose_bf16(X, rows, kFeat, kFeat, XT, cap, s));
+        TRY(transpose_bf16(dZ[0], rows, kHidden, kHidden, dZT, cap, s));
+        for (int l = 1; l < kLayers; ++l)
+            TRY(transpose_bf16(wbf + w_offset(l), kHidden, kHidden, kHidden, wbfT + (size_t)(l - 1) * kWh, kHidden, s));
         int cur = 0;
         for (int l = kLayers - 1; l >= 0; --l) {
             // weight gradient: dW [out x in] = dZ^T . input  (K = rows)
-            const bf16* input = l == 0 ? X : Hh[l - 1];
             GemmArgs gw = base_args();
-            gw.A = dZ[cur]; gw.lda = kHidden; gw.a_t = 1;           // A[m=out][k=row] = dZ[row][out]
-            gw.B = input; gw.ldb = layer_in(l); gw.b_t = 1;         // B[n=in][k=row] = input[row][in]
+            gw.A = dZT; gw.lda = cap;                               // A[m=out][k=row] = dZ[row][out]
+            gw.B = l == 0 ? XT : HT[l - 1]; gw.ldb = cap;           // B[n=in][k=row] = input[row][in]
             gw.M = kHidden; gw.N = layer_in(l); gw.K = rows;
             gw.ksplit = split_k(rows);                              // split the batch across CTAs
             gw.epi = EPI_F32_ADD; gw.ldc = layer_in(l); gw.C32 = grads + w_offset(l);
@@ -860,11 +986,12 @@ struct LearnedModel {
             if (l == 0) break;
             // input gradient: dH = dZ . W, then times GELU'(Z[l-1])
             GemmArgs gx = base_args();
-            gx.A = dZ[cur]; gx.lda = kHidden; gx.a_t = 0;           // A[m=row][k=out]
-            gx.B = wbf + w_offset(l); gx.ldb = layer_in(l); gx.b_t = 1;   // B[n=in][k=out] = W[out][in]
+            gx.A = dZ[cur]; gx.lda = kHidden;                       // A[m=row][k=out]
+            gx.B = wbfT + (size_t)(l - 1) * kWh; gx.ldb = kHidden;  // B[n=in][k=out] = W[out][in]
             gx.M = rows; gx.N = layer_in(l); gx.K = kHidden;
             gx.epi = EPI_BWD; gx.ldc = kHidden;
             gx.Zin = Z[l - 1]; gx.dZ = dZ[cur ^ 1];
+            gx.dZT = dZT; gx.ldt = cap;                             // the next layer's weight-gradient operand
             TRY(gemm(gx, s));
             cur ^= 1;
         }
@@ -1169,18 +1296,32 @@ int rlc_tc_gemm(const void* d_a, const void* d_b, float* d_c, int M, int N, int 
     if (M <= 0 || N <= 0 || K <= 0 || M % kBM || N % kBN || K % tc::kKChunk)
         return lfail(RLC_ERR_ARG, "M must be a multiple of 128, N of 256, K of 64");
     unsigned* err = nullptr;
+    bf16 *at = nullptr, *bt = nullptr;   // K-major copies of transposed operands
+    const cudaStream_t s = (cudaStream_t)stream;
     LTRY(cudaMalloc(&err, sizeof(unsigned)), "gemm");
     cudaError_t e = cudaMemset(err, 0, sizeof(unsigned));
     GemmArgs g{};
-    g.A = (const bf16*)d_a; g.lda = a_t ? M : K; g.a_t = a_t;
-    g.B = (const bf16*)d_b; g.ldb = b_t ? N : K; g.b_t = b_t;
+    g.A = (const bf16*)d_a; g.lda = K;
+    g.B = (const bf16*)d_b; g.ldb = K;
+    if (e == cudaSuccess && a_t) {   // A given as [K x M]
+        e = cudaMalloc(&at, (size_t)M * K * sizeof(bf16));
+        if (e == cudaSuccess) e = transpose_bf16((const bf16*)d_a, K, M, M, at, K, s);
+        g.A = at;
+    }
+    if (e == cudaSuccess && b_t) {   // B given as [K x N]
+        e = cudaMalloc(&bt, (size_t)N * K * sizeof(bf16));
+        if (e == cudaSuccess) e = transpose_bf16((const bf16*)d_b, K, N, N, bt, K, s);
+        g.B = bt;
+    }
     g.M = M; g.N = N; g.K = K;
     g.epi = EPI_F32; g.ldc = N; g.C32 = d_c; g.err = err;
-    if (e == cudaSuccess) e = gemm(g, (cudaStream_t)stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e == cudaSuccess) e = gemm(g, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     unsigned h = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(unsigned), cudaMemcpyDeviceToHost);
     cudaFree(err);
+    cudaFree(at);
+    cudaFree(bt);
     if (e != cudaSuccess) return lfail(RLC_ERR_CUDA, "tensor-core gemm", e);
     if (h) return lfail(RLC_ERR_CUDA, "tensor-core GEMM timed out waiting for its MMAs");
     return RLC_OK;

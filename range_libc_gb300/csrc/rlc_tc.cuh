@@ -1,7 +1,7 @@
 // tcgen05 (5th-generation tensor core) building blocks for sm_103a, written
 // as inline PTX: shared-memory matrix descriptors, the kind::f16 instruction
 // descriptor, TMEM allocation, MMA issue/commit, mbarrier waits with a time
-// bound, and TMEM loads.
+// bound, TMEM loads, and TMA tile loads.
 //
 // Shared-memory operand layout used throughout (no swizzle, K-major): a tile
 // of R rows x 64 K (bf16) is stored as 8x8 "core matrices" of 128 contiguous
@@ -126,6 +126,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- TMA (cp.async.bulk.tensor) ---------------------------------------------
+// arrive on the mbarrier (count 1) and expect `bytes` of asynchronous copies to complete on it
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// 2-D tiled TMA load of the box at (x = innermost coordinate, y) of the tensor map into shared
+// memory at dst, completing `bytes` of transaction count on the mbarrier.  x times the element
+// size must be a multiple of 16 bytes; dst 128-byte aligned.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* tmap, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch_map(const void* tmap) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
 }
 
 }  // namespace tc
