@@ -97,7 +97,7 @@ __device__ __forceinline__ float gelu_grad(float z) {
 // C tile [128 x 256] at (blockIdx.y * 128, blockIdx.x * 256) of C = A . B^T, both operands
 // K-major in global memory (A[m * lda + k], B[n * ldb + k]), K range [z * ksplit, (z+1) * ksplit).
 //
-// Warp-specialised, one CTA per SM (192 threads, 4 pipeline stages of 48 KB):
+// Warp-specialised (192 threads, pipeline stages of 48 KB):
 //   warp 0     TMA producer: per 64-wide K chunk, 8 + 8 tile loads (one per group of 8 K
 //              elements: a 128- or 256-row x 16-byte box) into stage s, completing on full[s];
 //              it reuses a stage once the MMAs that read it have committed to empty[s];
@@ -111,13 +111,18 @@ __device__ __forceinline__ float gelu_grad(float z) {
 // then 128 bytes, the next one along M 128 bytes on (SBO) and along K 2048 bytes on (LBO); B the
 // same with 256 rows (LBO 4096).  Every wait is bounded (about a second); a time-out sets bit 16 of
 // *err, the remaining roles stop at their next wait, and the CTA still frees its TMEM.
-constexpr int kStages = 4;
+//
+// kStages = 4 (one CTA per SM) for the long-K weight gradients; 2 (two CTAs per SM, so that one
+// CTA's epilogue overlaps the other's loads and MMAs) for the short-K forward and input-gradient
+// GEMMs (K = 256 or 512).
 constexpr uint32_t kStageA = kBM * tc::kKChunk * 2;   // 16 KB
 constexpr uint32_t kStageB = kBN * tc::kKChunk * 2;   // 32 KB
-constexpr size_t kTmaSmem = kStages * (size_t)(kStageA + kStageB) + 1024;   // + alignment slack
+template <int kStages>
+constexpr size_t tma_smem() { return kStages * (size_t)(kStageA + kStageB) + 1024; }   // + alignment slack
 constexpr int kGemmThreads = 192;
 
-__global__ void __launch_bounds__(kGemmThreads, 1)
+template <int kStages>
+__global__ void __launch_bounds__(kGemmThreads, kStages <= 2 ? 2 : 1)
 k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accum;
@@ -208,39 +213,50 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
                     float* out = g.C32 + (size_t)row * g.ldc + col0;
 #pragma unroll
                     for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-                } else if (g.epi == EPI_F32_ADD) {
+                } else if (g.epi == EPI_F32_ADD) {   // split-K partial sums: 16-byte vector reductions
                     float* out = g.C32 + (size_t)row * g.ldc + col0;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) atomicAdd(out + i, v[i]);
+                    for (int i = 0; i < 32; i += 4)
+                        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(out + i), "f"(v[i]),
+                                     "f"(v[i + 1]), "f"(v[i + 2]), "f"(v[i + 3])
+                                     : "memory");
                 } else if (g.epi == EPI_FWD) {
-                    bf16* zo = g.Zout + (size_t)row * g.ldc + col0;
-                    bf16* ho = g.Hout + (size_t)row * g.ldc + col0;
+                    __nv_bfloat162 zp[16], hp[16];
 #pragma unroll
                     for (int i = 0; i < 32; i += 2) {
                         const float z0 = v[i] + __ldg(g.bias + col0 + i), z1 = v[i + 1] + __ldg(g.bias + col0 + i + 1);
-                        const __nv_bfloat162 zb = __floats2bfloat162_rn(z0, z1);
-                        *reinterpret_cast<__nv_bfloat162*>(zo + i) = zb;
-                        const float2 zf = __bfloat1622float2(zb);   // GELU of the stored (rounded) pre-activation
-                        const __nv_bfloat162 hb = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
-                        *reinterpret_cast<__nv_bfloat162*>(ho + i) = hb;
+                        zp[i / 2] = __floats2bfloat162_rn(z0, z1);
+                        const float2 zf = __bfloat1622float2(zp[i / 2]);   // GELU of the stored (rounded) pre-activation
+                        hp[i / 2] = __floats2bfloat162_rn(gelu(zf.x), gelu(zf.y));
                         if (g.HoutT) {   // transposed copy [column][row] for the weight-gradient GEMMs
-                            g.HoutT[(size_t)(col0 + i) * g.ldt + row] = __low2bfloat16(hb);
-                            g.HoutT[(size_t)(col0 + i + 1) * g.ldt + row] = __high2bfloat16(hb);
+                            g.HoutT[(size_t)(col0 + i) * g.ldt + row] = __low2bfloat16(hp[i / 2]);
+                            g.HoutT[(size_t)(col0 + i + 1) * g.ldt + row] = __high2bfloat16(hp[i / 2]);
                         }
+                    }
+                    uint4* zo = reinterpret_cast<uint4*>(g.Zout + (size_t)row * g.ldc + col0);
+                    uint4* ho = reinterpret_cast<uint4*>(g.Hout + (size_t)row * g.ldc + col0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        zo[q] = *reinterpret_cast<const uint4*>(zp + 4 * q);
+                        ho[q] = *reinterpret_cast<const uint4*>(hp + 4 * q);
                     }
                 } else {
-                    const bf16* zi = g.Zin + (size_t)row * g.ldc + col0;
-                    bf16* dz = g.dZ + (size_t)row * g.ldc + col0;
+                    const uint4* zi = reinterpret_cast<const uint4*>(g.Zin + (size_t)row * g.ldc + col0);
+                    __nv_bfloat162 zin[16], dp[16];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) *reinterpret_cast<uint4*>(zin + 4 * q) = zi[q];
 #pragma unroll
                     for (int i = 0; i < 32; i += 2) {
-                        const float2 z = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(zi + i));
-                        const __nv_bfloat162 db = __floats2bfloat162_rn(v[i] * gelu_grad(z.x), v[i + 1] * gelu_grad(z.y));
-                        *reinterpret_cast<__nv_bfloat162*>(dz + i) = db;
+                        const float2 z = __bfloat1622float2(zin[i / 2]);
+                        dp[i / 2] = __floats2bfloat162_rn(v[i] * gelu_grad(z.x), v[i + 1] * gelu_grad(z.y));
                         if (g.dZT) {
-                            g.dZT[(size_t)(col0 + i) * g.ldt + row] = __low2bfloat16(db);
-                            g.dZT[(size_t)(col0 + i + 1) * g.ldt + row] = __high2bfloat16(db);
+                            g.dZT[(size_t)(col0 + i) * g.ldt + row] = __low2bfloat16(dp[i / 2]);
+                            g.dZT[(size_t)(col0 + i + 1) * g.ldt + row] = __high2bfloat16(dp[i / 2]);
                         }
                     }
+                    uint4* dz = reinterpret_cast<uint4*>(g.dZ + (size_t)row * g.ldc + col0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) dz[q] = *reinterpret_cast<const uint4*>(dp + 4 * q);
                 }
             }
         }
@@ -322,10 +338,15 @@ cudaError_t gemm(GemmArgs g, cudaStream_t s) {
     CUtensorMap ta, tb;
     if (cudaError_t e = operand_map(&ta, g.A, g.M, g.K, g.lda, kBM)) return e;
     if (cudaError_t e = operand_map(&tb, g.B, g.N, g.K, g.ldb, kBN)) return e;
-    static std::atomic<unsigned long long> attr{0};
-    if (cudaError_t e = ensure_smem_attr(k_gemm_tma, (int)kTmaSmem, attr)) return e;
+    static std::atomic<unsigned long long> attr2{0}, attr4{0};
     dim3 grid(g.N / kBN, g.M / kBM, g.K / g.ksplit);
-    k_gemm_tma<<<grid, kGemmThreads, kTmaSmem, s>>>(ta, tb, g);
+    if (g.ksplit / tc::kKChunk > 8) {
+        if (cudaError_t e = ensure_smem_attr(k_gemm_tma<4>, (int)tma_smem<4>(), attr4)) return e;
+        k_gemm_tma<4><<<grid, kGemmThreads, tma_smem<4>(), s>>>(ta, tb, g);
+    } else {
+        if (cudaError_t e = ensure_smem_attr(k_gemm_tma<2>, (int)tma_smem<2>(), attr2)) return e;
+        k_gemm_tma<2><<<grid, kGemmThreads, tma_smem<2>(), s>>>(ta, tb, g);
+    }
     return cudaGetLastError();
 }
 
@@ -646,25 +667,52 @@ __global__ void k_out_backward(const float* __restrict__ dy, const bf16* __restr
     }
 }
 
-// output-layer gradients: d w_out[j] = sum_r dy[r] H[r][j], d b_out = sum_r dy[r]
-__global__ void k_out_wgrad(const float* __restrict__ dy, const bf16* __restrict__ H, int n, float* __restrict__ grads) {
-    const int col = threadIdx.x;   // 256 threads
-    float acc = 0.0f, accb = 0.0f;
-    for (int r = blockIdx.x; r < n; r += gridDim.x) {
-        const float g = dy[r];
-        acc += g * __bfloat162float(H[(size_t)r * kHidden + col]);
-        accb += g;
+// Column sums over rows of a [n x 256] bf16 matrix, each row weighted by w[r] (or 1): a block of
+// 128 threads covers the 256 columns two per thread (one 4-byte load per row), its rows strided by
+// the grid and four in flight per thread, then one atomic per column and block.
+constexpr int kColSumBlocks = 4 * 152;
+__device__ __forceinline__ void column_sums(const bf16* __restrict__ M, const float* __restrict__ w, int n,
+                                            float* __restrict__ out, float* __restrict__ wsum) {
+    const int c = 2 * threadIdx.x;
+    float a0 = 0.0f, a1 = 0.0f, s = 0.0f;
+    int r = blockIdx.x;
+    for (; r + 3 * (int)gridDim.x < n; r += 4 * gridDim.x) {
+        float2 v[4];
+        float g[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int ru = r + u * gridDim.x;
+            v[u] = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(M + (size_t)ru * kHidden + c));
+            g[u] = w ? __ldg(w + ru) : 1.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a0 += g[u] * v[u].x;
+            a1 += g[u] * v[u].y;
+            s += g[u];
+        }
     }
-    atomicAdd(grads + kOutW + col, acc);
-    if (col == 0) atomicAdd(grads + kOutW + kHidden, accb);
+    for (; r < n; r += gridDim.x) {
+        const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(M + (size_t)r * kHidden + c));
+        const float g = w ? __ldg(w + r) : 1.0f;
+        a0 += g * v.x;
+        a1 += g * v.y;
+        s += g;
+    }
+    atomicAdd(out + c, a0);
+    atomicAdd(out + c + 1, a1);
+    if (wsum && threadIdx.x == 0) atomicAdd(wsum, s);
+}
+
+// output-layer gradients: d w_out[j] = sum_r dy[r] H[r][j], d b_out = sum_r dy[r]
+__global__ void __launch_bounds__(128) k_out_wgrad(const float* __restrict__ dy, const bf16* __restrict__ H, int n,
+                                                   float* __restrict__ grads) {
+    column_sums(H, dy, n, grads + kOutW, grads + kOutW + kHidden);
 }
 
 // column sums of dZ [n x 256] -> bias gradient
-__global__ void k_bias_grad(const bf16* __restrict__ dZ, int n, float* __restrict__ gb) {
-    const int col = threadIdx.x;   // 256 threads
-    float acc = 0.0f;
-    for (int r = blockIdx.x; r < n; r += gridDim.x) acc += __bfloat162float(dZ[(size_t)r * kHidden + col]);
-    atomicAdd(gb + col, acc);
+__global__ void __launch_bounds__(128) k_bias_grad(const bf16* __restrict__ dZ, int n, float* __restrict__ gb) {
+    column_sums(dZ, nullptr, n, gb, nullptr);
 }
 
 // Adam (bias-corrected), fp32 master weights; refreshes the bf16 copies
@@ -963,7 +1011,7 @@ struct LearnedModel {
         TRY(cudaMemsetAsync(grads, 0, kParamCount * sizeof(float), s));
         k_out_backward<<<blocks_for((long long)rows * 32, 256), 256, 0, s>>>(dy, Z[kLayers - 1], params, rows, dZ[0]);
         TRY(cudaGetLastError());
-        k_out_wgrad<<<256, 256, 0, s>>>(dy, Hh[kLayers - 1], rows, grads);
+        k_out_wgrad<<<kColSumBlocks, 128, 0, s>>>(dy, Hh[kLayers - 1], rows, grads);
         TRY(cudaGetLastError());
         // K-major operands of the weight and input gradients: features and the top gradient
         // transposed here, the hidden activations by the forward epilogue, the weights of layers 1-3
@@ -981,7 +1029,7 @@ struct LearnedModel {
             gw.ksplit = split_k(rows);                              // split the batch across CTAs
             gw.epi = EPI_F32_ADD; gw.ldc = layer_in(l); gw.C32 = grads + w_offset(l);
             TRY(gemm(gw, s));
-            k_bias_grad<<<256, 256, 0, s>>>(dZ[cur], rows, grads + b_offset(l));
+            k_bias_grad<<<kColSumBlocks, 128, 0, s>>>(dZ[cur], rows, grads + b_offset(l));
             TRY(cudaGetLastError());
             if (l == 0) break;
             // input gradient: dH = dZ . W, then times GELU'(Z[l-1])
