@@ -423,6 +423,8 @@ def main():
     ap.add_argument("--workload", default="fused",
                     choices=["fused", "plain", "batch", "cddt", "learned", "glt", "radial", "published"])
     ap.add_argument("--train-rays", type=int, default=64_000_000, help="learned workload: training rays")
+    ap.add_argument("--train-batch", type=int, default=8192, help="learned workload: rays per training step")
+    ap.add_argument("--train-lr", type=float, default=2e-3, help="learned workload: Adam learning rate")
     ap.add_argument("--td", type=int, default=108, help="cddt workload: theta discretization")
     ap.add_argument("--prune", action="store_true", help="cddt workload: pruned table (PCDDT)")
     ap.add_argument("--filters", type=int, default=32, help="batch workload: number of filters")
@@ -1058,11 +1060,11 @@ def run_learned(args, emit=True):
     table = W.sensor_table(K)
     rm.set_sensor_model(table)
     model = rl.PyLearnedRM(rm, seed=1)
-    batch = 8192
+    batch = args.train_batch
     steps = max(1, args.train_rays // batch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    loss = model.train(steps=steps, batch=batch, lr=2e-3, seed=2)
+    loss = model.train(steps=steps, batch=batch, lr=args.train_lr, seed=2)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
 
@@ -1123,7 +1125,8 @@ def run_learned(args, emit=True):
         "data": "synthetic",
         "config": {"workload": "learned surrogate, 4096^2 rect/disk map, RM max_range 300 px, 10,000 particles x 108 "
                                "beams; MLP 512 Fourier features -> 4 x 256 GELU -> 1",
-                   "train_rays": steps * batch, "train_batch": batch, "train_s": train_s, "final_loss": loss},
+                   "train_rays": steps * batch, "train_batch": batch, "train_s": train_s, "final_loss": loss,
+                   "train_rays_per_s": steps * batch / train_s},
         "exact_repeat_angles_rays_per_s": rays * args.steps / (sum(te) / 1e3),
         "exact_fused_rays_per_s": rays * args.steps / (sum(tf) / 1e3),
         "learned_over_exact": (sum(te) / sum(tl)),

@@ -98,19 +98,18 @@ __device__ __forceinline__ float gelu_grad(float z) {
 // K-major in global memory (A[m * lda + k], B[n * ldb + k]), K range [z * ksplit, (z+1) * ksplit).
 //
 // Warp-specialised (192 threads, pipeline stages of 48 KB):
-//   warp 0     TMA producer: per 64-wide K chunk, 8 + 8 tile loads (one per group of 8 K
-//              elements: a 128- or 256-row x 16-byte box) into stage s, completing on full[s];
-//              it reuses a stage once the MMAs that read it have committed to empty[s];
+//   warp 0     TMA producer: per 64-wide K chunk, one tile load of A (128 rows x 128 bytes) and
+//              one of B (256 rows) into stage s, completing on full[s]; it reuses a stage once the
+//              MMAs that read it have committed to empty[s];
 //   warp 1     allocates 256 TMEM columns; one thread issues the chunk's four
 //              tcgen05.mma (K = 16 each) per stage and commits them to empty[s], and after the
 //              last chunk to `accum`;
 //   warps 2-5  epilogue: wait for `accum`, read the accumulator with tcgen05.ld (warp w reads
 //              TMEM lanes 32 (w % 4) .. + 31) and apply the epilogue.
-// Shared-memory operand layout (no swizzle, K-major): stage A holds 8 groups of 128 rows x
-// 16 bytes, group g (K elements 8g .. 8g + 7) at g * 2048; a core matrix (8 rows x 16 bytes) is
-// then 128 bytes, the next one along M 128 bytes on (SBO) and along K 2048 bytes on (LBO); B the
-// same with 256 rows (LBO 4096).  Every wait is bounded (about a second); a time-out sets bit 16 of
-// *err, the remaining roles stop at their next wait, and the CTA still frees its TMEM.
+// Shared-memory operand layout (K-major, 128-byte swizzle, as the TMA writes it): row r of a
+// stage's tile at r * 128 bytes with its 16-byte chunks permuted by r & 7 (tc::make_desc_sw128).
+// Every wait is bounded (about a second); a time-out sets bit 16 of *err, the remaining roles stop
+// at their next wait, and the CTA still frees its TMEM.
 //
 // kStages = 4 (one CTA per SM) for the long-K weight gradients; 2 (two CTAs per SM, so that one
 // CTA's epilogue overlaps the other's loads and MMAs) for the short-K forward and input-gradient
@@ -167,10 +166,8 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             const uint32_t fb = tc::smem_addr(&full[st]);
             tc::mbar_arrive_expect_tx(fb, kStageA + kStageB);
             const int k0 = kbase + c * tc::kKChunk;
-#pragma unroll
-            for (int gi = 0; gi < 8; ++gi) tc::tma_load_2d(stage_a(st) + gi * (kBM * 16), &tmA, k0 + gi * 8, m0, fb);
-#pragma unroll
-            for (int gi = 0; gi < 8; ++gi) tc::tma_load_2d(stage_b(st) + gi * (kBN * 16), &tmB, k0 + gi * 8, n0, fb);
+            tc::tma_load_2d(stage_a(st), &tmA, k0, m0, fb);
+            tc::tma_load_2d(stage_b(st), &tmB, k0, n0, fb);
             n_issued = c + 1;
         }
     } else if (warp == 1 && lane == 0) {
@@ -186,8 +183,8 @@ k_gemm_tma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUte
             tc::fence_after_sync();
 #pragma unroll
             for (int ks = 0; ks < tc::kKChunk / 16; ++ks) {
-                const uint64_t ad = tc::make_desc(stage_a(st) + ks * 2 * (kBM * 16), kBM * 16, tc::kCoreBytes);
-                const uint64_t bd = tc::make_desc(stage_b(st) + ks * 2 * (kBN * 16), kBN * 16, tc::kCoreBytes);
+                const uint64_t ad = tc::make_desc_sw128(stage_a(st) + ks * 32);
+                const uint64_t bd = tc::make_desc_sw128(stage_b(st) + ks * 32);
                 tc::mma_bf16(tmem, ad, bd, idesc, (c > 0 || ks > 0) ? 1u : 0u);
             }
             tc::mma_commit(tc::smem_addr(&empty[st]));
@@ -314,17 +311,18 @@ EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// tensor map of a K-major bf16 operand [rows x K] (row stride ld elements), box 8 K x box_rows
+// tensor map of a K-major bf16 operand [rows x K] (row stride ld elements): boxes of 64 K x
+// box_rows, 128-byte swizzled in shared memory
 cudaError_t operand_map(CUtensorMap* map, const bf16* base, int rows, int K, int ld, int box_rows) {
     EncodeTiledFn enc = encode_tiled();
     if (!enc) return cudaErrorNotSupported;
     if (((uintptr_t)base & 15) || (ld * 2) % 16) return cudaErrorInvalidValue;
     const cuuint64_t dim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
     const cuuint64_t stride[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)tc::kKChunk, (cuuint32_t)box_rows};   // 128-byte rows
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(base), dim, stride, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }

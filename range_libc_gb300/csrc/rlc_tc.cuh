@@ -40,6 +40,21 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
     return d;                 // base offset 0, layout type 0 (no swizzle)
 }
 
+// Descriptor of a K-major operand in the 128-byte swizzled layout that a TMA load with
+// CU_TENSOR_MAP_SWIZZLE_128B and a 64-element (128-byte) inner box writes: row r of the tile at
+// r * 128 bytes, its eight 16-byte chunks permuted by (chunk ^ (r & 7)); 8-row groups 1024 bytes
+// apart (SBO); the tile 1024-byte aligned.  Successive 16-element K steps start 32 bytes further
+// into the row (the hardware applies the swizzle to the resulting addresses).
+__device__ __forceinline__ uint64_t make_desc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                        // leading byte offset (unused by swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset: 8 rows x 128 bytes
+    d |= (uint64_t)1 << 46;                        // version
+    d |= (uint64_t)2 << 61;                        // 128-byte swizzle
+    return d;
+}
+
 // kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, M x N
 __host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
