@@ -71,7 +71,8 @@ struct rlc_map {
     uint16_t* d_dt16 = nullptr;
     uint8_t* d_dt8 = nullptr;
     float* d_step = nullptr;
-    uint32_t* d_step_runs = nullptr;   // the step map with unit-step runs (DT_RUNS)
+    uint16_t* d_runs_y = nullptr;   // unit-step runs of the step map (DT_RUNS)
+    uint16_t* d_runs_x = nullptr;
     std::atomic<int> refs{1};
     std::mutex mu;
 
@@ -82,7 +83,8 @@ struct rlc_map {
         cudaFree(d_dt16);
         cudaFree(d_dt8);
         cudaFree(d_step);
-        cudaFree(d_step_runs);
+        cudaFree(d_runs_y);
+        cudaFree(d_runs_x);
     }
     // distance transform on first use (RayMarching constructor, RangeLib.h:924)
     int ensure_dt() {
@@ -95,8 +97,7 @@ struct rlc_map {
         uint16_t* dt16 = nullptr;
         uint8_t* dt8 = nullptr;
         float* step = nullptr;
-        uint16_t *runs_y = nullptr, *runs_x = nullptr;   // scratch of the run lengths
-        uint32_t* step_runs = nullptr;
+        uint16_t *runs_y = nullptr, *runs_x = nullptr;
         void* scratch = nullptr;
         size_t sb = edt_scratch_bytes(W, H);
         cudaError_t e = cudaMalloc(&dt, (n ? n : 1) * sizeof(float));
@@ -106,25 +107,23 @@ struct rlc_map {
         if (e == cudaSuccess) e = cudaMalloc(&step, (n ? n : 1) * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc(&runs_y, (n ? n : 1) * sizeof(uint16_t));
         if (e == cudaSuccess) e = cudaMalloc(&runs_x, (n ? n : 1) * sizeof(uint16_t));
-        if (e == cudaSuccess) e = cudaMalloc(&step_runs, (n ? n : 1) * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMalloc(&scratch, sb);
         if (e == cudaSuccess) e = launch_edt(d_bits, W, H, TY, dt, scratch, sb, 0);
         if (e == cudaSuccess) e = launch_dt_to_tiled(dt, W, H, dtt, 0);
         if (e == cudaSuccess) e = launch_dt_to_u16(dt, W, H, dt16, 0);
         if (e == cudaSuccess) e = launch_dt_to_u8(dt, W, H, dt8, 0);
         if (e == cudaSuccess) e = launch_dt_to_step(dt, W, H, step, 0);
-        if (e == cudaSuccess) e = launch_step_runs(step, W, H, runs_y, runs_x, step_runs, 0);
+        if (e == cudaSuccess) e = launch_step_runs(step, W, H, runs_y, runs_x, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         cudaFree(scratch);
-        cudaFree(runs_y);
-        cudaFree(runs_x);
         if (e != cudaSuccess) {
             cudaFree(dt);
             cudaFree(dtt);
             cudaFree(dt16);
             cudaFree(dt8);
             cudaFree(step);
-            cudaFree(step_runs);
+            cudaFree(runs_y);
+            cudaFree(runs_x);
             return cuda_fail(e, "distance transform");
         }
         d_dt = dt;
@@ -132,7 +131,8 @@ struct rlc_map {
         d_dt16 = dt16;
         d_dt8 = dt8;
         d_step = step;
-        d_step_runs = step_runs;
+        d_runs_y = runs_y;
+        d_runs_x = runs_x;
         return RLC_OK;
     }
     void retain() { refs.fetch_add(1); }
@@ -211,7 +211,8 @@ struct rlc_method {
         p.map.dt16 = map->d_dt16;
         p.map.dt8 = map->d_dt8;
         p.map.step = map->d_step;
-        p.map.step_runs = map->d_step_runs;
+        p.map.runs_y = map->d_runs_y;
+        p.map.runs_x = map->d_runs_x;
         p.map.bits = map->d_bits;
         p.cddt.td = td;
         p.cddt.td_div_2pi = td_div_2pi;

@@ -74,8 +74,7 @@ __device__ __forceinline__ const void* dt_ptr(const MapDev& m, int x, int y) {
     if (LAYOUT == DT_U16) return m.dt16 + u16_index(m, x, y);
     if (LAYOUT == DT_TILED)
         return m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7);
-    if (LAYOUT == DT_RUNS) return m.step_runs + (size_t)x * m.H + y;
-    if (LAYOUT == DT_STEP) return m.step + (size_t)x * m.H + y;
+    if (LAYOUT == DT_STEP || LAYOUT == DT_RUNS) return m.step + (size_t)x * m.H + y;
     return m.dt + (size_t)x * m.H + y;
 }
 
@@ -112,11 +111,12 @@ constexpr int kMinRun = 4;
 // too, every one of them is a unit step in the grid, and t_J+1 < max_range keeps the reference's
 // loop going.  The march then resumes at t_J+1 having counted J steps, exactly where the reference's
 // loop is after J more iterations.  Returns t1 when no skip applies.
-__device__ __forceinline__ float unit_run_skip(float mr, float x0, float y0, float c, float s, int px, int py, int L,
-                                               float t1, int* steps) {
-    if (L < kMinRun) return t1;
+__device__ __forceinline__ float unit_run_skip(float mr, float x0, float y0, float c, float s, int px, int py,
+                                               unsigned rr, float t1, int* steps) {
     const bool ydom = fabsf(s) >= fabsf(c);
     const float dmaj = ydom ? s : c, dmin = ydom ? c : s;
+    const int L = dmaj > 0.0f ? (int)(rr & 255u) : (int)(rr >> 8);
+    if (L < kMinRun) return t1;
     const float o_maj = ydom ? y0 : x0, o_min = ydom ? x0 : y0;
     const int cmaj = ydom ? py : px, cmin = ydom ? px : py;
     // estimated parameter limits (the exact check below decides)
@@ -146,9 +146,8 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
     if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
     float t = 0.0f;
     if (!(t < mr)) return mr;
-    // DT_RUNS: which 7-bit run length of a unit-step cell lies along the ray (major axis, direction)
-    const bool ydom = fabsf(s) >= fabsf(c);
-    const unsigned run_shift = ydom ? (s > 0.0f ? 0u : 7u) : (c > 0.0f ? 14u : 21u);
+    // DT_RUNS: the runs along the ray's major axis, read beside the step (no added latency)
+    const uint16_t* runs = fabsf(s) >= fabsf(c) ? m.runs_y : m.runs_x;
     // one exit test per step: an off-grid position reads cell (0, 0) and leaves
     for (;;) {
         const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
@@ -163,16 +162,11 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
         // linear layouts form the cell index in 32 bits (W * H < 2^31) and select it once.
         constexpr bool kStepMap = LAYOUT == DT_STEP || LAYOUT == DT_RUNS;
         float d;
-        int run = 0;
-        if (LAYOUT == DT_RUNS) {   // one word: the step, or a unit step's run lengths
+        unsigned rr = 0u;
+        if (LAYOUT == DT_LINEAR || kStepMap) {
             const unsigned cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
-            const uint32_t w = __ldg(m.step_runs + cell);
-            const bool unit = (w >> 31) != 0u;
-            d = unit ? 1.0f : __uint_as_float(w);
-            run = unit ? (int)((w >> run_shift) & 127u) : 0;
-        } else if (LAYOUT == DT_LINEAR || LAYOUT == DT_STEP) {
-            const unsigned cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
-            d = __ldg((LAYOUT == DT_STEP ? m.step : m.dt) + cell);
+            d = __ldg((kStepMap ? m.step : m.dt) + cell);
+            if (LAYOUT == DT_RUNS) rr = __ldg(runs + cell);
         } else {
             d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
         }
@@ -187,7 +181,7 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
             return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
         }
         t = tn;
-        if (LAYOUT == DT_RUNS && run >= kMinRun) t = unit_run_skip(mr, x0, y0, c, s, px, py, run, t, steps);
+        if (LAYOUT == DT_RUNS && st == 1.0f) t = unit_run_skip(mr, x0, y0, c, s, px, py, rr, t, steps);
     }
 }
 

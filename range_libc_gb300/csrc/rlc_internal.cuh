@@ -45,11 +45,10 @@ struct MapDev {
     const uint16_t* dt16;     // compact squared distances (DT_U16)
     const uint8_t* dt8;       // 8-bit squared distances (DT_STAGED windows)
     const float* step;        // march step per cell, max(dt * 0.999, 1), 0 on occupied cells (DT_STEP, DT_RUNS)
-    // DT_RUNS: the step map with the unit-step cells (step 1.0) replaced by their run lengths: bit 31
-    // set, then 7 bits each (at most 127) for how many consecutive cells after the cell along +y,
-    // -y, +x and -x also have the unit step (bits 0-6, 7-13, 14-20, 21-27); other cells hold the
-    // step's float bits (0 on occupied cells, above 1 elsewhere)
-    const uint32_t* step_runs;
+    // DT_RUNS: per cell, how many consecutive cells after it along +y / -y (runs_y: low / high byte)
+    // and along +x / -x (runs_x) have the unit step 1.0 (at most 255)
+    const uint16_t* runs_y;
+    const uint16_t* runs_x;
     const uint64_t* bits;     // occupancy bit tiles
 };
 
@@ -107,10 +106,9 @@ cudaError_t launch_dt_to_tiled(const float* d_lin, int W, int H, float* d_tiled,
 cudaError_t launch_dt_to_u16(const float* d_lin, int W, int H, uint16_t* d_u16, cudaStream_t s);
 // the ray-marching step of every cell (linear layout), as RayMarching::calc_range forms it
 cudaError_t launch_dt_to_step(const float* d_lin, int W, int H, float* d_step, cudaStream_t s);
-// the step map with run lengths of its unit steps (MapDev::step_runs); runs_y and runs_x are
-// W * H scratch entries each
+// unit-step run lengths of the step map along both axes (MapDev::runs_y, runs_x)
 cudaError_t launch_step_runs(const float* d_step, int W, int H, uint16_t* d_runs_y, uint16_t* d_runs_x,
-                             uint32_t* d_step_runs, cudaStream_t s);
+                             cudaStream_t s);
 cudaError_t launch_dt_to_u8(const float* d_lin, int W, int H, uint8_t* d_u8, cudaStream_t s);
 cudaError_t launch_edge_map(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_edge, cudaStream_t s);
 cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_occ, cudaStream_t s);

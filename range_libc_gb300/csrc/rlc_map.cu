@@ -499,7 +499,7 @@ cudaError_t launch_dt_to_step(const float* d_lin, int W, int H, float* d_step, c
 }
 
 // Unit-step runs along y: one thread per column x walks the column both ways; runs_y[x * H + y]
-// = (cells y + 1, y + 2, ... with step 1.0, up to 127) | (cells y - 1, y - 2, ... << 8)
+// = (cells y + 1, y + 2, ... with step 1.0, up to 255) | (cells y - 1, y - 2, ... << 8)
 __global__ void k_step_runs_y(const float* __restrict__ step, int W, int H, uint16_t* __restrict__ runs) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= W) return;
@@ -508,12 +508,12 @@ __global__ void k_step_runs_y(const float* __restrict__ step, int W, int H, uint
     unsigned run = 0;   // -y: unit cells just below y
     for (int y = 0; y < H; ++y) {
         out[y] = (uint16_t)(run << 8);
-        run = col[y] == 1.0f ? min(run + 1u, 127u) : 0u;
+        run = col[y] == 1.0f ? min(run + 1u, 255u) : 0u;
     }
     run = 0;            // +y: unit cells just above y
     for (int y = H - 1; y >= 0; --y) {
         out[y] = (uint16_t)(out[y] | run);
-        run = col[y] == 1.0f ? min(run + 1u, 127u) : 0u;
+        run = col[y] == 1.0f ? min(run + 1u, 255u) : 0u;
     }
 }
 
@@ -525,41 +525,23 @@ __global__ void k_step_runs_x(const float* __restrict__ step, int W, int H, uint
     for (int x = 0; x < W; ++x) {
         const size_t i = (size_t)x * H + y;
         runs[i] = (uint16_t)(run << 8);
-        run = step[i] == 1.0f ? min(run + 1u, 127u) : 0u;
+        run = step[i] == 1.0f ? min(run + 1u, 255u) : 0u;
     }
     run = 0;
     for (int x = W - 1; x >= 0; --x) {
         const size_t i = (size_t)x * H + y;
         runs[i] = (uint16_t)(runs[i] | run);
-        run = step[i] == 1.0f ? min(run + 1u, 127u) : 0u;
+        run = step[i] == 1.0f ? min(run + 1u, 255u) : 0u;
     }
-}
-
-// one word per cell: the step's float bits, or for a unit step bit 31 and its four run lengths
-__global__ void k_pack_step_runs(const float* __restrict__ step, const uint16_t* __restrict__ ry,
-                                 const uint16_t* __restrict__ rx, long long n, uint32_t* __restrict__ out) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float v = step[i];
-    if (v != 1.0f) {
-        out[i] = __float_as_uint(v);
-        return;
-    }
-    const uint32_t y = ry[i], x = rx[i];
-    out[i] = 0x80000000u | (y & 127u) | ((y >> 8) & 127u) << 7 | (x & 127u) << 14 | ((x >> 8) & 127u) << 21;
 }
 
 cudaError_t launch_step_runs(const float* d_step, int W, int H, uint16_t* d_runs_y, uint16_t* d_runs_x,
-                             uint32_t* d_step_runs, cudaStream_t s) {
-    const long long n = (long long)W * H;
-    if (n == 0) return cudaSuccess;
+                             cudaStream_t s) {
+    if ((long long)W * H == 0) return cudaSuccess;
     k_step_runs_y<<<blocks_for(W, 128), 128, 0, s>>>(d_step, W, H, d_runs_y);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_step_runs_x<<<blocks_for(H, 128), 128, 0, s>>>(d_step, W, H, d_runs_x);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_pack_step_runs<<<blocks_for(n, 256), 256, 0, s>>>(d_step, d_runs_y, d_runs_x, n, d_step_runs);
     return cudaGetLastError();
 }
 
