@@ -111,10 +111,11 @@ constexpr int kMinRun = 4;
 // too, every one of them is a unit step in the grid, and t_J+1 < max_range keeps the reference's
 // loop going.  The march then resumes at t_J+1 having counted J steps, exactly where the reference's
 // loop is after J more iterations.  Returns t1 when no skip applies.
-__device__ __forceinline__ float unit_run_skip(float mr, float x0, float y0, float c, float s, int px, int py,
-                                               unsigned rr, float t1, int* steps) {
+__device__ __forceinline__ float unit_run_skip(const MapDev& m, float mr, float x0, float y0, float c, float s,
+                                               int px, int py, unsigned cell, float t1, int* steps) {
     const bool ydom = fabsf(s) >= fabsf(c);
     const float dmaj = ydom ? s : c, dmin = ydom ? c : s;
+    const unsigned rr = __ldg((ydom ? m.runs_y : m.runs_x) + cell);
     const int L = dmaj > 0.0f ? (int)(rr & 255u) : (int)(rr >> 8);
     if (L < kMinRun) return t1;
     const float o_maj = ydom ? y0 : x0, o_min = ydom ? x0 : y0;
@@ -146,8 +147,6 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
     if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
     float t = 0.0f;
     if (!(t < mr)) return mr;
-    // DT_RUNS: the runs along the ray's major axis, read beside the step (no added latency)
-    const uint16_t* runs = fabsf(s) >= fabsf(c) ? m.runs_y : m.runs_x;
     // one exit test per step: an off-grid position reads cell (0, 0) and leaves
     for (;;) {
         const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
@@ -162,11 +161,10 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
         // linear layouts form the cell index in 32 bits (W * H < 2^31) and select it once.
         constexpr bool kStepMap = LAYOUT == DT_STEP || LAYOUT == DT_RUNS;
         float d;
-        unsigned rr = 0u;
+        unsigned cell = 0u;
         if (LAYOUT == DT_LINEAR || kStepMap) {
-            const unsigned cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
+            cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
             d = __ldg((kStepMap ? m.step : m.dt) + cell);
-            if (LAYOUT == DT_RUNS) rr = __ldg(runs + cell);
         } else {
             d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
         }
@@ -181,7 +179,7 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
             return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
         }
         t = tn;
-        if (LAYOUT == DT_RUNS && st == 1.0f) t = unit_run_skip(mr, x0, y0, c, s, px, py, rr, t, steps);
+        if (LAYOUT == DT_RUNS && st == 1.0f) t = unit_run_skip(m, mr, x0, y0, c, s, px, py, cell, t, steps);
     }
 }
 
