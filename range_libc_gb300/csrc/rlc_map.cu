@@ -498,53 +498,6 @@ cudaError_t launch_dt_to_step(const float* d_lin, int W, int H, float* d_step, c
     return cudaGetLastError();
 }
 
-// Unit-step runs along y: one thread per column x walks the column both ways; runs_y[x * H + y]
-// = (cells y + 1, y + 2, ... with step 1.0, up to 255) | (cells y - 1, y - 2, ... << 8)
-__global__ void k_step_runs_y(const float* __restrict__ step, int W, int H, uint16_t* __restrict__ runs) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= W) return;
-    const float* col = step + (size_t)x * H;
-    uint16_t* out = runs + (size_t)x * H;
-    unsigned run = 0;   // -y: unit cells just below y
-    for (int y = 0; y < H; ++y) {
-        out[y] = (uint16_t)(run << 8);
-        run = col[y] == 1.0f ? min(run + 1u, 255u) : 0u;
-    }
-    run = 0;            // +y: unit cells just above y
-    for (int y = H - 1; y >= 0; --y) {
-        out[y] = (uint16_t)(out[y] | run);
-        run = col[y] == 1.0f ? min(run + 1u, 255u) : 0u;
-    }
-}
-
-// Unit-step runs along x: one thread per row y; runs_x[x * H + y] = (+x run) | (-x run << 8)
-__global__ void k_step_runs_x(const float* __restrict__ step, int W, int H, uint16_t* __restrict__ runs) {
-    const int y = blockIdx.x * blockDim.x + threadIdx.x;
-    if (y >= H) return;
-    unsigned run = 0;
-    for (int x = 0; x < W; ++x) {
-        const size_t i = (size_t)x * H + y;
-        runs[i] = (uint16_t)(run << 8);
-        run = step[i] == 1.0f ? min(run + 1u, 255u) : 0u;
-    }
-    run = 0;
-    for (int x = W - 1; x >= 0; --x) {
-        const size_t i = (size_t)x * H + y;
-        runs[i] = (uint16_t)(runs[i] | run);
-        run = step[i] == 1.0f ? min(run + 1u, 255u) : 0u;
-    }
-}
-
-cudaError_t launch_step_runs(const float* d_step, int W, int H, uint16_t* d_runs_y, uint16_t* d_runs_x,
-                             cudaStream_t s) {
-    if ((long long)W * H == 0) return cudaSuccess;
-    k_step_runs_y<<<blocks_for(W, 128), 128, 0, s>>>(d_step, W, H, d_runs_y);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_step_runs_x<<<blocks_for(H, 128), 128, 0, s>>>(d_step, W, H, d_runs_x);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_dt_to_u8(const float* d_lin, int W, int H, uint8_t* d_u8, cudaStream_t s) {
     int TY = (H + 7) >> 3, TX = (W + 7) >> 3;
     long long n = (long long)TX * TY * 64;
