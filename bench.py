@@ -508,8 +508,10 @@ def main():
     torch.cuda.synchronize()
     clocks.start()
     gpu_lead_in(torch)
+    flush.fill_(-1.0)
+    step()                                # untimed: the first step after the lead-in
     for k in range(args.steps):
-        flush.fill_(float(k))
+        flush.fill_(float(k + 1))
         starts[k].record(stream)
         launches += step()
         ends[k].record(stream)
@@ -647,7 +649,10 @@ def gpu_lead_in(torch, ms: float = 2.0):
     """Queue ~`ms` of GPU work (a spin kernel) ahead of a timed loop, so that the host has queued
     the loop's first steps before the GPU reaches them: a host-side pause (the clock sampler's
     NVML calls, the interpreter) then cannot leave the GPU idle between a step's start event and
-    its launch, which would count as step time.  Every step's work stays inside its events."""
+    its launch, which would count as step time.  Every step's work stays inside its events; the
+    callers run one more untimed step right after the lead-in (the first step after it ran up to
+    80 us slower) and fill the flush buffer with non-zero values (a zero fill may take another
+    path than the other steps')."""
     torch.cuda._sleep(int(ms * 1e-3 * 2.0e9))
 
 
@@ -658,8 +663,10 @@ def _event_steps(torch, stream, steps, flush, step_fn):
     launches = 0
     torch.cuda.synchronize()
     gpu_lead_in(torch)
+    flush.fill_(-1.0)
+    step_fn()                             # untimed: the first step after the lead-in
     for k in range(steps):
-        flush.fill_(float(k))
+        flush.fill_(float(k + 1))
         starts[k].record(stream)
         launches += step_fn()
         ends[k].record(stream)
