@@ -504,6 +504,7 @@ def main():
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     clocks = ClockSampler(dev_index)
     launches = 0
+    gpu_lead_in(torch, 0.0)               # loads the spin kernel before the timed region
     barrier(dist)
     torch.cuda.synchronize()
     clocks.start()
@@ -645,6 +646,9 @@ def north_star_figures(args, fused_value):
     return out
 
 
+_LEAD_IN_READY = False
+
+
 def gpu_lead_in(torch, ms: float = 2.0):
     """Queue ~`ms` of GPU work (a spin kernel) ahead of a timed loop, so that the host has queued
     the loop's first steps before the GPU reaches them: a host-side pause (the clock sampler's
@@ -653,6 +657,11 @@ def gpu_lead_in(torch, ms: float = 2.0):
     callers run one more untimed step right after the lead-in (the first step after it ran up to
     80 us slower) and fill the flush buffer with non-zero values (a zero fill may take another
     path than the other steps')."""
+    global _LEAD_IN_READY
+    if not _LEAD_IN_READY:   # the spin kernel's first launch loads its module (host time): not here
+        torch.cuda._sleep(1000)
+        torch.cuda.synchronize()
+        _LEAD_IN_READY = True
     torch.cuda._sleep(int(ms * 1e-3 * 2.0e9))
 
 

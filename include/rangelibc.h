@@ -217,7 +217,10 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
 /* ---- tuning ------------------------------------------------------------ */
 /* Schedule of the kernels: dt_layout 0 = linear x-major distance transform, 1 = 8x8 tiles,
  * 2 = compact 16-bit squared distances, 4 = linear map of each cell's march step
- * max(d * 0.999, 1) (0 on occupied cells), 3 = beam-major fused update that stages each bundle's
+ * max(d * 0.999, 1) (0 on occupied cells), 5 = that step map plus, per cell, how many cells after
+ * it along each axis have the same step, so that a ray repeating one step beside a wall skips the
+ * run in one go (exactly: the skipped steps' parameters are formed by the reference's own float
+ * additions and the landing cell is checked), 3 = beam-major fused update that stages each bundle's
  * window of 8-bit squared distances in shared memory (RM only; tile = particle chunks per beam,
  * 0 = one block per SM) (-1 = autotune on the next fused call); fused_block = threads per block of the fused kernel
  * (0 = keep); prefetch 1 = prefetch the distance transform ahead of each RM ray; for CDDT
@@ -283,7 +286,8 @@ typedef struct rlc_filter_desc {
 RLC_API int rlc_batch_create(const rlc_filter_desc* filters, int n_filters, int block, rlc_batch** out);
 RLC_API int rlc_batch_run(rlc_batch* b, void* stream);
 /* Schedule of the persistent launch: distance-transform layout (0 linear, 1 tiled, 2 compact
- * 16-bit, 4 step map) and prefetch of every ray-marching filter, threads per block, particles per tile
+ * 16-bit, 4 step map, 5 step map with equal-step runs) and prefetch of every ray-marching filter,
+ * threads per block, particles per tile
  * (0 = 32).  Results are identical under every schedule. */
 RLC_API int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile);
 RLC_API int rlc_batch_get_schedule(const rlc_batch* b, int* dt_layout, int* prefetch, int* block, int* tile);

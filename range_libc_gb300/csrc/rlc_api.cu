@@ -71,6 +71,7 @@ struct rlc_map {
     uint16_t* d_dt16 = nullptr;
     uint8_t* d_dt8 = nullptr;
     float* d_step = nullptr;
+    uint32_t* d_runs = nullptr;   // equal-step runs of the step map (DT_RUNS)
     std::atomic<int> refs{1};
     std::mutex mu;
 
@@ -81,6 +82,7 @@ struct rlc_map {
         cudaFree(d_dt16);
         cudaFree(d_dt8);
         cudaFree(d_step);
+        cudaFree(d_runs);
     }
     // distance transform on first use (RayMarching constructor, RangeLib.h:924)
     int ensure_dt() {
@@ -93,6 +95,7 @@ struct rlc_map {
         uint16_t* dt16 = nullptr;
         uint8_t* dt8 = nullptr;
         float* step = nullptr;
+        uint32_t* runs = nullptr;
         void* scratch = nullptr;
         size_t sb = edt_scratch_bytes(W, H);
         cudaError_t e = cudaMalloc(&dt, (n ? n : 1) * sizeof(float));
@@ -100,12 +103,14 @@ struct rlc_map {
         if (e == cudaSuccess) e = cudaMalloc(&dt16, (tiled ? tiled : 1) * sizeof(uint16_t));
         if (e == cudaSuccess) e = cudaMalloc(&dt8, (tiled ? tiled : 1) * sizeof(uint8_t));
         if (e == cudaSuccess) e = cudaMalloc(&step, (n ? n : 1) * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&runs, (n ? n : 1) * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMalloc(&scratch, sb);
         if (e == cudaSuccess) e = launch_edt(d_bits, W, H, TY, dt, scratch, sb, 0);
         if (e == cudaSuccess) e = launch_dt_to_tiled(dt, W, H, dtt, 0);
         if (e == cudaSuccess) e = launch_dt_to_u16(dt, W, H, dt16, 0);
         if (e == cudaSuccess) e = launch_dt_to_u8(dt, W, H, dt8, 0);
         if (e == cudaSuccess) e = launch_dt_to_step(dt, W, H, step, 0);
+        if (e == cudaSuccess) e = launch_step_runs(step, W, H, runs, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
         cudaFree(scratch);
         if (e != cudaSuccess) {
@@ -114,6 +119,7 @@ struct rlc_map {
             cudaFree(dt16);
             cudaFree(dt8);
             cudaFree(step);
+            cudaFree(runs);
             return cuda_fail(e, "distance transform");
         }
         d_dt = dt;
@@ -121,6 +127,7 @@ struct rlc_map {
         d_dt16 = dt16;
         d_dt8 = dt8;
         d_step = step;
+        d_runs = runs;
         return RLC_OK;
     }
     void retain() { refs.fetch_add(1); }
@@ -199,6 +206,7 @@ struct rlc_method {
         p.map.dt16 = map->d_dt16;
         p.map.dt8 = map->d_dt8;
         p.map.step = map->d_step;
+        p.map.runs = map->d_runs;
         p.map.bits = map->d_bits;
         p.cddt.td = td;
         p.cddt.td_div_2pi = td_div_2pi;
@@ -961,7 +969,7 @@ int rlc_count_steps(rlc_method* m, const float* ins, const float* angles, int n,
 
 int rlc_method_set_schedule(rlc_method* m, int dt_layout, int fused_block, int prefetch, int tile) {
     if (int rc = check_method(m)) return rc;
-    if (dt_layout < -1 || dt_layout > 4) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2, 3 or 4");
+    if (dt_layout < -1 || dt_layout > 5) return fail(RLC_ERR_ARG, "dt_layout must be -1, 0, 1, 2, 3, 4 or 5");
     if (fused_block != 0 && (fused_block < 32 || fused_block > 512 || fused_block % 32))
         return fail(RLC_ERR_ARG, "fused_block must be a multiple of 32 in [32, 512]");
     if (prefetch < 0 || prefetch > (m->dkind == K_CDDT ? 2 : 1))
@@ -1014,8 +1022,8 @@ int rlc_method_autotune_ex(rlc_method* m, const float* ins, const float* angles,
     const int blocks[3] = {128, 256, 512};
     const int tiles[3] = {0, 16, 32};
     const bool rm = m->dkind == K_RM;
-    static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
-    for (int lk = 0; lk < (rm ? 4 : 1); ++lk)
+    static const int kLayouts[5] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP, DT_RUNS};
+    for (int lk = 0; lk < (rm ? 5 : 1); ++lk)
         // march variants: RM plain / prefetching; CDDT binary / sector search
         for (int pk = 0; pk < (rm || m->dkind == K_CDDT ? 2 : 1); ++pk)
             for (int bi = 0; bi < 3; ++bi)
@@ -1333,8 +1341,8 @@ int rlc_batch_create(const rlc_filter_desc* fd, int nf, int block, rlc_batch** o
 
 int rlc_batch_set_schedule(rlc_batch* b, int dt_layout, int prefetch, int block, int tile) {
     if (!b) return fail(RLC_ERR_ARG, "null batch handle");
-    if (dt_layout < 0 || dt_layout > 4 || dt_layout == DT_STAGED)
-        return fail(RLC_ERR_ARG, "dt_layout must be 0, 1, 2 or 4");
+    if (dt_layout < 0 || dt_layout > 5 || dt_layout == DT_STAGED)
+        return fail(RLC_ERR_ARG, "dt_layout must be 0, 1, 2, 4 or 5");
     if (prefetch < 0 || prefetch > 1) return fail(RLC_ERR_ARG, "prefetch must be 0 or 1");
     if (block != 0 && (block < 32 || block > 512 || block % 32)) return fail(RLC_ERR_ARG, "block must be a multiple of 32 in [32, 512]");
     if (tile < 0 || tile > 512) return fail(RLC_ERR_ARG, "tile must be in [0, 512]");
@@ -1379,9 +1387,9 @@ int rlc_batch_autotune(rlc_batch* b, void* stream) {
     std::vector<Cand> cands;
     const int blocks[2] = {256, 512};
     const int tiles[3] = {8, 16, 32};
-    static const int kLayouts[4] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP};
+    static const int kLayouts[5] = {DT_LINEAR, DT_TILED, DT_U16, DT_STEP, DT_RUNS};
     for (int sp = 0; sp < 2; ++sp)
-        for (int lk = 0; lk < 4; ++lk)
+        for (int lk = 0; lk < 5; ++lk)
             for (int pf = 0; pf < 2; ++pf)
                 for (int bi = 0; bi < 2; ++bi)
                     for (int ti = 0; ti < 3; ++ti) {

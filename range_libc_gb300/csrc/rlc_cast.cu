@@ -65,7 +65,7 @@ __device__ __forceinline__ float dt_at(const MapDev& m, int x, int y) {
     }
     if (LAYOUT == DT_TILED)
         return __ldg(m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7));
-    if (LAYOUT == DT_STEP) return __ldg(m.step + (size_t)x * m.H + y);   // the step itself (0 on walls)
+    if (LAYOUT == DT_STEP || LAYOUT == DT_RUNS) return __ldg(m.step + (size_t)x * m.H + y);   // the step (0 on walls)
     return __ldg(m.dt + (size_t)x * m.H + y);
 }
 
@@ -74,7 +74,7 @@ __device__ __forceinline__ const void* dt_ptr(const MapDev& m, int x, int y) {
     if (LAYOUT == DT_U16) return m.dt16 + u16_index(m, x, y);
     if (LAYOUT == DT_TILED)
         return m.dt + (((size_t)(x >> 3) * m.tiles_y + (y >> 3)) << 6) + ((x & 7) << 3) + (y & 7);
-    if (LAYOUT == DT_STEP) return m.step + (size_t)x * m.H + y;
+    if (LAYOUT == DT_STEP || LAYOUT == DT_RUNS) return m.step + (size_t)x * m.H + y;
     return m.dt + (size_t)x * m.H + y;
 }
 
@@ -96,11 +96,58 @@ __device__ __forceinline__ bool occ_at(const MapDev& m, int x, int y) {
 // further along the ray.  Near walls the march advances ~1 px per step, so
 // the cell a later step reads is already on its way when that step starts;
 // the prefetch is a hint and never changes a result.
+//
+// DT_RUNS: the step map plus equal-step runs (run_skip below).
+constexpr int kMinRun = 4;
+
+// Exact skip over a run of equal steps (DT_RUNS).  A ray running beside a wall keeps the same
+// distance to it, so its march repeats one step value v for many iterations: the longest rays of
+// a particle-filter step repeat a step of 1 (one pixel) or 1.998 over a hundred times.  Once a
+// ray has taken two equal steps from cell (px, py), the run map says how many cells after it along
+// the ray's major axis (L, direction of travel) have step v too.  The march parameters of such a
+// run are known without reading a cell: t_j+1 = t_j + v rounded as the reference's addition.  An
+// estimate J of how many positions t_1 .. t_J stay in the box {the current row or column} x {the
+// run} is checked exactly at t_J with the march's own float operations; positions are monotone in
+// t, so every position before t_J lies in the box too -- a cell of step v in the grid -- and
+// t_J+1 < max_range keeps the reference's loop going.  The march then resumes at t_J+1 having
+// counted J steps, exactly where the reference's loop is after J more iterations.  Returns t1 (the
+// parameter after the current step) when no skip applies.
+__device__ __forceinline__ float run_skip(float mr, float x0, float y0, float c, float s, int px, int py, int L, float v,
+                                       float t1, int* steps) {
+    const bool ydom = fabsf(s) >= fabsf(c);
+    const float dmaj = ydom ? s : c, dmin = ydom ? c : s;
+    const float o_maj = ydom ? y0 : x0, o_min = ydom ? x0 : y0;
+    const int cmaj = ydom ? py : px, cmin = ydom ? px : py;
+    // estimated parameter limits (the exact check below decides)
+    float lim = (dmaj > 0.0f ? (float)(cmaj + L + 1) - o_maj : (float)(cmaj - L) - o_maj) / dmaj;
+    if (dmin > 0.0f) lim = fminf(lim, ((float)(cmin + 1) - o_min) / dmin);
+    else if (dmin < 0.0f) lim = fminf(lim, ((float)cmin - o_min) / dmin);
+    lim = fminf(lim, mr - v);
+    int J = (int)fminf((lim - t1) / v - 1.0f, 255.0f);
+    for (int attempt = 0; attempt < 3 && J >= 2; ++attempt, J >>= 1) {
+        float tj = t1;
+        for (int j = 1; j < J; ++j) tj = __fadd_rn(tj, v);
+        const int qx = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, tj)));
+        const int qy = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, tj)));
+        const int qmaj = ydom ? qy : qx, qmin = ydom ? qx : qy;
+        const bool in_run = dmaj > 0.0f ? (qmaj >= cmaj && qmaj <= cmaj + L) : (qmaj <= cmaj && qmaj >= cmaj - L);
+        const float tn = __fadd_rn(tj, v);
+        if (qmin == cmin && in_run && tn < mr) {
+            if (steps) *steps += J;
+            return tn;
+        }
+    }
+    return t1;
+}
+
 template <int LAYOUT, int PF = 0>
 __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps = nullptr) {
     if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
     float t = 0.0f;
     if (!(t < mr)) return mr;
+    // DT_RUNS: the byte of the run word that lies along the ray (major axis, direction of travel)
+    const unsigned run_shift = fabsf(s) >= fabsf(c) ? (s > 0.0f ? 0u : 8u) : (c > 0.0f ? 16u : 24u);
+    float prev = -1.0f;
     // one exit test per step: an off-grid position reads cell (0, 0) and leaves
     for (;;) {
         const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
@@ -113,15 +160,18 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
         }
         // DT_STEP reads the step max(d * 0.999, 1) precomputed per cell (0 where d = 0).  The
         // linear layouts form the cell index in 32 bits (W * H < 2^31) and select it once.
+        constexpr bool kStepMap = LAYOUT == DT_STEP || LAYOUT == DT_RUNS;
         float d;
-        if (LAYOUT == DT_LINEAR || LAYOUT == DT_STEP) {
-            const unsigned cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
-            d = __ldg((LAYOUT == DT_STEP ? m.step : m.dt) + cell);
+        unsigned cell = 0u;
+        if (LAYOUT == DT_LINEAR || kStepMap) {
+            cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
+            d = __ldg((kStepMap ? m.step : m.dt) + cell);
         } else {
             d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
         }
         if (steps && !out) ++*steps;
-        const float tn = __fadd_rn(t, LAYOUT == DT_STEP ? d : ref_maxf(__fmul_rn(d, 0.999f), 1.0f));
+        const float st = kStepMap ? d : ref_maxf(__fmul_rn(d, 0.999f), 1.0f);
+        const float tn = __fadd_rn(t, st);
         const bool hit = d <= 0.0f;
         if (out | hit | !(tn < mr)) {
             if (out || !hit) return mr;
@@ -130,6 +180,13 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
             return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
         }
         t = tn;
+        if (LAYOUT == DT_RUNS) {
+            if (st == prev) {   // two equal steps in a row: look for a run of them
+                const int L = (int)((__ldg(m.runs + cell) >> run_shift) & 255u);
+                if (L >= kMinRun) t = run_skip(mr, x0, y0, c, s, px, py, L, st, t, steps);
+            }
+            prev = st;
+        }
     }
 }
 
@@ -753,6 +810,8 @@ __device__ __forceinline__ float cast_ray(const CastParams& p, const float* __re
     if (KIND == kRmOnly) return cast_one<K_RM, LAYOUT, PF>(p, ax, ay, h, ray);   // every filter ray-marches
     // mixed kinds: dispatch at run time
     if (p.kind == K_RM) {
+        if (layout == DT_RUNS)
+            return pf ? cast_one<K_RM, DT_RUNS, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_RUNS, 0>(p, ax, ay, h, ray);
         if (layout == DT_STEP)
             return pf ? cast_one<K_RM, DT_STEP, kPrefetch>(p, ax, ay, h, ray) : cast_one<K_RM, DT_STEP, 0>(p, ax, ay, h, ray);
         if (layout == DT_U16)
@@ -1118,11 +1177,13 @@ template <template <int, int, int> class F, class... Args>
 cudaError_t dispatch(int kind, int layout, int pf, Args... args) {
     if (kind == K_RM) {
         if (pf) {
+            if (layout == DT_RUNS) return F<K_RM, DT_RUNS, kPrefetch>::run(args...);
             if (layout == DT_STEP) return F<K_RM, DT_STEP, kPrefetch>::run(args...);
             if (layout == DT_U16) return F<K_RM, DT_U16, kPrefetch>::run(args...);
             if (layout == DT_TILED) return F<K_RM, DT_TILED, kPrefetch>::run(args...);
             return F<K_RM, DT_LINEAR, kPrefetch>::run(args...);
         }
+        if (layout == DT_RUNS) return F<K_RM, DT_RUNS, 0>::run(args...);
         if (layout == DT_STEP) return F<K_RM, DT_STEP, 0>::run(args...);
         if (layout == DT_U16) return F<K_RM, DT_U16, 0>::run(args...);
         if (layout == DT_TILED) return F<K_RM, DT_TILED, 0>::run(args...);
@@ -1262,11 +1323,13 @@ template <bool SEP>
 static BatchKernel batch_kernel_t(bool rm_only, int layout, int pf) {
     if (!rm_only) return k_batch<kAnyKind, 0, 0, SEP>;
     if (pf) {
+        if (layout == DT_RUNS) return k_batch<kRmOnly, DT_RUNS, kPrefetch, SEP>;
         if (layout == DT_STEP) return k_batch<kRmOnly, DT_STEP, kPrefetch, SEP>;
         if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, kPrefetch, SEP>;
         if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, kPrefetch, SEP>;
         return k_batch<kRmOnly, DT_LINEAR, kPrefetch, SEP>;
     }
+    if (layout == DT_RUNS) return k_batch<kRmOnly, DT_RUNS, 0, SEP>;
     if (layout == DT_STEP) return k_batch<kRmOnly, DT_STEP, 0, SEP>;
     if (layout == DT_U16) return k_batch<kRmOnly, DT_U16, 0, SEP>;
     if (layout == DT_TILED) return k_batch<kRmOnly, DT_TILED, 0, SEP>;

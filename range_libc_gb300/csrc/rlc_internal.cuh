@@ -36,7 +36,7 @@ enum DevFlag : unsigned {
     F_NAN_INDEX = 8u,      // NaN range/observation mapped to sensor bin 0
 };
 
-enum DtLayout : int { DT_LINEAR = 0, DT_TILED = 1, DT_U16 = 2, DT_STAGED = 3, DT_STEP = 4 };
+enum DtLayout : int { DT_LINEAR = 0, DT_TILED = 1, DT_U16 = 2, DT_STAGED = 3, DT_STEP = 4, DT_RUNS = 5 };
 
 struct MapDev {
     int W, H;
@@ -44,7 +44,10 @@ struct MapDev {
     const float* dt;          // distance transform (DT_LINEAR / DT_TILED; linear for DT_U16)
     const uint16_t* dt16;     // compact squared distances (DT_U16)
     const uint8_t* dt8;       // 8-bit squared distances (DT_STAGED windows)
-    const float* step;        // march step per cell, max(dt * 0.999, 1), 0 on occupied cells (DT_STEP)
+    const float* step;        // march step per cell, max(dt * 0.999, 1), 0 on occupied cells (DT_STEP, DT_RUNS)
+    // DT_RUNS: per cell, how many consecutive cells after it have the same step value, along +y,
+    // -y, +x and -x (bits 0-7, 8-15, 16-23, 24-31; at most 255)
+    const uint32_t* runs;
     const uint64_t* bits;     // occupancy bit tiles
 };
 
@@ -102,6 +105,8 @@ cudaError_t launch_dt_to_tiled(const float* d_lin, int W, int H, float* d_tiled,
 cudaError_t launch_dt_to_u16(const float* d_lin, int W, int H, uint16_t* d_u16, cudaStream_t s);
 // the ray-marching step of every cell (linear layout), as RayMarching::calc_range forms it
 cudaError_t launch_dt_to_step(const float* d_lin, int W, int H, float* d_step, cudaStream_t s);
+// equal-step run lengths of the step map along both axes (MapDev::runs)
+cudaError_t launch_step_runs(const float* d_step, int W, int H, uint32_t* d_runs, cudaStream_t s);
 cudaError_t launch_dt_to_u8(const float* d_lin, int W, int H, uint8_t* d_u8, cudaStream_t s);
 cudaError_t launch_edge_map(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_edge, cudaStream_t s);
 cudaError_t launch_unpack_bits(const uint64_t* d_bits, int W, int H, int tiles_y, uint8_t* d_occ, cudaStream_t s);

@@ -498,6 +498,54 @@ cudaError_t launch_dt_to_step(const float* d_lin, int W, int H, float* d_step, c
     return cudaGetLastError();
 }
 
+// Equal-step runs along y: one thread per column x walks it both ways; bits 0-7 of runs[x * H + y]
+// count the cells y + 1, y + 2, ... whose step equals the step of (x, y), bits 8-15 the cells
+// y - 1, y - 2, ... (at most 255 each); bits 16-31 are cleared for the x pass.
+__global__ void k_step_runs_y(const float* __restrict__ step, int W, int H, uint32_t* __restrict__ runs) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const float* col = step + (size_t)x * H;
+    uint32_t* out = runs + (size_t)x * H;
+    unsigned run = 0;
+    for (int y = 1; y < H; ++y) {   // -y: run ending just below y
+        run = col[y - 1] == col[y] ? min(run + 1u, 255u) : 0u;
+        out[y] = run << 8;
+    }
+    out[0] = 0u;
+    run = 0;
+    for (int y = H - 2; y >= 0; --y) {   // +y
+        run = col[y + 1] == col[y] ? min(run + 1u, 255u) : 0u;
+        out[y] |= run;
+    }
+}
+
+// the same along x, one thread per row y: bits 16-23 (+x) and 24-31 (-x)
+__global__ void k_step_runs_x(const float* __restrict__ step, int W, int H, uint32_t* __restrict__ runs) {
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= H) return;
+    unsigned run = 0;
+    for (int x = 1; x < W; ++x) {
+        const size_t i = (size_t)x * H + y;
+        run = step[i - H] == step[i] ? min(run + 1u, 255u) : 0u;
+        runs[i] |= run << 24;
+    }
+    run = 0;
+    for (int x = W - 2; x >= 0; --x) {
+        const size_t i = (size_t)x * H + y;
+        run = step[i + H] == step[i] ? min(run + 1u, 255u) : 0u;
+        runs[i] |= run << 16;
+    }
+}
+
+cudaError_t launch_step_runs(const float* d_step, int W, int H, uint32_t* d_runs, cudaStream_t s) {
+    if ((long long)W * H == 0) return cudaSuccess;
+    k_step_runs_y<<<blocks_for(W, 128), 128, 0, s>>>(d_step, W, H, d_runs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_step_runs_x<<<blocks_for(H, 128), 128, 0, s>>>(d_step, W, H, d_runs);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_dt_to_u8(const float* d_lin, int W, int H, uint8_t* d_u8, cudaStream_t s) {
     int TY = (H + 7) >> 3, TX = (W + 7) >> 3;
     long long n = (long long)TX * TY * 64;

@@ -459,8 +459,9 @@ class _RangeMethod:
         return tot.value
 
     def set_schedule(self, dt_layout: int = 0, fused_block: int = 0, prefetch: int = 0, tile: int = 0) -> None:
-        """dt_layout 0 linear / 1 tiled / 2 compact 16-bit / 4 per-cell step map / 3 beam-major
-        update with staged 8-bit windows (-1: autotune on the next fused call), threads per block of the fused kernel
+        """dt_layout 0 linear / 1 tiled / 2 compact 16-bit / 4 per-cell step map / 5 step map with
+        equal-step runs (a ray beside a wall skips its repeated steps exactly) / 3 beam-major update
+        with staged 8-bit windows (-1: autotune on the next fused call), threads per block of the fused kernel
         (0 keeps it), prefetch (RM: 0 plain / 1 prefetching march; CDDT: 0 binary / 1 warp-cooperative /
         2 sector bin search), particles per tile (0 automatic; for layout 3 the particle
         chunks per beam).  Results do not depend on the schedule."""

@@ -149,7 +149,7 @@ def test_particle_filter_step_2048_4000x61(rl, oracle_mod, pf_full):
     w = np.empty(n, np.float64)
     r = np.empty(n * na, np.float32)
     we = np.empty(n, np.float64)
-    for sched in (tuned, (0, 0, 0, 0), (4, 0, 0, 0), (2, 0, 1, 0)):
+    for sched in (tuned, (0, 0, 0, 0), (4, 0, 0, 0), (5, 0, 0, 0), (2, 0, 1, 0)):
         meth.set_schedule(*sched)
         meth.set_trig_override(trig_libm)                     # parity mode
         meth.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, w)

@@ -203,7 +203,7 @@ def test_repeat_angles_parity(rl, oracle_mod, kind):
         g.calc_range_repeat_angles(ins, angles, out)
         assert np.array_equal(_bits(out), _bits(exp))
     if kind == "rm":     # every distance-transform layout, with and without prefetch
-        for layout in (0, 1, 2, 4):
+        for layout in (0, 1, 2, 4, 5):
             for pf in (0, 1):
                 g.set_schedule(layout, 0, pf, 0)
                 g.calc_range_repeat_angles(ins, angles, out)
@@ -252,7 +252,7 @@ def test_narrow_corridor_parity(rl, oracle_mod, mr):
     _, trig_a = oracle_mod.world_rays(m.world, ins, angles)
     obs = (np.linspace(1, 30, 31) % mr).astype(np.float32)
     exp_w = ref.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs)
-    for layout in (0, 1, 2, 4):
+    for layout in (0, 1, 2, 4, 5):
         for pf in (0, 1):
             g.set_schedule(layout, 0, pf, 0)
             g.set_trig_override(trig)
@@ -673,7 +673,8 @@ def test_batch_matches_per_filter_calls(rl, oracle_mod):
     batch = rl.PyFilterBatch(filters)
     rays, tiles = batch.info()
     assert rays == sum(len(f[1]) * len(f[2]) for f in filters) and tiles > 0
-    for sched in ((0, 0, 256, 0), (1, 1, 128, 8), (2, 1, 512, 32), (2, 0, 256, 3), (4, 0, 256, 32), "separate"):
+    for sched in ((0, 0, 256, 0), (1, 1, 128, 8), (2, 1, 512, 32), (2, 0, 256, 3), (4, 0, 256, 32), (5, 1, 256, 16),
+                  "separate"):
         if sched == "separate":
             batch.set_product_mode(True)
             assert batch.product_mode() == "separate"
@@ -713,7 +714,7 @@ def test_batch_of_ray_marchers_schedules(rl):
         filters.append((g, t[0], t[1], t[2], torch.zeros(len(wl.ins), dtype=torch.float64, device=dev)))
         keep.append(m)
     batch = rl.PyFilterBatch(filters)
-    for layout in (0, 1, 2, 4):
+    for layout in (0, 1, 2, 4, 5):
         for pf in (0, 1):
             batch.set_schedule(layout, pf, 256, 16)
             batch.run()
@@ -734,7 +735,7 @@ def test_results_do_not_depend_on_the_schedule(rl):
     g.set_schedule(0, 256, 0, 0)
     g.calc_range_repeat_angles_eval_sensor_model(wl.ins, wl.angles, wl.obs, base_w)
     g.calc_range_repeat_angles(wl.ins, wl.angles, base_r)
-    for layout in (0, 1, 2, 3, 4):
+    for layout in (0, 1, 2, 3, 4, 5):
         for pf in (0, 1):
             for block in (64, 128, 512):
                 for tile in (0, 1, 7, 32):
@@ -813,7 +814,7 @@ def test_count_steps_matches_oracle_under_every_schedule(rl, oracle_mod):
         _, trig = oracle_mod.world_rays(m.world, wl.ins, wl.angles)
         g.set_trig_override(trig)
         exp = ref.mean_steps(wl.ins, wl.angles) * len(wl.ins) * len(wl.angles)
-        for layout in ((0, 1, 2, 3, 4) if kind == "rm" else (0,)):
+        for layout in ((0, 1, 2, 3, 4, 5) if kind == "rm" else (0,)):
             g.set_schedule(layout, 0, 0, 0)
             assert g.count_steps(wl.ins, wl.angles) == round(exp), (kind, layout)
 
