@@ -98,13 +98,15 @@ __device__ __forceinline__ bool occ_at(const MapDev& m, int x, int y) {
 // the prefetch is a hint and never changes a result.
 //
 // DT_RUNS: the step map plus equal-step runs (run_skip below).
-constexpr int kMinRun = 4;
+constexpr int kMinRun = 16;       // shortest run worth a skip
+constexpr int kRunTrigger = 8;    // equal steps in a row before the run map is read
 
 // Exact skip over a run of equal steps (DT_RUNS).  A ray running beside a wall keeps the same
 // distance to it, so its march repeats one step value v for many iterations: the longest rays of
 // a particle-filter step repeat a step of 1 (one pixel) or 1.998 over a hundred times.  Once a
-// ray has taken two equal steps from cell (px, py), the run map says how many cells after it along
-// the ray's major axis (L, direction of travel) have step v too.  The march parameters of such a
+// ray has taken kRunTrigger equal steps in a row, at cell (px, py), the run map says how many
+// cells after it along the ray's major axis (L, direction of travel) have step v too (only then:
+// the read would lengthen the march of every other ray).  The march parameters of such a
 // run are known without reading a cell: t_j+1 = t_j + v rounded as the reference's addition.  An
 // estimate J of how many positions t_1 .. t_J stay in the box {the current row or column} x {the
 // run} is checked exactly at t_J with the march's own float operations; positions are monotone in
@@ -148,6 +150,7 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
     // DT_RUNS: the byte of the run word that lies along the ray (major axis, direction of travel)
     const unsigned run_shift = fabsf(s) >= fabsf(c) ? (s > 0.0f ? 0u : 8u) : (c > 0.0f ? 16u : 24u);
     float prev = -1.0f;
+    int rep = 0;   // equal steps in a row
     // one exit test per step: an off-grid position reads cell (0, 0) and leaves
     for (;;) {
         const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
@@ -181,11 +184,13 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
         }
         t = tn;
         if (LAYOUT == DT_RUNS) {
-            if (st == prev) {   // two equal steps in a row: look for a run of them
+            rep = st == prev ? rep + 1 : 0;
+            prev = st;
+            if (rep == kRunTrigger) {   // a ray repeating one step (beside a wall): look for the run
+                rep = 0;
                 const int L = (int)((__ldg(m.runs + cell) >> run_shift) & 255u);
                 if (L >= kMinRun) t = run_skip(mr, x0, y0, c, s, px, py, L, st, t, steps);
             }
-            prev = st;
         }
     }
 }
