@@ -218,7 +218,7 @@ RLC_API int rlc_count_steps(rlc_method* m, const float* ins, const float* angles
 /* Schedule of the kernels: dt_layout 0 = linear x-major distance transform, 1 = 8x8 tiles,
  * 2 = compact 16-bit squared distances, 4 = linear map of each cell's march step
  * max(d * 0.999, 1) (0 on occupied cells), 5 = that step map plus, per cell, how many cells after
- * it along each axis have the same step, so that a ray repeating one step beside a wall (8 times
+ * it along each axis have the same step, so that a ray repeating one step beside a wall (6 times
  * in a row) skips the rest of the run in one go (exactly: the skipped steps' parameters are formed by the reference's own float
  * additions and the landing cell is checked), 3 = beam-major fused update that stages each bundle's
  * window of 8-bit squared distances in shared memory (RM only; tile = particle chunks per beam,

@@ -98,8 +98,8 @@ __device__ __forceinline__ bool occ_at(const MapDev& m, int x, int y) {
 // the prefetch is a hint and never changes a result.
 //
 // DT_RUNS: the step map plus equal-step runs (run_skip below).
-constexpr int kMinRun = 16;       // shortest run worth a skip
-constexpr int kRunTrigger = 8;    // equal steps in a row before the run map is read
+constexpr int kMinRun = 12;       // shortest run worth a skip
+constexpr int kRunTrigger = 6;    // equal steps in a row before the run map is read
 
 // Exact skip over a run of equal steps (DT_RUNS).  A ray running beside a wall keeps the same
 // distance to it, so its march repeats one step value v for many iterations: the longest rays of
