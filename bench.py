@@ -296,6 +296,8 @@ FUSED_NCU_TRAFFIC = {
     0: (512_256, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"),
     4: (522_112, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, step map>, this workload "
                  "(mean of 2 launches: 521,984 and 522,240 B read, 0 written)"),
+    5: (564_608, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, step map with equal-step runs>, "
+                 "this workload (mean of 2 launches: 565,248 and 563,968 B read, 0 written)"),
 }
 BATCH_NCU_TRAFFIC = {
     6: (539_045_376 + 38_185_216, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
