@@ -392,6 +392,9 @@ __device__ __forceinline__ float cddt_front(const CastParams& p, float x, float 
     const float mr = p.mr;
     q.mode = 0;
     if (isnan(x) || isnan(y) || isnan(heading)) return mr;
+    // grid[x][y] with float indices: the cell under the query point.  It depends on the pose alone,
+    // so its read is issued first and overlaps the table reads below.
+    const bool occ = (x > -1.0f) && (y > -1.0f) && occ_at(p.map, __float2int_rz(x), __float2int_rz(y));
     int a;
     bool fl;
     cddt_discretize(c, -heading, a, fl, p.err);   // discretize_theta(-1.0 * heading)
@@ -407,8 +410,6 @@ __device__ __forceinline__ float cddt_front(const CastParams& p, float x, float 
     const int high = n - 1;
     if (high == -1) return mr;
     const float first = __ldg(bin), last = __ldg(bin + high);
-    // grid[x][y] with float indices: the cell under the query point
-    const bool occ = (x > -1.0f) && (y > -1.0f) && occ_at(p.map, __float2int_rz(x), __float2int_rz(y));
     q.bin = bin;
     q.n = n;
     q.lx = lx;
