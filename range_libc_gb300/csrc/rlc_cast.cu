@@ -326,14 +326,27 @@ __device__ __forceinline__ int bound_g(const float* __restrict__ bin, int n, flo
     return lo;
 }
 
-__device__ __forceinline__ int bound_s(const float* __restrict__ bin, int n, float v, bool upper) {
+// the aligned 32-byte sector around entry mid of a bin (two 16-byte reads)
+struct Sector {
+    float4 a, b;
+};
+__device__ __forceinline__ Sector sector_at(const float* __restrict__ bin, int mid) {
+    const float4* sec = reinterpret_cast<const float4*>(reinterpret_cast<uintptr_t>(bin + mid) & ~(uintptr_t)31);
+    return Sector{__ldg(sec), __ldg(sec + 1)};
+}
+
+// first: the sector of the first round (at n / 2), when the caller has already requested it
+__device__ __forceinline__ int bound_s(const float* __restrict__ bin, int n, float v, bool upper,
+                                      const Sector* first = nullptr) {
     int lo = 0, hi = n;
+    bool pre = first != nullptr;
     while (hi - lo > kSectorSearch) {
         const int mid = (lo + hi) >> 1;
         const uintptr_t pm = reinterpret_cast<uintptr_t>(bin + mid);
-        const float4* sec = reinterpret_cast<const float4*>(pm & ~(uintptr_t)31);
         const int s0 = mid - (int)((pm & 31) >> 2);   // index in the bin of the sector's first entry
-        const float4 a = __ldg(sec), b = __ldg(sec + 1);
+        const Sector sc = pre ? *first : sector_at(bin, mid);
+        pre = false;
+        const float4 a = sc.a, b = sc.b;
         const float z[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
         const int w0 = max(lo, s0), w1 = min(hi, s0 + 8);   // the sector's entries inside [lo, hi)
         int k = w1;                                          // first of them at or past the bound
@@ -385,8 +398,12 @@ struct CddtPending {
     int n;
     float lx;
     int mode;
+    Sector mid;   // SECTOR searches of bins longer than kSectorSearch: the first round's sector
 };
 
+// SECTOR: the sector search's first read (the sector at the bin's midpoint) is issued together with
+// the bin's first and last entries instead of after them
+template <bool SECTOR = false>
 __device__ __forceinline__ float cddt_front(const CastParams& p, float x, float y, float heading, CddtPending& q) {
     const CddtDev& c = p.cddt;
     const float mr = p.mr;
@@ -410,6 +427,7 @@ __device__ __forceinline__ float cddt_front(const CastParams& p, float x, float 
     const int high = n - 1;
     if (high == -1) return mr;
     const float first = __ldg(bin), last = __ldg(bin + high);
+    if (SECTOR && n > kSectorSearch) q.mid = sector_at(bin, n >> 1);
     q.bin = bin;
     q.n = n;
     q.lx = lx;
@@ -439,10 +457,11 @@ __device__ __forceinline__ float cddt_finish(const CastParams& p, const CddtPend
 template <bool SECTOR = false>
 __device__ float cddt_cast(const CastParams& p, float x, float y, float heading) {
     CddtPending q;
-    const float r = cddt_front(p, x, y, heading, q);
+    const float r = cddt_front<SECTOR>(p, x, y, heading, q);
     if (q.mode == 0) return r;
     const bool upper = q.mode != 3;
-    return cddt_finish(p, q, SECTOR ? bound_s(q.bin, q.n, q.lx, upper) : bound_g(q.bin, q.n, q.lx, upper));
+    return cddt_finish(p, q, SECTOR ? bound_s(q.bin, q.n, q.lx, upper, q.n > kSectorSearch ? &q.mid : nullptr)
+                                    : bound_g(q.bin, q.n, q.lx, upper));
 }
 
 // warp-cooperative variant: every lane resolves its own query up to the bin,
