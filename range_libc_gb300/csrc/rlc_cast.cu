@@ -718,13 +718,14 @@ __global__ void __launch_bounds__(256) k_repeat_angles(CastParams p, const float
 // ------------------------------------------------------------ sensor model
 // The weight of a particle is the product of its beams' table values in beam
 // order (RangeLib.h:533-555, 558-612), in double, exactly as the reference
-// multiplies -- so weights are bit-identical.  A tile holds P particles;
-// its rays store their 16-bit range bin in shared memory (sdi, particle-
-// major), the beams' observation bins are in sri, and the products run one
-// particle per lane: each double multiply instruction then serves up to 32
-// particles instead of one (the FP64 pipe spends the same time on a warp
-// instruction with one active lane as with 32).  Shared memory per block:
-// (P * na + na) * 2 bytes.
+// multiplies -- so weights are bit-identical.  A tile holds P particles
+// and the products run one particle per lane: each double multiply
+// instruction then serves up to 32 particles instead of one (the FP64 pipe
+// spends the same time on a warp instruction with one active lane as with
+// 32).  In eval_sensor_model's tiles the given ranges' 16-bit bins sit in
+// shared memory (sdi, particle-major) beside the beams' observation bins
+// (sri): (P * na + na) * 2 bytes per block; the fused update keeps each
+// ray's table factor instead (k_fused).
 struct TileSmem {
     uint16_t* sdi;   // [P * na] range bins
     uint16_t* sri;   // [na] observation bins
@@ -851,44 +852,41 @@ __device__ __forceinline__ float cast_ray(const CastParams& p, const float* __re
     return cast_one<K_CDDT, DT_LINEAR, 0>(p, ax, ay, h, ray);
 }
 
-// one tile of the fused update: cast P particles x na beams and bin them into ts.sdi
+// Fused update, one tile of P particles per block.  Each ray's thread casts the ray, bins it
+// and reads its table factor -- row: the beam's observation bin, column: the range bin -- into
+// shared memory (sf, particle-major, double); after the block's barrier the P particles' lanes
+// multiply their factors in beam order.  The factor reads run beside the other rays' marches,
+// one per ray, instead of as a chain of dependent groups after the barrier: in this one-wave
+// launch on a flushed L2 that chain sat on the step's critical path.  Shared memory per block:
+// P * na * 8 bytes.  The march kernels are held to 32 registers (the bounds' 4 blocks of 512
+// threads), so that a particle-filter step's blocks of 128 threads stay resident at 16 per SM
+// in one wave; the CDDT searches keep their registers.
 template <int KIND, int LAYOUT, int PF>
-__device__ __forceinline__ void tile_cast(const CastParams& p, const SensorDev& sm, const float* __restrict__ ins,
-                                          const float* __restrict__ angles, const float* __restrict__ obs,
-                                          float* __restrict__ ranges, int n, int na, int P, int first,
-                                          const TileSmem& ts, int layout, int pf) {
-    tile_obs_bins(p, sm, obs, na, ts.sri);
-    const int nr = P * na;
+__global__ void __launch_bounds__(512, KIND == K_CDDT ? 1 : 4) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
+                                               const float* __restrict__ angles, const float* __restrict__ obs,
+                                               double* __restrict__ weights, int n, int na, int P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* sf = reinterpret_cast<double*>(smem_raw);
+    const int first = blockIdx.x * P, nr = P * na;
     const float inv_na = __frcp_rn(__int2float_rn(na));
     for (int r = threadIdx.x; r < nr; r += blockDim.x) {
         const int li = div_small(r, na, inv_na), a = r - li * na, i = first + li;
         if (i < n) {
-            const float d = cast_ray<KIND, LAYOUT, PF>(p, ins, angles, i, a, na, layout, pf);
-            if (ranges) ranges[(size_t)i * na + a] = d;
-            ts.sdi[r] = (uint16_t)sensor_bin(d, sm.K, p.err);
+            const int ob = sensor_bin(__fmul_rn(__ldg(obs + a), p.world.inv_s), sm.K, p.err);
+            const float d = cast_ray<KIND, LAYOUT, PF>(p, ins, angles, i, a, na, LAYOUT, PF);
+            sf[r] = __ldg(sm.table + (size_t)ob * sm.K + sensor_bin(d, sm.K, p.err));
         }
     }
     __syncthreads();
-}
-
-// cast a tile, then multiply its particles' factors
-template <int KIND, int LAYOUT, int PF>
-__device__ __forceinline__ void fused_tile(const CastParams& p, const SensorDev& sm, const float* __restrict__ ins,
-                                           const float* __restrict__ angles, const float* __restrict__ obs,
-                                           double* __restrict__ weights, float* __restrict__ ranges, int n, int na,
-                                           int P, int first, const TileSmem& ts, int layout, int pf) {
-    tile_cast<KIND, LAYOUT, PF>(p, sm, ins, angles, obs, ranges, n, na, P, first, ts, layout, pf);
-    tile_products(sm, ts, na, P, first, n, weights);
-}
-
-// fused update, one tile of P particles per block
-template <int KIND, int LAYOUT, int PF>
-__global__ void __launch_bounds__(512) k_fused(CastParams p, SensorDev sm, const float* __restrict__ ins,
-                                               const float* __restrict__ angles, const float* __restrict__ obs,
-                                               double* __restrict__ weights, int n, int na, int P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    fused_tile<KIND, LAYOUT, PF>(p, sm, ins, angles, obs, weights, nullptr, n, na, P, blockIdx.x * P,
-                                 tile_layout(smem_raw, P, na), LAYOUT, PF);
+    for (int li = threadIdx.x; li < P; li += blockDim.x) {
+        const int i = first + li;
+        if (i >= n) continue;
+        const double* f = sf + (size_t)li * na;
+        double w = 1.0;
+#pragma unroll 8
+        for (int a = 0; a < na; ++a) w = __dmul_rn(w, f[a]);
+        weights[i] = w;
+    }
 }
 
 // ------------------------------------------------- persistent multi-filter
@@ -1244,13 +1242,14 @@ struct RunAngles {
 
 // particles per tile (P) and threads per block: P = tile if given, else the
 // most particles whose rays fit one ray per thread; P is capped so that the
-// tile's bins fit kTileSmem bytes
+// tile's per-ray entries (ray_bytes each: a 16-bit bin, or the fused update's
+// 8-byte factor) and the beams' 16-bit observation bins fit kTileSmem bytes
 constexpr size_t kTileSmem = 48 * 1024;
-inline void product_shape(int na, int block, int tile, int& P, int& threads) {
+inline void product_shape(int na, int block, int tile, int& P, int& threads, size_t ray_bytes = sizeof(uint16_t)) {
     if (block <= 0) block = 256;
     if (na <= 0) { P = block; threads = block; return; }   // empty product: weight 1.0
     P = tile > 0 ? tile : (na >= block ? 1 : block / na);
-    int cap = (int)((kTileSmem / sizeof(uint16_t) - (size_t)na) / (size_t)na);
+    int cap = (int)((kTileSmem - (size_t)na * sizeof(uint16_t)) / ((size_t)na * ray_bytes));
     if (cap < 1) cap = 1;
     if (P > cap) P = cap;
     int nr = P * na;
@@ -1270,8 +1269,8 @@ struct RunFused {
                            const float* obs, double* w, int n, int na, int block, int tile, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
         int P, threads;
-        product_shape(na, block, tile, P, threads);
-        size_t smem = tile_smem(P, na);
+        product_shape(na, block, tile, P, threads, sizeof(double));
+        const size_t smem = (size_t)P * na * sizeof(double);
         cudaError_t e = set_smem(k_fused<KIND, LAYOUT, PF>, smem);
         if (e != cudaSuccess) return e;
         k_fused<KIND, LAYOUT, PF><<<blocks_for(n, P), threads, smem, s>>>(p, sm, ins, angles, obs, w, n, na, P);
@@ -1311,7 +1310,7 @@ cudaError_t launch_fused(const CastParams& p, int layout, int pf, const SensorDe
 
 int tile_particles(int na, int block, int tile) {
     int P, threads;
-    product_shape(na, block, tile, P, threads);
+    product_shape(na, block, tile, P, threads, sizeof(double));
     return P;
 }
 
