@@ -293,11 +293,13 @@ def run_reference(args):
 # of the same workload (the k_fused and k_batch summaries under profiles/)
 # per distance-transform layout of the fused kernel (the schedules the autotuner picks here)
 FUSED_NCU_TRAFFIC = {
-    0: (512_256, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload"),
+    0: (512_256, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, linear DT>, this workload "
+                 "(the kernel version with 16-bit range bins in shared memory)"),
     4: (522_112, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, step map>, this workload "
-                 "(mean of 2 launches: 521,984 and 522,240 B read, 0 written)"),
-    5: (564_608, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, step map with equal-step runs>, "
-                 "this workload (mean of 2 launches: 565,248 and 563,968 B read, 0 written)"),
+                 "(mean of 2 launches: 521,984 and 522,240 B read, 0 written; the kernel version with 16-bit "
+                 "range bins in shared memory)"),
+    5: (566_400, "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_fused<RM, step map with equal-step runs>, "
+                 "this workload (mean of 2 launches: 566,528 and 566,272 B read, 0 written)"),
 }
 BATCH_NCU_TRAFFIC = {
     6: (539_045_376 + 38_185_216, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
@@ -511,8 +513,9 @@ def main():
     torch.cuda.synchronize()
     clocks.start()
     gpu_lead_in(torch)
-    flush.fill_(-1.0)
-    step()                                # untimed: the first step after the lead-in
+    for u in range(UNTIMED_AFTER_LEAD_IN):   # untimed: the first steps after the lead-in
+        flush.fill_(-1.0 - u)
+        step()
     for k in range(args.steps):
         flush.fill_(float(k + 1))
         starts[k].record(stream)
@@ -651,14 +654,18 @@ def north_star_figures(args, fused_value):
 _LEAD_IN_READY = False
 
 
+UNTIMED_AFTER_LEAD_IN = 3
+
+
 def gpu_lead_in(torch, ms: float = 2.0):
     """Queue ~`ms` of GPU work (a spin kernel) ahead of a timed loop, so that the host has queued
     the loop's first steps before the GPU reaches them: a host-side pause (the clock sampler's
     NVML calls, the interpreter) then cannot leave the GPU idle between a step's start event and
     its launch, which would count as step time.  Every step's work stays inside its events; the
-    callers run one more untimed step right after the lead-in (the first step after it ran up to
-    80 us slower) and fill the flush buffer with non-zero values (a zero fill may take another
-    path than the other steps')."""
+    callers run UNTIMED_AFTER_LEAD_IN untimed steps right after the lead-in (with one, the first
+    timed step still ran 5-25 us slower than the median in nearly every run of the particle-filter
+    step) and fill the flush buffer with non-zero values (a zero fill may take another path than
+    the other steps')."""
     global _LEAD_IN_READY
     if not _LEAD_IN_READY:   # the spin kernel's first launch loads its module (host time): not here
         torch.cuda._sleep(1000)
@@ -674,8 +681,9 @@ def _event_steps(torch, stream, steps, flush, step_fn):
     launches = 0
     torch.cuda.synchronize()
     gpu_lead_in(torch)
-    flush.fill_(-1.0)
-    step_fn()                             # untimed: the first step after the lead-in
+    for u in range(UNTIMED_AFTER_LEAD_IN):   # untimed: the first steps after the lead-in
+        flush.fill_(-1.0 - u)
+        step_fn()
     for k in range(steps):
         flush.fill_(float(k + 1))
         starts[k].record(stream)
