@@ -36,8 +36,8 @@ constexpr float kMPiUpF = 0x1.921fb6p+1f;
 constexpr float kMPiHiF = 0x1.921fb6p+1f;     // (float)M_PI
 constexpr float kMPiLoF = -0x1.777a5cp-24f;   // (float)(M_PI - kMPiHiF)
 constexpr int kPrefetch = 8;                        // RM prefetch distance (px) of the prefetching schedule
-constexpr int kAnyKind = -1;                        // fused_tile: kind, layout and prefetch chosen per filter
-constexpr int kRmOnly = -2;                         // fused_tile: every filter ray-marches (LAYOUT, PF given)
+constexpr int kAnyKind = -1;                        // k_batch: kind, layout and prefetch chosen per filter
+constexpr int kRmOnly = -2;                         // k_batch: every filter ray-marches (LAYOUT, PF given)
 
 __device__ __forceinline__ float ref_maxf(float a, float b) { return (a < b) ? b : a; }
 
