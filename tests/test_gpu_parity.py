@@ -640,6 +640,13 @@ def test_argument_errors(rl):
     g.set_sensor_model(np.ones((3, 4)))   # non-square: reference prints and returns
     with pytest.raises(rl._lib.RangeLibError):
         rl.PyCDDTCast(m, 50.0, 1)
+    with pytest.raises(rl._lib.RangeLibError):   # RM schedules: prefetch 0 or 1
+        g.set_schedule(0, 0, 2, 0)
+    c = rl.PyCDDTCast(m, 50.0, 16)
+    c.set_schedule(0, 0, 2, 0)                   # CDDT searches: 0 .. 2
+    with pytest.raises(rl._lib.RangeLibError):
+        c.set_schedule(0, 0, 3, 0)
+    assert c.schedule()[2] == 2
 
 
 def test_batch_matches_per_filter_calls(rl, oracle_mod):
