@@ -1248,7 +1248,8 @@ struct rlc_batch {
         int dev = 0, sms = 0, per_sm = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = batch_occupancy(block, 0, rm_only, layout, prefetch, separate, &per_sm);
+        smem = batch_smem(block, rm_only);
+        if (e == cudaSuccess) e = batch_occupancy(block, smem, rm_only, layout, prefetch, separate, &per_sm);
         if (e == cudaSuccess && per_sm <= 0) e = cudaErrorInvalidConfiguration;
         if (e == cudaSuccess && !d_filters) e = cudaMalloc(&d_filters, descs.size() * sizeof(FilterDev));
         if (e == cudaSuccess)
@@ -1259,7 +1260,6 @@ struct rlc_batch {
         nf = (int)hf.size();
         total_tiles = (unsigned)tiles;
         total_particles = (unsigned)parts;
-        smem = 0;
         long long g = (long long)sms * per_sm;
         if (g > (long long)tiles) g = (long long)tiles;
         grid = (int)(g > 0 ? g : 1);

@@ -142,20 +142,34 @@ __device__ __forceinline__ float run_skip(float mr, float x0, float y0, float c,
     return t1;
 }
 
-template <int LAYOUT, int PF = 0>
-__device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps = nullptr) {
-    if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
-    float t = 0.0f;
-    if (!(t < mr)) return mr;
+// A ray's march state (RangeLib.h:927-962): origin, direction, the parameter t, and for DT_RUNS
+// the last step and how many equal steps in a row ended with it; r is the caller's ray index.
+struct __align__(16) RmRay {
+    float x0, y0, c, s, t, prev;
+    int rep, r;
+};
+
+// Marches q from its parameter q.t.  BUDGETED: at most `budget` rounds of the loop (a run skip is
+// one round), after which it returns false with q holding the state of the next round, exactly
+// where the reference's loop stands; otherwise (and when the ray ends first) it returns true with
+// the range in *out.  One exit test per step: an off-grid position reads cell (0, 0) and leaves.
+template <int LAYOUT, int PF, bool BUDGETED>
+__device__ __forceinline__ bool rm_advance(const MapDev& m, float mr, RmRay& q, int budget, float* out, int* steps) {
+    const float x0 = q.x0, y0 = q.y0, c = q.c, s = q.s;
+    float t = q.t, prev = q.prev;
+    int rep = q.rep;   // equal steps in a row
     // DT_RUNS: the byte of the run word that lies along the ray (major axis, direction of travel)
     const unsigned run_shift = fabsf(s) >= fabsf(c) ? (s > 0.0f ? 0u : 8u) : (c > 0.0f ? 16u : 24u);
-    float prev = -1.0f;
-    int rep = 0;   // equal steps in a row
-    // one exit test per step: an off-grid position reads cell (0, 0) and leaves
-    for (;;) {
+    for (int round = 0;; ++round) {
+        if (BUDGETED && round >= budget) {
+            q.t = t;
+            q.prev = prev;
+            q.rep = rep;
+            return false;
+        }
         const int px = __float2int_rz(__fadd_rn(x0, __fmul_rn(c, t)));
         const int py = __float2int_rz(__fadd_rn(y0, __fmul_rn(s, t)));
-        const bool out = (unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H;
+        const bool out_of_grid = (unsigned)px >= (unsigned)m.W || (unsigned)py >= (unsigned)m.H;
         if (PF > 0) {
             const float tp = t + (float)PF;
             const int qx = __float2int_rz(x0 + c * tp), qy = __float2int_rz(y0 + s * tp);
@@ -167,20 +181,24 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
         float d;
         unsigned cell = 0u;
         if (LAYOUT == DT_LINEAR || kStepMap) {
-            cell = out ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
+            cell = out_of_grid ? 0u : (unsigned)px * (unsigned)m.H + (unsigned)py;
             d = __ldg((kStepMap ? m.step : m.dt) + cell);
         } else {
-            d = dt_at<LAYOUT>(m, out ? 0 : px, out ? 0 : py);
+            d = dt_at<LAYOUT>(m, out_of_grid ? 0 : px, out_of_grid ? 0 : py);
         }
-        if (steps && !out) ++*steps;
+        if (steps && !out_of_grid) ++*steps;
         const float st = kStepMap ? d : ref_maxf(__fmul_rn(d, 0.999f), 1.0f);
         const float tn = __fadd_rn(t, st);
         const bool hit = d <= 0.0f;
-        if (out | hit | !(tn < mr)) {
-            if (out || !hit) return mr;
-            const float xd = __fsub_rn(__int2float_rn(px), x0);
-            const float yd = __fsub_rn(__int2float_rn(py), y0);
-            return __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+        if (out_of_grid | hit | !(tn < mr)) {
+            if (out_of_grid || !hit) {
+                *out = mr;
+            } else {
+                const float xd = __fsub_rn(__int2float_rn(px), x0);
+                const float yd = __fsub_rn(__int2float_rn(py), y0);
+                *out = __fsqrt_rn(__fadd_rn(__fmul_rn(xd, xd), __fmul_rn(yd, yd)));
+            }
+            return true;
         }
         t = tn;
         if (LAYOUT == DT_RUNS) {
@@ -193,6 +211,17 @@ __device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c,
             }
         }
     }
+}
+
+// the march from t = 0; NaN arguments give max_range (the reference's loop never ends on them)
+template <int LAYOUT, int PF = 0>
+__device__ float rm_cast(const MapDev& m, float mr, float x0, float y0, float c, float s, int* steps = nullptr) {
+    if (isnan(x0) || isnan(y0) || isnan(c) || isnan(s)) return mr;
+    if (!(0.0f < mr)) return mr;
+    RmRay q{x0, y0, c, s, 0.0f, -1.0f, 0, 0};
+    float d = mr;
+    rm_advance<LAYOUT, PF, false>(m, mr, q, 0, &d, steps);
+    return d;
 }
 
 // ---------------------------------------------------- Bresenham's line (BL)
@@ -922,6 +951,101 @@ __device__ __forceinline__ void batch_products(const FilterDev& F, int tile, int
     }
 }
 
+// ray r of a tile: its range into the filter's ranges (if kept) and its bin into the tile's bins
+__device__ __forceinline__ void batch_store(const FilterDev& F, int first, uint16_t* bins, int r, float d) {
+    const int P = F.ppb, na = F.na;
+    const int li = div_small(r, na, F.inv_na), a = r - li * na;
+    if (F.ranges) F.ranges[(size_t)(first + li) * na + a] = d;
+    bins[((size_t)(a >> 2) * P + li) * 4 + (a & 3)] = (uint16_t)sensor_bin(d, F.sm.K, F.p.err);
+}
+
+// Ray (particle i, beam a) of a ray-marching filter at the start of its march: cast_ray's world
+// transform, heading and cos/sin (RangeLib.h:558-612, 927-931); r is the tile's index of the ray.
+__device__ __forceinline__ RmRay rm_ray_start(const CastParams& p, const float* __restrict__ ins,
+                                              const float* __restrict__ angles, int i, int a, int na, int r) {
+    float ax, ay, th;
+    world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1), __ldg(ins + 3 * (size_t)i + 2),
+                  ax, ay, th);
+    const long long ray = (long long)i * na + a;
+    const float h = __fsub_rn(th, __ldg(angles + a));
+    float c, s;
+    if (p.trig) {
+        c = p.trig[2 * ray];
+        s = p.trig[2 * ray + 1];
+    } else {
+        rlc_trig::sincos_cr(h, &s, &c);
+    }
+    return RmRay{ax, ay, c, s, 0.0f, -1.0f, 0, r};
+}
+
+// A tile's rays in a ray-marching batch, with a march budget.  A warp takes 32 rays at a time;
+// each lane marches its ray for at most kBatchBudget rounds, and rays that have not ended are
+// handed on: their march state goes to the warp's slots in shared memory, and whenever 32 are
+// waiting the warp marches them to their ends together.  A warp's time per 32 rays is its
+// slowest lane's; the handed-on rays -- the long ones -- now share warps with one another instead
+// of holding up 31 short ones (a CPU count over the uneven batch: 15 % fewer warp rounds at a
+// budget of 16; measured on the 32-filter batch: 3.09 -> 2.84 ms, against 2.87 / 2.92 / 2.99 ms
+// at budgets 12 / 10 / 8 and 2.85 / 3.22 ms at 20 / 24).  The saved state is the march's own
+// (RmRay), so every range is the one the uninterrupted march gives.
+constexpr int kBatchBudget = 16;   // march rounds before a ray is handed on
+constexpr int kBatchSlots = 64;    // handed-on rays a warp can hold (at most 31 + 32 wait at once)
+
+template <int LAYOUT, int PF>
+__device__ __forceinline__ void batch_cast_budgeted(const FilterDev& F, int first, int nr, uint16_t* bins,
+                                                    RmRay* slots, unsigned* next) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const CastParams& p = F.p;
+    int held = 0;        // handed-on rays in the warp's slots (the same in every lane)
+    bool fresh = true;   // the tile still hands out rays
+    for (;;) {
+        unsigned base = 0u;
+        if (fresh) {
+            if (lane == 0) base = atomicAdd(next, 32u);
+            base = __shfl_sync(full, base, 0);
+            fresh = base < (unsigned)nr;
+        }
+        if (!fresh) {   // the tile's rays are handed out: finish the warp's handed-on rays
+            if (held == 0) return;
+            const int take = min(held, 32);
+            __syncwarp();
+            if (lane < take) {
+                RmRay q = slots[held - take + lane];
+                float d = p.mr;
+                rm_advance<LAYOUT, PF, false>(p.map, p.mr, q, 0, &d, nullptr);
+                batch_store(F, first, bins, q.r, d);
+            }
+            held -= take;
+            continue;
+        }
+        const int r = (int)base + lane;
+        bool pending = false;
+        RmRay q;
+        if (r < nr) {
+            const int li = div_small(r, F.na, F.inv_na), a = r - li * F.na;
+            q = rm_ray_start(p, F.ins, F.angles, first + li, a, F.na, r);
+            float d = p.mr;
+            bool done = true;   // NaN arguments and max_range <= 0 give max_range (rm_cast)
+            if (!(isnan(q.x0) || isnan(q.y0) || isnan(q.c) || isnan(q.s)) && 0.0f < p.mr)
+                done = rm_advance<LAYOUT, PF, true>(p.map, p.mr, q, kBatchBudget, &d, nullptr);
+            if (done) batch_store(F, first, bins, r, d); else pending = true;
+        }
+        const unsigned pm = __ballot_sync(full, pending);
+        if (pending) slots[held + __popc(pm & below)] = q;
+        held += __popc(pm);
+        if (held >= 32) {   // 32 handed-on rays: march them to their ends together
+            __syncwarp();
+            RmRay h = slots[held - 32 + lane];
+            held -= 32;
+            __syncwarp();   // every lane has read its slot before the next rays land there
+            float d = p.mr;
+            rm_advance<LAYOUT, PF, false>(p.map, p.mr, h, 0, &d, nullptr);
+            batch_store(F, first, bins, h.r, d);
+        }
+    }
+}
+
 template <int MODE, int LAYOUT, int PF, bool SEPARATE>
 __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ filters, int nf, unsigned total_tiles,
                                                unsigned* __restrict__ queue) {
@@ -953,17 +1077,24 @@ __global__ void __launch_bounds__(512, 4) k_batch(const FilterDev* __restrict__ 
         const int tile = (int)(t - F.tile_begin), first = tile * P;
         const int nr = min(P, n - first) * na;
         uint16_t* bins = F.bins + batch_tile_offset(F, tile);
-        for (;;) {
-            unsigned base = 0u;
-            if (lane == 0) base = atomicAdd(&s_next, 32u);
-            base = __shfl_sync(full, base, 0);
-            if (base >= (unsigned)nr) break;
-            const int r = (int)base + lane;
-            if (r < nr) {
-                const int li = div_small(r, na, F.inv_na), a = r - li * na;
-                const float d = cast_ray<MODE, LAYOUT, PF>(F.p, F.ins, F.angles, first + li, a, na, F.layout, F.prefetch);
-                if (F.ranges) F.ranges[(size_t)(first + li) * na + a] = d;
-                bins[((size_t)(a >> 2) * P + li) * 4 + (a & 3)] = (uint16_t)sensor_bin(d, F.sm.K, F.p.err);
+        if (MODE == kRmOnly) {
+            extern __shared__ __align__(16) unsigned char smem_raw[];
+            batch_cast_budgeted<LAYOUT, PF>(F, first, nr, bins,
+                                            reinterpret_cast<RmRay*>(smem_raw) + (threadIdx.x >> 5) * kBatchSlots,
+                                            &s_next);
+        } else {
+            for (;;) {
+                unsigned base = 0u;
+                if (lane == 0) base = atomicAdd(&s_next, 32u);
+                base = __shfl_sync(full, base, 0);
+                if (base >= (unsigned)nr) break;
+                const int r = (int)base + lane;
+                if (r < nr) {
+                    const int li = div_small(r, na, F.inv_na), a = r - li * na;
+                    const float d =
+                        cast_ray<MODE, LAYOUT, PF>(F.p, F.ins, F.angles, first + li, a, na, F.layout, F.prefetch);
+                    batch_store(F, first, bins, r, d);
+                }
             }
         }
         __syncthreads();   // the tile's bins are written; s_tile, s_f and s_next may be reused
@@ -1410,6 +1541,10 @@ cudaError_t launch_cddt_radial(const CastParams& p, const float* ins, const floa
     if (total <= 0 || num_rays <= 0) return cudaSuccess;
     k_cddt_radial<<<blocks_for(total, 256), 256, 0, s>>>(p, ins, angles, outs, n, num_rays, mp, off, A);
     return cudaGetLastError();
+}
+
+size_t batch_smem(int block, bool rm_only) {
+    return rm_only ? (size_t)((block + 31) / 32) * kBatchSlots * sizeof(RmRay) : 0;
 }
 
 cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, bool separate,

@@ -205,6 +205,8 @@ inline size_t cddt_zeros_bytes(size_t nz) { return ((nz + 7) / 8 + (nz == 0)) * 
 cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tiles, unsigned* queue, int grid,
                          int block, size_t smem, bool rm_only, int layout, int pf, bool separate,
                          unsigned total_particles, cudaStream_t s);
+// dynamic shared memory of a batch launch (the ray-marching kernel's per-warp slots of handed-on rays)
+size_t batch_smem(int block, bool rm_only);
 cudaError_t batch_occupancy(int block, size_t smem, bool rm_only, int layout, int pf, bool separate,
                             int* blocks_per_sm);
 
