@@ -302,9 +302,10 @@ FUSED_NCU_TRAFFIC = {
                  "this workload (mean of 2 launches: 566,528 and 566,272 B read, 0 written)"),
 }
 BATCH_NCU_TRAFFIC = {
-    6: (539_045_376 + 38_185_216, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
-                                   "filters (--filters 6)"),
-    32: (2_615_891_200 + 407_052_544, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch, all 32 filters, "
+    6: (482_937_600 + 33_567_744, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
+                                   "filters (--filters 6), schedule step map / 256 threads / 8 particles per tile / "
+                                   "separate products"),
+    32: (2_661_218_816 + 405_684_480, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch, all 32 filters, "
                                       "schedule step map / 256 threads / 8 particles per tile / separate products"),
 }
 
