@@ -730,6 +730,62 @@ def test_batch_of_ray_marchers_schedules(rl):
                 assert np.array_equal(f[4].cpu().numpy(), w), (layout, pf)
 
 
+def test_batch_march_budget_edges(rl):
+    """The ray-marching batch hands rays that outlast their march budget on to full warps: corridor
+    maps whose wall-hugging rays march hundreds of rounds, NaN / infinite / far off-grid poses,
+    max_range below one step, beam counts that fill neither a warp nor a group of four, and tiles
+    of one particle give the per-filter calls' ranges and weights bit for bit, under every layout,
+    prefetch, block size, tile and product mode."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(77)
+    cases = []
+    for side, seed, n, na, mr in ((512, 31, 300, 61, 300.0), (256, 32, 41, 7, 150.0), (384, 33, 90, 129, 0.5),
+                                  (200, 34, 5, 1, 220.0)):
+        occ = W.corridor_map(side, seed)
+        ins = W.free_cell_queries(occ, n, seed)
+        if n >= 4:
+            ins[0] = (np.nan, 5.0, 0.0)
+            ins[1] = (5.0, 5.0, np.inf)
+            ins[2] = (1e9, -1e9, 0.3)
+        angles = W.laser_angles(na) if na > 1 else np.zeros(1, np.float32)
+        K = int(max(mr, 1.0)) + 1
+        table = W.sensor_table(K)
+        obs = rng.uniform(0, mr, na).astype(np.float32)
+        cases.append((occ, ins.astype(np.float32), angles.astype(np.float32), obs, table, mr))
+    filters, expect, keep = [], [], []
+    for occ, ins, angles, obs, table, mr in cases:
+        m = _pymap(rl, occ)
+        g = rl.PyRayMarching(m, mr)
+        g.set_sensor_model(table)
+        w = np.empty(len(ins), np.float64)
+        g.calc_range_repeat_angles_eval_sensor_model(ins, angles, obs, w)
+        r = np.empty(len(ins) * len(angles), np.float32)
+        g.calc_range_repeat_angles(ins, angles, r)
+        expect.append((w, r))
+        t = [torch.from_numpy(a).to(dev) for a in (ins, angles, obs)]
+        filters.append((g, t[0], t[1], t[2], torch.zeros(len(ins), dtype=torch.float64, device=dev),
+                        torch.zeros(len(ins) * len(angles), dtype=torch.float32, device=dev)))
+        keep.append(m)
+    assert np.mean(expect[0][1] == np.float32(300.0)) < 0.9   # the corridor's rays do meet walls
+    batch = rl.PyFilterBatch(filters)
+    for layout in (0, 4, 5):
+        for pf in (0, 1):
+            for block, tile in ((32, 1), (256, 8), (512, 3)):
+                for separate in (False, True):
+                    batch.set_schedule(layout, pf, block, tile)
+                    batch.set_product_mode(separate)
+                    for f in filters:
+                        f[4].fill_(-1.0)
+                        f[5].fill_(-1.0)
+                    batch.run()
+                    torch.cuda.synchronize()
+                    for f, (w, r) in zip(filters, expect):
+                        key = (layout, pf, block, tile, separate)
+                        assert np.array_equal(_bits(f[5].cpu().numpy()), _bits(r)), key
+                        assert np.array_equal(_bits(f[4].cpu().numpy()), _bits(w)), key
+
+
 def test_results_do_not_depend_on_the_schedule(rl):
     """Every schedule (DT layout x prefetch x block size x tile) gives bit-identical ranges and weights."""
     torch = pytest.importorskip("torch")
