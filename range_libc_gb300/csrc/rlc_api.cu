@@ -1158,6 +1158,7 @@ struct rlc_batch {
     uint16_t* d_bins = nullptr;   // every filter's range bins, tile by tile (batch_tile_bins)
     size_t bins_cap = 0;          // entries of d_bins
     uint16_t* d_obs_bins = nullptr;   // every filter's observation bins
+    float4* d_rec = nullptr;          // every filter's particle and beam records (FilterDev::part_rec, beam_rec)
     unsigned total_tiles = 0;
     unsigned total_particles = 0;
     long long rays = 0;
@@ -1181,6 +1182,7 @@ struct rlc_batch {
         cudaFree(d_queue);
         cudaFree(d_bins);
         cudaFree(d_obs_bins);
+        cudaFree(d_rec);
     }
 
     // (re)build the device filter table for the current schedule
@@ -1189,10 +1191,11 @@ struct rlc_batch {
         struct Item { FilterDev f; double cost; };
         std::vector<Item> items;
         const int ppb = tile > 0 ? tile : 32;   // 32 particles: one full lane set of the product warp
-        size_t need = 0, nobs = 0;
+        size_t need = 0, nobs = 0, nrec = 0;
         for (const rlc_filter_desc& d : descs) {
             need += (size_t)((d.n_particles + ppb - 1) / ppb) * batch_tile_bins(d.n_angles, ppb);
             nobs += (size_t)d.n_angles;
+            nrec += 2 * (size_t)d.n_particles + (size_t)d.n_angles;
         }
         if (need > bins_cap) {
             cudaFree(d_bins);
@@ -1202,7 +1205,8 @@ struct rlc_batch {
             bins_cap = need;
         }
         if (!d_obs_bins) CUDA_OR_FAIL(cudaMalloc(&d_obs_bins, (nobs ? nobs : 1) * sizeof(uint16_t)), "batch observation bins");
-        size_t bin_ofs = 0, obs_ofs = 0;
+        if (!d_rec) CUDA_OR_FAIL(cudaMalloc(&d_rec, (nrec ? nrec : 1) * sizeof(float4)), "batch particle and beam records");
+        size_t bin_ofs = 0, obs_ofs = 0, rec_ofs = 0;
         for (const rlc_filter_desc& d : descs) {
             rlc_method* m = d.method;
             Item it{};
@@ -1227,6 +1231,10 @@ struct rlc_batch {
             bin_ofs += (size_t)((d.n_particles + ppb - 1) / ppb) * batch_tile_bins(d.n_angles, ppb);
             it.f.obs_bins = d_obs_bins + obs_ofs;
             obs_ofs += (size_t)d.n_angles;
+            it.f.part_rec = d_rec + rec_ofs;
+            rec_ofs += 2 * (size_t)d.n_particles;
+            it.f.beam_rec = d_rec + rec_ofs;
+            rec_ofs += (size_t)d.n_angles;
             // heavier tiles first: rays per tile x march length
             it.cost = (double)it.f.ppb * (d.n_angles > 0 ? d.n_angles : 1) * (double)(m->mr > 1.0f ? m->mr : 1.0f);
             items.push_back(it);

@@ -959,23 +959,29 @@ __device__ __forceinline__ void batch_store(const FilterDev& F, int first, uint1
     bins[((size_t)(a >> 2) * P + li) * 4 + (a & 3)] = (uint16_t)sensor_bin(d, F.sm.K, F.p.err);
 }
 
-// Ray (particle i, beam a) of a ray-marching filter at the start of its march: cast_ray's world
-// transform, heading and cos/sin (RangeLib.h:558-612, 927-931); r is the tile's index of the ray.
-__device__ __forceinline__ RmRay rm_ray_start(const CastParams& p, const float* __restrict__ ins,
-                                              const float* __restrict__ angles, int i, int a, int na, int r) {
-    float ax, ay, th;
-    world_to_grid(p.world, __ldg(ins + 3 * (size_t)i), __ldg(ins + 3 * (size_t)i + 1), __ldg(ins + 3 * (size_t)i + 2),
-                  ax, ay, th);
-    const long long ray = (long long)i * na + a;
-    const float h = __fsub_rn(th, __ldg(angles + a));
+// Ray (particle i, beam a) of a ray-marching filter at the start of its march (RangeLib.h:558-612,
+// 927-931); r is the tile's index of the ray.  The particle's grid-frame pose comes from its
+// record; the ray's cos/sin from the caller's override, else from the float pairs of the particle
+// heading's and the beam angle's sin and cos (rlc_trig::sincos_diff: the correctly rounded values
+// of the ray's heading fl(th - a), for about a third of the instructions of computing them from
+// the heading), else -- where no pairs exist or their rounding is not certain -- from the heading.
+__device__ __forceinline__ RmRay rm_ray_start(const FilterDev& F, int i, int a, int r) {
+    const float4 pose = __ldg(F.part_rec + 2 * (size_t)i);
+    const float ang = __ldg(F.angles + a);
+    const float h = __fsub_rn(pose.z, ang);
     float c, s;
-    if (p.trig) {
-        c = p.trig[2 * ray];
-        s = p.trig[2 * ray + 1];
+    if (F.p.trig) {
+        const long long ray = (long long)i * F.na + a;
+        c = F.p.trig[2 * ray];
+        s = F.p.trig[2 * ray + 1];
     } else {
-        rlc_trig::sincos_cr(h, &s, &c);
+        const float4 pt = __ldg(F.part_rec + 2 * (size_t)i + 1), bt = __ldg(F.beam_rec + a);
+        if (isnan(pt.x) || isnan(bt.x) ||
+            !rlc_trig::sincos_diff(pose.z, ang, rlc_trig::F2{pt.x, pt.y}, rlc_trig::F2{pt.z, pt.w},
+                                   rlc_trig::F2{bt.x, bt.y}, rlc_trig::F2{bt.z, bt.w}, &s, &c))
+            rlc_trig::sincos_cr(h, &s, &c);
     }
-    return RmRay{ax, ay, c, s, 0.0f, -1.0f, 0, r};
+    return RmRay{pose.x, pose.y, c, s, 0.0f, -1.0f, 0, r};
 }
 
 // A tile's rays in a ray-marching batch, with a march budget.  A warp takes 32 rays at a time;
@@ -1024,7 +1030,7 @@ __device__ __forceinline__ void batch_cast_budgeted(const FilterDev& F, int firs
         RmRay q;
         if (r < nr) {
             const int li = div_small(r, F.na, F.inv_na), a = r - li * F.na;
-            q = rm_ray_start(p, F.ins, F.angles, first + li, a, F.na, r);
+            q = rm_ray_start(F, first + li, a, r);
             float d = p.mr;
             bool done = true;   // NaN arguments and max_range <= 0 give max_range (rm_cast)
             if (!(isnan(q.x0) || isnan(q.y0) || isnan(q.c) || isnan(q.s)) && 0.0f < p.mr)
@@ -1128,10 +1134,40 @@ __global__ void __launch_bounds__(256) k_batch_products(const FilterDev* __restr
 }
 
 // the observation bin of every beam of every filter, once per batch run (products read them)
-__global__ void k_batch_obs_bins(const FilterDev* __restrict__ filters) {
+// (ray-marching batches: and every beam's record -- the angle's sin and cos as float pairs)
+__global__ void k_batch_obs_bins(const FilterDev* __restrict__ filters, bool records) {
     const FilterDev& F = filters[blockIdx.x];
-    for (int a = threadIdx.x; a < F.na; a += blockDim.x)
+    for (int a = threadIdx.x; a < F.na; a += blockDim.x) {
         F.obs_bins[a] = (uint16_t)sensor_bin(__fmul_rn(__ldg(F.obs + a), F.p.world.inv_s), F.sm.K, F.p.err);
+        if (records) {
+            rlc_trig::F2 sn, cs;
+            F.beam_rec[a] = rlc_trig::sincos_pairs(__ldg(F.angles + a), &sn, &cs) ? make_float4(sn.h, sn.l, cs.h, cs.l)
+                                                                                    : make_float4(__int_as_float(0x7fc00000), 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
+// Every particle's record of a ray-marching batch, once per run: the world -> grid transform of
+// its pose (RangeLib.h:468-475) and, unless the filter has a trig override, its heading's sin and
+// cos as float pairs; one thread per particle of the batch.
+__global__ void __launch_bounds__(256) k_batch_particles(const FilterDev* __restrict__ filters, int nf,
+                                                         unsigned total_particles) {
+    const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total_particles) return;
+    int lo = 0, hi = nf - 1;   // last filter with part_begin <= g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (filters[mid].part_begin <= g) lo = mid; else hi = mid - 1;
+    }
+    const FilterDev& F = filters[lo];
+    const size_t i = g - F.part_begin;
+    float ax, ay, th;
+    world_to_grid(F.p.world, __ldg(F.ins + 3 * i), __ldg(F.ins + 3 * i + 1), __ldg(F.ins + 3 * i + 2), ax, ay, th);
+    F.part_rec[2 * i] = make_float4(ax, ay, th, 0.0f);
+    rlc_trig::F2 sn, cs;
+    F.part_rec[2 * i + 1] = !F.p.trig && rlc_trig::sincos_pairs(th, &sn, &cs)
+                                ? make_float4(sn.h, sn.l, cs.h, cs.l)
+                                : make_float4(__int_as_float(0x7fc00000), 0.0f, 0.0f, 0.0f);
 }
 
 
@@ -1562,9 +1598,14 @@ cudaError_t launch_batch(const FilterDev* d_filters, int nf, unsigned total_tile
     BatchKernel k = batch_kernel(rm_only, layout, pf, separate);
     cudaError_t e = set_smem(k, smem);
     if (e != cudaSuccess) return e;
-    k_batch_obs_bins<<<nf, 256, 0, s>>>(d_filters);
+    k_batch_obs_bins<<<nf, 256, 0, s>>>(d_filters, rm_only);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (rm_only && total_particles) {
+        k_batch_particles<<<blocks_for(total_particles, 256), 256, 0, s>>>(d_filters, nf, total_particles);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     k<<<grid, block, smem, s>>>(d_filters, nf, total_tiles, queue);
     e = cudaGetLastError();
     if (e != cudaSuccess || !separate || total_particles == 0) return e;

@@ -167,6 +167,12 @@ struct FilterDev {
     double* weights;
     uint16_t* bins;           // range bins (batch scratch), per tile beam-major in groups of 4 beams
     uint16_t* obs_bins;       // na observation bins (batch scratch, written at the start of each run)
+    // ray-marching batches (batch scratch, written at the start of each run): per particle two
+    // float4, {x, y, heading} in the grid frame and the heading's sin and cos as float pairs
+    // {sin hi, sin lo, cos hi, cos lo}; per beam the angle's sin and cos as float pairs.  A NaN
+    // sin hi marks a value without pairs (its rays compute their cos/sin directly).
+    float4* part_rec;
+    float4* beam_rec;
     int n, na, ppb;           // particles, beams, particles per tile
     float inv_na;             // 1 / (float)na rounded to nearest (tile ray -> particle, beam)
     unsigned tile_begin;      // first global tile of this filter

@@ -121,15 +121,9 @@ RLC_TRIG_HD bool rounds_safely(F2 v) {
     return fabsf(v.l) + ah * 0x1p-40f < half;
 }
 
-// Fast path: returns false where the double-precision fallback must decide.
-RLC_TRIG_HD bool sincos_fast(float x, float* sp, float* cp) {
-    const float ax = fabsf(x);
-    if (!(ax < 4096.0f)) return false;   // also NaN and infinities
-    if (ax < 0x1p-12f) {
-        *sp = x;
-        *cp = 1.0f;
-        return true;
-    }
+// Steps 2 and 3 for 2^-12 <= |x| < 4096: float pairs of sin and cos of the reduced argument
+// r = x - j pi/2, and j mod 4; false where the reduction's relative error grows.
+RLC_TRIG_HD bool sincos_reduced(float x, F2* sr_out, F2* cr_out, int* q_out) {
     // 2. reduction
     const float j = rintf(x * RLC_TRIG_TWO_OVER_PI);
     const F2 p0 = two_prod(j, RLC_TRIG_C0);
@@ -177,11 +171,84 @@ RLC_TRIG_HD bool sincos_fast(float x, float* sp, float* cp) {
     cc = fmaf(T.cl, q1, cc);
     cc = fmaf(T.ch, q1, cc);
     const F2 cr = fast_two_sum(ac.h, cc);
+    *sr_out = sr;
+    *cr_out = cr;
+    *q_out = (int)j & 3;
+    return true;
+}
+
+// Fast path: returns false where the double-precision fallback must decide.
+RLC_TRIG_HD bool sincos_fast(float x, float* sp, float* cp) {
+    const float ax = fabsf(x);
+    if (!(ax < 4096.0f)) return false;   // also NaN and infinities
+    if (ax < 0x1p-12f) {
+        *sp = x;
+        *cp = 1.0f;
+        return true;
+    }
+    F2 sr, cr;
+    int q;
+    if (!sincos_reduced(x, &sr, &cr, &q)) return false;
     if (!rounds_safely(sr) || !rounds_safely(cr)) return false;
-    const int q = (int)j & 3;
     const float s = sr.h, c = cr.h;
     *sp = (q == 0) ? s : (q == 1) ? c : (q == 2) ? -s : -c;
     *cp = (q == 0) ? c : (q == 1) ? -s : (q == 2) ? -c : s;
+    return true;
+}
+
+// sin(x) and cos(x) as float pairs within 2^-42 of the exact values (relative): the fast path's
+// values before their rounding, turned to x's quadrant.  False for |x| < 2^-12, |x| >= 4096,
+// NaN, infinities and where the reduction's relative error grows.
+RLC_TRIG_HD bool sincos_pairs(float x, F2* sp, F2* cp) {
+    const float ax = fabsf(x);
+    if (!(ax < 4096.0f) || ax < 0x1p-12f) return false;
+    F2 sr, cr;
+    int q;
+    if (!sincos_reduced(x, &sr, &cr, &q)) return false;
+    const F2 ns{-sr.h, -sr.l}, nc{-cr.h, -cr.l};
+    *sp = (q == 0) ? sr : (q == 1) ? cr : (q == 2) ? ns : nc;
+    *cp = (q == 0) ? cr : (q == 1) ? ns : (q == 2) ? nc : sr;
+    return true;
+}
+
+// true when h is the correctly rounded value of every number within 2^-39 of h + l (absolute;
+// h normal, |l| <= half an ulp of h)
+RLC_TRIG_HD bool rounds_safely_abs(F2 v) {
+    const float ah = fabsf(v.h);
+    const uint32_t b = bits_of(ah);
+    const float ulp = float_of(b & 0x7f800000u) * 0x1p-23f;
+    const float half = (b & 0x007fffffu) ? ulp * 0.5f : ulp * 0.25f;   // below a power of two: a quarter
+    return fabsf(v.l) + 0x1p-39f < half;
+}
+
+// The correctly rounded sin h and cos h of h = fl(th - a) from float pairs of sin and cos of th
+// (ps, pc) and of a (bs, bc), each within 2^-42 of its exact value (relative; sincos_pairs), or
+// false where the caller must compute them directly.  th - a = h + e exactly (two_sum), and
+//   sin h = sin(th - a) cos e - cos(th - a) sin e,   cos h = cos(th - a) cos e + sin(th - a) sin e,
+//   sin(th - a) = ps bc - pc bs,   cos(th - a) = pc bc + ps bs.
+// The products of the high parts are formed exactly, every other term (the products' errors, the
+// cross terms with the low parts, -e cos(th - a) and e sin(th - a)) is summed in one float.  For
+// |e| <= 2^-21 the results lie within 2^-40.2 of sin h and cos h: 2^-41 from the four inputs
+// (|sin th cos a| + |cos th sin a| <= 1), 2^-43 for the dropped e^2 / 2 terms, about 2^-42.2 for
+// the float sums of the low terms and the e terms, below 2^-47 for the dropped products of low
+// parts; rounds_safely_abs then allows for 2^-39.
+RLC_TRIG_HD bool sincos_diff(float th, float a, F2 ps, F2 pc, F2 bs, F2 bc, float* sp, float* cp) {
+    const F2 d = two_sum(th, -a);   // d.h = fl(th - a) = h
+    const float e = d.l;
+    if (!(fabsf(e) <= 0x1p-21f)) return false;
+    const F2 p1 = two_prod(ps.h, bc.h), p2 = two_prod(pc.h, bs.h);
+    const F2 p3 = two_prod(pc.h, bc.h), p4 = two_prod(ps.h, bs.h);
+    const F2 s0 = two_sum(p1.h, -p2.h), c0 = two_sum(p3.h, p4.h);
+    float sl = fmaf(ps.h, bc.l, fmaf(ps.l, bc.h, p1.l - p2.l));
+    sl = fmaf(-pc.h, bs.l, fmaf(-pc.l, bs.h, sl));
+    float cl = fmaf(pc.h, bc.l, fmaf(pc.l, bc.h, p3.l + p4.l));
+    cl = fmaf(ps.h, bs.l, fmaf(ps.l, bs.h, cl));
+    sl = fmaf(-e, c0.h, s0.l + sl);
+    cl = fmaf(e, s0.h, c0.l + cl);
+    const F2 S = two_sum(s0.h, sl), C = two_sum(c0.h, cl);
+    if (!rounds_safely_abs(S) || !rounds_safely_abs(C)) return false;
+    *sp = S.h;
+    *cp = C.h;
     return true;
 }
 

@@ -6,6 +6,9 @@
 //       often the fast path defers to the double fallback and how often the host libm's
 //       sinf/cosf differ from the correctly rounded values.
 //   trig_check eval            reads float32 arguments on stdin, writes (sin, cos) pairs
+//   trig_check diff N THREADS  N random (th, a) pairs per thread and family: sin and cos of
+//       fl(th - a) through rlc_trig::sincos_diff (float pairs of th's and a's sin and cos, the
+//       angle-difference formulas and a rounding check) against rlc_trig::sincos_cr, bit for bit
 // Compile with -ffp-contract=off (no contraction: the device build uses -fmad=false).
 #include "../../range_libc_gb300/csrc/rlc_trig.cuh"
 
@@ -28,8 +31,64 @@ int main(int argc, char** argv) {
         }
         return 0;
     }
+    if (argc >= 4 && !strcmp(argv[1], "diff")) {
+        const long per = strtol(argv[2], nullptr, 10);
+        const int nt = atoi(argv[3]) > 0 ? atoi(argv[3]) : 1;
+        std::atomic<long> n{0}, bad{0}, fallback{0}, nopair{0};
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t) {
+            th.emplace_back([&, t]() {
+                uint64_t st = 0x9E3779B97F4A7C15ull * (uint64_t)(t + 1);
+                auto next = [&]() {
+                    st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+                    return (double)(st >> 11) * 0x1p-53;
+                };
+                long ln = 0, lbad = 0, lfb = 0, lnp = 0;
+                for (long i = 0; i < per; ++i) {
+                    for (int fam = 0; fam < 4; ++fam) {
+                        float hd, an;
+                        if (fam == 0) {          // the workloads: grid headings, beams over 270 degrees
+                            hd = (float)(-12.0 + 14.0 * next());
+                            an = (float)(-2.4 + 4.8 * next());
+                        } else if (fam == 1) {   // wide arguments
+                            hd = (float)(-64.0 + 128.0 * next());
+                            an = (float)(-64.0 + 128.0 * next());
+                        } else if (fam == 2) {   // differences near multiples of pi / 2 (small sines or cosines)
+                            an = (float)(-3.0 + 6.0 * next());
+                            const int k = (int)(next() * 9.0) - 4;
+                            hd = (float)((double)an + k * 1.5707963267948966 + (next() - 0.5) * 1e-3);
+                        } else {                 // beams that nearly cancel the heading
+                            an = (float)(-3.0 + 6.0 * next());
+                            hd = an + (float)((next() - 0.5) * 0x1p-8);
+                        }
+                        rlc_trig::F2 ps, pc, bs, bc;
+                        ++ln;
+                        if (!rlc_trig::sincos_pairs(hd, &ps, &pc) || !rlc_trig::sincos_pairs(an, &bs, &bc)) {
+                            ++lnp;
+                            continue;
+                        }
+                        float s1, c1, s2, c2;
+                        if (!rlc_trig::sincos_diff(hd, an, ps, pc, bs, bc, &s1, &c1)) {
+                            ++lfb;
+                            continue;
+                        }
+                        rlc_trig::sincos_cr(hd - an, &s2, &c2);
+                        if (memcmp(&s1, &s2, 4) || memcmp(&c1, &c2, 4)) {
+                            if (lbad < 5) fprintf(stderr, "mismatch th=%a a=%a: %a %a vs %a %a\n", hd, an, s1, c1, s2, c2);
+                            ++lbad;
+                        }
+                    }
+                }
+                n += ln; bad += lbad; fallback += lfb; nopair += lnp;
+            });
+        }
+        for (auto& x : th) x.join();
+        printf("{\"n\": %ld, \"mismatch\": %ld, \"fallback\": %ld, \"no_pair\": %ld}\n", n.load(), bad.load(),
+               fallback.load(), nopair.load());
+        return bad.load() != 0;
+    }
     if (argc < 6 || strcmp(argv[1], "scan")) {
-        fprintf(stderr, "usage: trig_check scan LO HI STRIDE THREADS | trig_check eval\n");
+        fprintf(stderr, "usage: trig_check scan LO HI STRIDE THREADS | trig_check eval | trig_check diff N THREADS\n");
         return 2;
     }
     const float lo = strtof(argv[2], nullptr), hi = strtof(argv[3], nullptr);

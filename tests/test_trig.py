@@ -47,6 +47,20 @@ def test_host_build_is_correctly_rounded(trig_check):
     _scan(trig_check, -1e7, -4096, 100003)
 
 
+def test_difference_formula_is_correctly_rounded(trig_check):
+    """The batch's per-ray cos/sin from float pairs of the particle heading's and the beam angle's
+    sin and cos (rlc_trig::sincos_diff, with its rounding check) against the correctly rounded
+    values of fl(th - a), bit for bit, on 32 M random pairs: workload-like headings and beams, wide
+    arguments, differences near multiples of pi / 2 and beams that nearly cancel the heading (the
+    check then declines and the caller computes the values directly)."""
+    import json
+    nt = max(1, min(16, os.cpu_count() or 1))
+    out = subprocess.run([trig_check, "diff", str(8_000_000 // nt), str(nt)], capture_output=True, text=True)
+    res = json.loads(out.stdout)
+    assert out.returncode == 0 and res["mismatch"] == 0, (out.stdout, out.stderr[-2000:])
+    assert res["n"] >= 30_000_000 and res["fallback"] + res["no_pair"] < res["n"] // 2
+
+
 def _host_eval(exe, x):
     x = np.ascontiguousarray(x, np.float32)
     out = subprocess.run([exe, "eval"], input=x.tobytes(), capture_output=True, check=True)
