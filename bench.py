@@ -302,10 +302,10 @@ FUSED_NCU_TRAFFIC = {
                  "this workload (mean of 2 launches: 566,528 and 566,272 B read, 0 written)"),
 }
 BATCH_NCU_TRAFFIC = {
-    6: (482_937_600 + 33_567_744, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
+    6: (501_862_656 + 35_385_856, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch on the first 6 "
                                    "filters (--filters 6), schedule step map / 256 threads / 8 particles per tile / "
                                    "separate products"),
-    32: (2_661_218_816 + 405_684_480, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch, all 32 filters, "
+    32: (2_628_463_616 + 402_988_544, "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_batch, all 32 filters, "
                                       "schedule step map / 256 threads / 8 particles per tile / separate products"),
 }
 
