@@ -28,6 +28,12 @@
 //     below 2^-16 after a reduction, NaN, infinities) rounds the double
 //     precision sin and cos, whose error (a few units in the 53rd bit) can
 //     misround only arguments within ~2^-50 of a midpoint.
+//  6. sincos_diff: for a ray heading h = fl(th - a) whose th and a have float
+//     pairs of their sin and cos (sincos_pairs: the pairs of step 4 before
+//     rounding), the angle-difference formulas with an exact correction for
+//     the rounding of th - a give pairs within 2^-40.2 of sin h and cos h; a
+//     rounding check against 2^-39 (absolute) certifies their high parts as
+//     the values of sincos_cr, else the caller computes them directly.
 //
 // Every operation is written out (no contraction: the library is compiled
 // with -fmad=false and host checks with -ffp-contract=off), so the host and
