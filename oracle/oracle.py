@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE.
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
-import this module, as the checker (or as the timed CPU baseline).  Nothing in
+import this module, as the oracle that results are compared with (or as the timed CPU
+baseline).  Nothing in
 ``range_libc_gb300`` imports it.
 
 ``Oracle*`` classes wrap ``oracle/rlc_oracle.c`` (a plain-C restatement of the
@@ -202,7 +203,7 @@ class OracleMethod:
     kind: 'bl', 'rm', 'cddt', 'pcddt' (pruned at construction) or 'glt' (GiantLUTCast with td
     angle bins, built from the distance transform with ``nthreads`` threads).  fast=True runs the
     queries on the same restatement built with the reference's shipped flags (a speed baseline:
-    fast-math changes some results, so it is never the checker).
+    fast-math changes some results, so parity checks never use it).
     """
 
     def __init__(self, occ, kind: str, max_range: float, td: int = 108, world=None, nthreads: int = 1,

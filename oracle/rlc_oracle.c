@@ -2,7 +2,8 @@
  * CPU oracle for the range_libc ray-casting hot path -- TEST INFRASTRUCTURE.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
- * this file, always as the checker or as the timed CPU baseline.  It is a
+ * this file, always as the oracle that results are compared with or as the
+ * timed CPU baseline.  It is a
  * restatement in plain C of kctess5/range_libc (cited as RangeLib.h:<line>,
  * distance_transform.h:<line>, RangeUtils.h:<line>).  Build flags must keep
  * strict IEEE semantics: -O3 -ffp-contract=off (see oracle/Makefile).

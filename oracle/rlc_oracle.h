@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
  * algorithms (kctess5/range_libc, includes/RangeLib.h and the vendored
  * Felzenszwalb-Huttenlocher distance transform) that the test-suite, the
- * smoke check and the CPU-baseline leg of bench.py use as the checker.
+ * smoke check and the CPU-baseline leg of bench.py compare results with.
  * Nothing in the shipped library links or calls it.
  *
  * Parity is pinned two ways: against golden vectors produced by the

@@ -20,7 +20,7 @@ Two modes are checked for the casts that take a per-ray cos/sin (BL, RM):
     Its ranges and weights must be bit-identical to the oracle fed those same values, and
     against the oracle with the host libm (the reference's own result on this host) every
     differing ray or particle must be one whose cos/sin differ between the two.  The counts are
-    printed ("PARITY ..." lines, pytest -s): the benchmark spec's tolerances (hit cells exact, RM
+    printed ("PARITY ..." lines, pytest -s): the target tolerances (hit cells exact, RM
     within 1e-4 px, weights within 1e-6 relative) hold on every other ray and particle.
 
 CDDT needs only the cos/sin of its slice angles, which both sides take from the host libm, so
